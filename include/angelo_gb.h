@@ -1,0 +1,182 @@
+/*
+ * angelo_gb.h -- C ABI of libangelo_gb.so, the sm_103a (GB300) kernels of the
+ * NeuS / Neuralangelo hot path of Instant-angelo.
+ *
+ * Conventions
+ *   - Every entry point is extern "C", takes plain device pointers, element
+ *     counts and a cudaStream_t passed as void*, and returns an int status:
+ *     ANGELO_OK (0) or one of ANGELO_E_*; angelo_last_error_string() returns a
+ *     thread-local description of the last failure.  No C++ exception crosses
+ *     the ABI.
+ *   - Calls are stream-ordered and asynchronous; the library keeps no mutable
+ *     global state and never allocates device memory: outputs and workspace
+ *     belong to the caller (workspace sizes are queried per op).
+ *   - Tensors are row-major.  Points/directions are float32 (n, 3).  A hash
+ *     table is the tcnn flat parameter vector: entries of F=2 features, level
+ *     l starting at entry offsets[l].
+ *
+ * Each declaration names the reference call it replaces (path:line in the
+ * Instant-angelo tree).
+ */
+#ifndef ANGELO_GB_H
+#define ANGELO_GB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ANGELO_OK 0
+#define ANGELO_E_INVALID 1     /* bad argument: null pointer, size, alignment */
+#define ANGELO_E_CUDA 2        /* CUDA launch or runtime error */
+#define ANGELO_E_UNSUPPORTED 3 /* configuration outside what the kernels handle */
+#define ANGELO_E_CAPACITY 4    /* an output would exceed its stated capacity */
+
+#define ANGELO_MAX_LEVELS 32
+
+#define ANGELO_DTYPE_F32 0
+#define ANGELO_DTYPE_F16 1
+
+/* Hash-grid description: the keys of the reference's xyz_encoding_config
+ * (configs/neuralangelo-colmap_sparse.yaml:48-58). */
+typedef struct {
+    int32_t n_levels;          /* <= ANGELO_MAX_LEVELS */
+    int32_t n_features;        /* must be 2 */
+    int32_t log2_hashmap_size; /* <= 30 */
+    int32_t base_resolution;
+    float per_level_scale;
+} angelo_hashgrid_desc;
+
+/* Per-level layout derived from a description (tcnn's offset table). */
+typedef struct {
+    int32_t n_levels;
+    int32_t n_features;
+    uint32_t offsets[ANGELO_MAX_LEVELS + 1]; /* entry offset of every level, last = total */
+    uint32_t resolutions[ANGELO_MAX_LEVELS];
+    float scales[ANGELO_MAX_LEVELS];
+} angelo_hashgrid_layout_t;
+
+const char *angelo_last_error_string(void);
+int angelo_version(void);
+
+/* --------------------------------------------------------------- hash grid */
+
+/* Layout of tcnn.Encoding(otype=HashGrid) (models/network_utils.py:47):
+ * scale_l = exp2f(l*log2f(b))*base - 1, res_l = ceil(scale_l)+1,
+ * entries_l = min(align8(res_l^3), 2^log2T).  Host only. */
+int angelo_hashgrid_layout(const angelo_hashgrid_desc *desc, angelo_hashgrid_layout_t *out);
+
+/* Encode forward, replaces ProgressiveBandHashGrid.forward
+ * (models/network_utils.py:56-59) and CompositeEncoding.forward (:78-79).
+ * x: (n,3) contracted points.  Writes, per point i, at out + i*out_stride +
+ * out_col: [x*2-1 (3 values, only if include_xyz)] then L*2 features; levels
+ * >= active_levels are written as 0 (band mask).  table_dtype: F32 or F16. */
+int angelo_hashgrid_fwd(const angelo_hashgrid_layout_t *lay, int32_t active_levels,
+                        const float *x, int64_t n, const void *table, int32_t table_dtype,
+                        int32_t include_xyz, float *out, int64_t out_stride, int64_t out_col,
+                        void *stream);
+
+/* Encode backward (tcnn HashGrid backward behind the same call).
+ * dout holds dL/d(encoding) with the same stride/column convention.
+ * dtable (float32, may be NULL) is ACCUMULATED (atomic, order not fixed).
+ * dx (n,3, may be NULL) is WRITTEN with dL/dx, including the xyz columns when
+ * include_xyz; computing it reads table. */
+int angelo_hashgrid_bwd(const angelo_hashgrid_layout_t *lay, int32_t active_levels,
+                        const float *x, int64_t n, const void *table, int32_t table_dtype,
+                        int32_t include_xyz, const float *dout, int64_t dout_stride,
+                        int64_t dout_col, float *dtable, float *dx, void *stream);
+
+/* Corner indices / weights of every (point, level): idx (n, L, 8) uint32
+ * entry index inside the level, w (n, L, 8) float32.  Test hook for the
+ * bit-exact index check. */
+int angelo_hashgrid_index(const angelo_hashgrid_layout_t *lay, const float *x, int64_t n,
+                          uint32_t *idx, float *w, void *stream);
+
+/* ------------------------------------------------------ spherical harmonics */
+
+/* Degree-4 real SH (16 values), replaces tcnn SphericalHarmonics reached
+ * through get_encoding at models/texture.py:17,24-25.  With from_unit != 0 the
+ * input is a unit direction d and the reference's (d+1)/2 mapping is applied
+ * in the kernel; otherwise the input is already in [0,1]. */
+int angelo_sh4_fwd(const float *dirs, int64_t n, int32_t from_unit, float *out,
+                   int64_t out_stride, int64_t out_col, void *stream);
+/* dL/ddirs (written) from dL/dout. */
+int angelo_sh4_bwd(const float *dirs, int64_t n, int32_t from_unit, const float *dout,
+                   int64_t dout_stride, int64_t dout_col, float *ddirs, void *stream);
+
+/* ------------------------------------------------------------ ray marching */
+
+/* nerfacc.intersection.ray_aabb_intersect (models/neus.py:12,153). */
+int angelo_ray_aabb(const float *rays_o, const float *rays_d, int64_t n, const float *aabb6,
+                    float *t_min, float *t_max, void *stream);
+
+/* Occupancy grid as seen by the marcher: res^3 cells over roi, one bit per
+ * cell, cell index = ix*res_y*res_z + iy*res_z + iz, bit (c & 31) of word
+ * c >> 5.  A NULL bits pointer means "every cell occupied". */
+typedef struct {
+    float roi[6];
+    int32_t res[3];
+    const uint32_t *bits;
+} angelo_grid_t;
+
+/* nerfacc.ray_marching (models/neus.py:210-220), pass 1: samples per ray.
+ * status (device int32, may be NULL) gets bit 0 set when a ray reaches
+ * max_steps loop iterations. */
+int angelo_march_count(const float *rays_o, const float *rays_d, const float *t_min,
+                       const float *t_max, int64_t n_rays, const angelo_grid_t *grid,
+                       float step, float cone_angle, int64_t max_steps, int32_t *counts,
+                       int32_t *status, void *stream);
+
+/* Exclusive scan of int32 counts into int64 offsets (n+1 values, last =
+ * total).  Workspace: angelo_scan_workspace_size(n) bytes. */
+int64_t angelo_scan_workspace_size(int64_t n);
+int angelo_scan(const int32_t *counts, int64_t n, int64_t *offsets, void *workspace,
+                void *stream);
+
+/* Pass 2: writes ray_indices (int32), t_starts, t_ends at offsets[i] + j.
+ * Samples at or past capacity are dropped and status bit 1 is set. */
+int angelo_march_fill(const float *rays_o, const float *rays_d, const float *t_min,
+                      const float *t_max, int64_t n_rays, const angelo_grid_t *grid, float step,
+                      float cone_angle, int64_t max_steps, const int64_t *offsets,
+                      int64_t capacity, int32_t *ray_indices, float *t_starts, float *t_ends,
+                      int32_t *status, void *stream);
+
+/* ------------------------------------------------------- occupancy update */
+
+/* OccupancyGrid._update's EMA + threshold (models/neus.py:108-109 through
+ * nerfacc 0.3.3): occs[c] = max(occs[c]*decay, max over the k with
+ * cells[k]==c of occ[k]) for every sampled cell, then bits = occs >
+ * min(mean(occs), thre).  Workspace: angelo_occ_workspace_size(n_cells). */
+int64_t angelo_occ_workspace_size(int64_t n_cells);
+int angelo_occ_update(float *occs, int64_t n_cells, const int64_t *cells, const float *occ,
+                      int64_t k, float decay, float thre, uint32_t *bits, void *workspace,
+                      void *stream);
+
+/* -------------------------------------------------------------- compositing */
+
+/* nerfacc.render_weight_from_alpha (models/neus.py:234): per ray in sample
+ * order T_0 = 1, w_j = a_j*T_j, T_{j+1} = T_j*(1-a_j); w_j = 0 once T_j <
+ * early_stop_eps.  trans (may be NULL) receives T_j. */
+int angelo_weights_fwd(const float *alpha, const int64_t *offsets, int64_t n_rays,
+                       float early_stop_eps, float *weights, float *trans, void *stream);
+/* dL/dalpha (written) from dL/dweights and the forward's transmittance by the
+ * reverse scan R_{j-1} = g_j a_j + (1-a_j) R_j, dalpha_j = T_j (g_j - R_j). */
+int angelo_weights_bwd(const float *alpha, const float *trans, const int64_t *offsets,
+                       int64_t n_rays, float early_stop_eps, const float *dweights,
+                       float *dalpha, void *stream);
+
+/* nerfacc.accumulate_along_rays (models/neus.py:235-240): out[r, c] =
+ * sum_j w_j * v[j, c] over the samples of ray r (v == NULL: v = 1, C = 1). */
+int angelo_accumulate_fwd(const float *weights, const float *values, int32_t channels,
+                          const int64_t *offsets, int64_t n_rays, float *out, void *stream);
+/* dweights (written) and dvalues (written, may be NULL). */
+int angelo_accumulate_bwd(const float *weights, const float *values, int32_t channels,
+                          const int64_t *offsets, int64_t n_rays, const float *dout,
+                          float *dweights, float *dvalues, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ANGELO_GB_H */

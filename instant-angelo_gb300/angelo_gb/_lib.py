@@ -1,0 +1,110 @@
+"""ctypes binding of libangelo_gb.so (the C ABI declared in include/angelo_gb.h).
+
+The library is the only compute path: if it is missing or does not load, every
+op raises instead of falling back to anything else."""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libangelo_gb.so")
+
+ANGELO_OK = 0
+ANGELO_E_INVALID = 1
+ANGELO_E_CUDA = 2
+ANGELO_E_UNSUPPORTED = 3
+ANGELO_E_CAPACITY = 4
+MAX_LEVELS = 32
+DTYPE_F32 = 0
+DTYPE_F16 = 1
+
+c_i32, c_i64, c_f32, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p
+
+
+class HashGridDesc(ctypes.Structure):
+    _fields_ = [("n_levels", c_i32), ("n_features", c_i32), ("log2_hashmap_size", c_i32),
+                ("base_resolution", c_i32), ("per_level_scale", c_f32)]
+
+
+class HashGridLayout(ctypes.Structure):
+    _fields_ = [("n_levels", c_i32), ("n_features", c_i32),
+                ("offsets", ctypes.c_uint32 * (MAX_LEVELS + 1)),
+                ("resolutions", ctypes.c_uint32 * MAX_LEVELS),
+                ("scales", c_f32 * MAX_LEVELS)]
+
+
+class GridDesc(ctypes.Structure):
+    _fields_ = [("roi", c_f32 * 6), ("res", c_i32 * 3), ("bits", c_vp)]
+
+
+class AngeloError(RuntimeError):
+    def __init__(self, fn, code, msg):
+        super().__init__(f"{fn} failed with status {code}: {msg}")
+        self.code = code
+
+
+# name -> (restype, argtypes)
+_P = ctypes.POINTER
+SIGNATURES = {
+    "angelo_last_error_string": (ctypes.c_char_p, []),
+    "angelo_version": (c_i32, []),
+    "angelo_hashgrid_layout": (c_i32, [_P(HashGridDesc), _P(HashGridLayout)]),
+    "angelo_hashgrid_fwd": (c_i32, [_P(HashGridLayout), c_i32, c_vp, c_i64, c_vp, c_i32, c_i32,
+                                    c_vp, c_i64, c_i64, c_vp]),
+    "angelo_hashgrid_bwd": (c_i32, [_P(HashGridLayout), c_i32, c_vp, c_i64, c_vp, c_i32, c_i32,
+                                    c_vp, c_i64, c_i64, c_vp, c_vp, c_vp]),
+    "angelo_hashgrid_index": (c_i32, [_P(HashGridLayout), c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "angelo_sh4_fwd": (c_i32, [c_vp, c_i64, c_i32, c_vp, c_i64, c_i64, c_vp]),
+    "angelo_sh4_bwd": (c_i32, [c_vp, c_i64, c_i32, c_vp, c_i64, c_i64, c_vp, c_vp]),
+    "angelo_ray_aabb": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_march_count": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, _P(GridDesc), c_f32, c_f32,
+                                   c_i64, c_vp, c_vp, c_vp]),
+    "angelo_scan_workspace_size": (c_i64, [c_i64]),
+    "angelo_scan": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "angelo_march_fill": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, _P(GridDesc), c_f32, c_f32,
+                                  c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_occ_workspace_size": (c_i64, [c_i64]),
+    "angelo_occ_update": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_i64, c_f32, c_f32, c_vp, c_vp,
+                                  c_vp]),
+    "angelo_weights_fwd": (c_i32, [c_vp, c_vp, c_i64, c_f32, c_vp, c_vp, c_vp]),
+    "angelo_weights_bwd": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_f32, c_vp, c_vp, c_vp]),
+    "angelo_accumulate_fwd": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp]),
+    "angelo_accumulate_bwd": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libangelo_gb.so and bind every entry point of the C ABI."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(path):
+                raise RuntimeError(
+                    f"libangelo_gb.so not found at {path}: build it with "
+                    "`python -m angelo_gb.build` (needs nvcc); there is no fallback path")
+            L = ctypes.CDLL(path)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def call(name, *args):
+    """Call an int-status entry point; raise AngeloError on a non-zero status."""
+    L = load()
+    rc = getattr(L, name)(*args)
+    if rc != ANGELO_OK:
+        msg = L.angelo_last_error_string().decode(errors="replace")
+        raise AngeloError(name, rc, msg)
+    return rc
+
+
+def raw(name):
+    return getattr(load(), name)

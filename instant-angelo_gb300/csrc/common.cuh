@@ -1,0 +1,109 @@
+// Shared helpers of libangelo_gb.so: status codes, error string, launch
+// checks and the per-level hash-grid arithmetic used by several kernels.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+
+#include "angelo_gb.h"
+
+namespace angelo {
+
+// Thread-local message behind angelo_last_error_string().
+void set_error(const char *fmt, ...);
+
+inline int check_launch(const char *what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error("%s: %s", what, cudaGetErrorString(e));
+        return ANGELO_E_CUDA;
+    }
+    return ANGELO_OK;
+}
+
+#define ANGELO_REQUIRE(cond, ...)          \
+    do {                                   \
+        if (!(cond)) {                     \
+            ::angelo::set_error(__VA_ARGS__); \
+            return ANGELO_E_INVALID;       \
+        }                                  \
+    } while (0)
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline unsigned blocks_for(int64_t n, int threads) {
+    return (unsigned)((n + threads - 1) / threads);
+}
+
+// ------------------------------------------------------------- hash grid math
+//
+// tcnn HashGrid per-level arithmetic for 3 input dims (the reference's
+// tcnn.Encoding at models/network_utils.py:47):
+//   pos = fmaf(scale, x, 0.5); cell = (uint32)(int)floor(pos); frac = pos - floor
+//   corner c (bit d set = +1 along dim d), weight = prod_d (bit ? frac : 1-frac)
+//   index = dense x + y*res + z*res^2 while the stride fits the level, else
+//           x*1 ^ y*2654435761 ^ z*805459861; then mod the level size.
+
+__device__ __forceinline__ uint32_t grid_index(uint32_t hashmap_size, uint32_t res, uint32_t g0,
+                                               uint32_t g1, uint32_t g2) {
+    uint32_t stride = 1, index = 0;
+    const uint32_t g[3] = {g0, g1, g2};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        if (stride <= hashmap_size) {
+            index += g[d] * stride;
+            stride *= res;
+        }
+    }
+    // The dense loop above stops adding once stride exceeds the level size,
+    // exactly where the reference's loop condition stops.
+    if (hashmap_size < stride) index = (g0 * 1u) ^ (g1 * 2654435761u) ^ (g2 * 805459861u);
+    return index % hashmap_size;
+}
+
+struct LevelPos {
+    uint32_t g[3];
+    float f[3];
+};
+
+__device__ __forceinline__ LevelPos level_pos(float x0, float x1, float x2, float scale) {
+    LevelPos p;
+    const float xs[3] = {x0, x1, x2};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float pos = __fmaf_rn(scale, xs[d], 0.5f);
+        const float fl = floorf(pos);
+        p.g[d] = (uint32_t)(int32_t)fl;
+        p.f[d] = __fsub_rn(pos, fl);
+    }
+    return p;
+}
+
+// Weight of corner c, multiplied in tcnn's order (dim 0, 1, 2) with no
+// contraction so the float32 result is reproducible on the host.
+__device__ __forceinline__ float corner_weight(const LevelPos &p, int c) {
+    float w = 1.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) w = __fmul_rn(w, (c >> d) & 1 ? p.f[d] : __fsub_rn(1.0f, p.f[d]));
+    return w;
+}
+
+__device__ __forceinline__ uint32_t corner_index(const angelo_hashgrid_layout_t &lay, int l,
+                                                 const LevelPos &p, int c) {
+    const uint32_t hs = lay.offsets[l + 1] - lay.offsets[l];
+    return grid_index(hs, lay.resolutions[l], p.g[0] + (c & 1), p.g[1] + ((c >> 1) & 1),
+                      p.g[2] + ((c >> 2) & 1));
+}
+
+__device__ __forceinline__ float2 load_entry(const void *table, int dtype, uint64_t entry) {
+    if (dtype == ANGELO_DTYPE_F32) {
+        return __ldg(reinterpret_cast<const float2 *>(table) + entry);
+    }
+    const __half2 h = __ldg(reinterpret_cast<const __half2 *>(table) + entry);
+    return __half22float2(h);
+}
+
+}  // namespace angelo

@@ -1,0 +1,332 @@
+// Ray-AABB clipping and occupancy-grid ray marching (the nerfacc 0.3.3 calls
+// at models/neus.py:153 and models/neus.py:210-220).
+//
+// The per-ray march is a sequential float32 recurrence (t0 <- t1, t1 <- t0 +
+// dt, DDA skips over empty cells) whose rounding fixes which samples exist, so
+// each ray is marched by one thread exactly in the reference's order; the
+// occupancy bitfield (res^3 bits, 256 KiB at 128^3) stays L1/L2 resident.
+// Count, scan and fill are three launches, as in the reference.
+#include "common.cuh"
+
+using namespace angelo;
+
+namespace {
+
+struct Grid {
+    float lo[3], hi[3];
+    int res[3];
+    const uint32_t *bits;
+};
+
+__device__ __forceinline__ bool occupied(const Grid &g, const float xyz[3]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+        if (xyz[d] < g.lo[d] || xyz[d] > g.hi[d]) return false;
+    if (g.bits == nullptr) return true;
+    int ix[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float u = __fdiv_rn(__fsub_rn(xyz[d], g.lo[d]), __fsub_rn(g.hi[d], g.lo[d]));
+        int v = (int)__fmul_rn(u, (float)g.res[d]);
+        v = v < 0 ? 0 : (v > g.res[d] - 1 ? g.res[d] - 1 : v);
+        ix[d] = v;
+    }
+    const int64_t c = ((int64_t)ix[0] * g.res[1] + ix[1]) * g.res[2] + ix[2];
+    return (__ldg(g.bits + (c >> 5)) >> (c & 31)) & 1u;
+}
+
+__device__ __forceinline__ float sgn(float v) { return v > 0.f ? 1.f : (v < 0.f ? -1.f : 0.f); }
+
+__device__ __forceinline__ float calc_dt(float t, float cone, float dt_min) {
+    float v = __fmul_rn(t, cone);
+    v = v < dt_min ? dt_min : v;
+    return v > 1e10f ? 1e10f : v;
+}
+
+__device__ __forceinline__ float dist_next_voxel(const Grid &g, const float xyz[3],
+                                                 const float dir[3], const float inv[3]) {
+    float t = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const float ext = __fsub_rn(g.hi[d], g.lo[d]);
+        const float r = (float)g.res[d];
+        const float u = __fmul_rn(__fdiv_rn(__fsub_rn(xyz[d], g.lo[d]), ext), r);
+        const float tgt = floorf(__fadd_rn(__fadd_rn(u, 0.5f), __fmul_rn(0.5f, sgn(dir[d]))));
+        const float td = __fmul_rn(__fdiv_rn(__fmul_rn(__fsub_rn(tgt, u), inv[d]), r), ext);
+        t = d == 0 ? td : fminf(t, td);
+    }
+    return t > 0.f ? t : 0.f;
+}
+
+// One ray; emit(j, t0, t1) for each sample; returns the sample count.
+template <typename Emit>
+__device__ __forceinline__ int64_t march_ray(const Grid &g, const float o[3], const float d[3],
+                                             float near, float far, float step, float cone,
+                                             int64_t max_steps, int32_t *status, Emit emit) {
+    float inv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) inv[k] = __fdiv_rn(1.0f, d[k]);
+    int64_t j = 0, it = 0;
+    float t0 = near;
+    float t1 = __fadd_rn(t0, calc_dt(t0, cone, step));
+    float tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
+    while (tm < far) {
+        if (++it > max_steps) {
+            if (status) atomicOr(status, 1);
+            break;
+        }
+        float xyz[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) xyz[k] = __fmaf_rn(tm, d[k], o[k]);
+        if (occupied(g, xyz)) {
+            emit(j, t0, t1);
+            ++j;
+            t0 = t1;
+            t1 = __fadd_rn(t0, calc_dt(t0, cone, step));
+            tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
+        } else {
+            const float tgt = __fadd_rn(tm, dist_next_voxel(g, xyz, d, inv));
+            float tt = tm;
+            int64_t guard = 0;
+            do {
+                tt = __fadd_rn(tt, step);
+            } while (tt < tgt && ++guard < max_steps);
+            tm = tt;
+            const float dt = calc_dt(tm, cone, step);
+            t0 = __fsub_rn(tm, __fmul_rn(dt, 0.5f));
+            t1 = __fadd_rn(tm, __fmul_rn(dt, 0.5f));
+        }
+    }
+    return j;
+}
+
+__global__ void ray_aabb_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
+                                int64_t n, const float *__restrict__ aabb, float *__restrict__ tmin_out,
+                                float *__restrict__ tmax_out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float *o = ro + i * 3, *d = rd + i * 3;
+    float tmin = __fdiv_rn(aabb[0] - o[0], d[0]);
+    float tmax = __fdiv_rn(aabb[3] - o[0], d[0]);
+    if (tmin > tmax) { const float t = tmin; tmin = tmax; tmax = t; }
+    float tymin = __fdiv_rn(aabb[1] - o[1], d[1]);
+    float tymax = __fdiv_rn(aabb[4] - o[1], d[1]);
+    if (tymin > tymax) { const float t = tymin; tymin = tymax; tymax = t; }
+    float nr = 1e10f, fr = 1e10f;
+    if (!(tmin > tymax || tymin > tmax)) {
+        if (tymin > tmin) tmin = tymin;
+        if (tymax < tmax) tmax = tymax;
+        float tzmin = __fdiv_rn(aabb[2] - o[2], d[2]);
+        float tzmax = __fdiv_rn(aabb[5] - o[2], d[2]);
+        if (tzmin > tzmax) { const float t = tzmin; tzmin = tzmax; tzmax = t; }
+        if (!(tmin > tzmax || tzmin > tmax)) {
+            if (tzmin > tmin) tmin = tzmin;
+            if (tzmax < tmax) tmax = tzmax;
+            nr = tmin;
+            fr = tmax;
+        }
+    }
+    tmin_out[i] = nr > 0.f ? nr : 0.f;
+    tmax_out[i] = fr;
+}
+
+__global__ void march_count_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
+                                   const float *__restrict__ tmin, const float *__restrict__ tmax,
+                                   int64_t n, Grid g, float step, float cone, int64_t max_steps,
+                                   int32_t *__restrict__ counts, int32_t *status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float o[3] = {ro[i * 3], ro[i * 3 + 1], ro[i * 3 + 2]};
+    const float d[3] = {rd[i * 3], rd[i * 3 + 1], rd[i * 3 + 2]};
+    const int64_t c = march_ray(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status,
+                                [](int64_t, float, float) {});
+    counts[i] = (int32_t)(c > 0x7fffffff ? 0x7fffffff : c);
+}
+
+__global__ void march_fill_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
+                                  const float *__restrict__ tmin, const float *__restrict__ tmax,
+                                  int64_t n, Grid g, float step, float cone, int64_t max_steps,
+                                  const int64_t *__restrict__ offsets, int64_t capacity,
+                                  int32_t *__restrict__ ray_idx, float *__restrict__ ts,
+                                  float *__restrict__ te, int32_t *status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float o[3] = {ro[i * 3], ro[i * 3 + 1], ro[i * 3 + 2]};
+    const float d[3] = {rd[i * 3], rd[i * 3 + 1], rd[i * 3 + 2]};
+    const int64_t base = offsets[i];
+    const int64_t limit = offsets[i + 1];
+    bool dropped = false;
+    march_ray(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status,
+              [&](int64_t j, float t0, float t1) {
+                  const int64_t p = base + j;
+                  if (p < capacity && p < limit) {
+                      ray_idx[p] = (int32_t)i;
+                      ts[p] = t0;
+                      te[p] = t1;
+                  } else {
+                      dropped = true;
+                  }
+              });
+    if (dropped && status) atomicOr(status, 2);
+}
+
+// ---------------------------------------------------------------- scan
+// Three-phase exclusive scan of int32 counts into int64 offsets: per-block
+// scans of 1024 counts (256 threads x 4), one block scanning the block sums,
+// then the block offsets added back.
+
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ int64_t block_exclusive_scan(int64_t v, int64_t *total) {
+    __shared__ int64_t warp_sums[kScanThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        int64_t s = lane < kScanThreads / 32 ? warp_sums[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < kScanThreads / 32) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const int64_t before = warp > 0 ? warp_sums[warp - 1] : 0;
+    *total = warp_sums[kScanThreads / 32 - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_tiles_kernel(const int32_t *__restrict__ in,
+                                                                  int64_t n, int64_t *__restrict__ out,
+                                                                  int64_t *__restrict__ tile_sums) {
+    const int64_t base = (int64_t)blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    int64_t v[kScanItems];
+    int64_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = base + k < n ? (int64_t)in[base + k] : 0;
+        s += v[k];
+    }
+    int64_t total;
+    int64_t run = block_exclusive_scan(s, &total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_sums_kernel(int64_t *__restrict__ sums,
+                                                                 int64_t n_tiles,
+                                                                 int64_t *__restrict__ grand) {
+    int64_t carry = 0;
+    for (int64_t start = 0; start < n_tiles; start += kScanThreads) {
+        const int64_t i = start + threadIdx.x;
+        const int64_t v = i < n_tiles ? sums[i] : 0;
+        int64_t total;
+        const int64_t ex = block_exclusive_scan(v, &total);
+        if (i < n_tiles) sums[i] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) *grand = carry;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_add_kernel(int64_t *__restrict__ out,
+                                                                int64_t n,
+                                                                const int64_t *__restrict__ sums) {
+    const int64_t base = (int64_t)blockIdx.x * kScanTile;
+    const int64_t add = sums[blockIdx.x];
+    for (int k = threadIdx.x; k < kScanTile; k += kScanThreads)
+        if (base + k < n) out[base + k] += add;
+}
+
+int make_grid(const angelo_grid_t *in, Grid *g) {
+    ANGELO_REQUIRE(in != nullptr, "march: null grid");
+    for (int d = 0; d < 3; ++d) {
+        g->lo[d] = in->roi[d];
+        g->hi[d] = in->roi[3 + d];
+        g->res[d] = in->res[d];
+        ANGELO_REQUIRE(in->res[d] >= 1 && in->res[d] <= 4096, "march: grid resolution %d",
+                       in->res[d]);
+    }
+    g->bits = in->bits;
+    return ANGELO_OK;
+}
+
+}  // namespace
+
+extern "C" int angelo_ray_aabb(const float *rays_o, const float *rays_d, int64_t n,
+                               const float *aabb6, float *t_min, float *t_max, void *stream) {
+    ANGELO_REQUIRE(n >= 0, "ray_aabb: negative n");
+    if (n == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(rays_o && rays_d && aabb6 && t_min && t_max, "ray_aabb: null pointer");
+    ray_aabb_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(rays_o, rays_d, n, aabb6,
+                                                                      t_min, t_max);
+    return check_launch("ray_aabb");
+}
+
+extern "C" int angelo_march_count(const float *rays_o, const float *rays_d, const float *t_min,
+                                  const float *t_max, int64_t n_rays, const angelo_grid_t *grid,
+                                  float step, float cone_angle, int64_t max_steps, int32_t *counts,
+                                  int32_t *status, void *stream) {
+    Grid g;
+    if (int e = make_grid(grid, &g)) return e;
+    ANGELO_REQUIRE(n_rays >= 0 && step > 0.f && max_steps > 0, "march_count: bad arguments");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(rays_o && rays_d && t_min && t_max && counts, "march_count: null pointer");
+    march_count_kernel<<<blocks_for(n_rays, 128), 128, 0, as_stream(stream)>>>(
+        rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, counts, status);
+    return check_launch("march_count");
+}
+
+extern "C" int64_t angelo_scan_workspace_size(int64_t n) {
+    const int64_t tiles = (n + kScanTile - 1) / kScanTile;
+    return (tiles + 1) * (int64_t)sizeof(int64_t);
+}
+
+extern "C" int angelo_scan(const int32_t *counts, int64_t n, int64_t *offsets, void *workspace,
+                           void *stream) {
+    ANGELO_REQUIRE(n >= 0 && offsets && workspace, "scan: bad arguments");
+    cudaStream_t s = as_stream(stream);
+    if (n == 0) {
+        if (cudaMemsetAsync(offsets, 0, sizeof(int64_t), s) != cudaSuccess)
+            return check_launch("scan(memset)");
+        return ANGELO_OK;
+    }
+    ANGELO_REQUIRE(counts != nullptr, "scan: null counts");
+    const int64_t tiles = (n + kScanTile - 1) / kScanTile;
+    int64_t *sums = reinterpret_cast<int64_t *>(workspace);
+    scan_tiles_kernel<<<(unsigned)tiles, kScanThreads, 0, s>>>(counts, n, offsets, sums);
+    scan_sums_kernel<<<1, kScanThreads, 0, s>>>(sums, tiles, offsets + n);
+    scan_add_kernel<<<(unsigned)tiles, kScanThreads, 0, s>>>(offsets, n, sums);
+    return check_launch("scan");
+}
+
+extern "C" int angelo_march_fill(const float *rays_o, const float *rays_d, const float *t_min,
+                                 const float *t_max, int64_t n_rays, const angelo_grid_t *grid,
+                                 float step, float cone_angle, int64_t max_steps,
+                                 const int64_t *offsets, int64_t capacity, int32_t *ray_indices,
+                                 float *t_starts, float *t_ends, int32_t *status, void *stream) {
+    Grid g;
+    if (int e = make_grid(grid, &g)) return e;
+    ANGELO_REQUIRE(n_rays >= 0 && step > 0.f && max_steps > 0 && capacity >= 0,
+                   "march_fill: bad arguments");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(rays_o && rays_d && t_min && t_max && offsets, "march_fill: null pointer");
+    ANGELO_REQUIRE(capacity == 0 || (ray_indices && t_starts && t_ends), "march_fill: null output");
+    march_fill_kernel<<<blocks_for(n_rays, 128), 128, 0, as_stream(stream)>>>(
+        rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, offsets, capacity,
+        ray_indices, t_starts, t_ends, status);
+    return check_launch("march_fill");
+}

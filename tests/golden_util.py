@@ -37,3 +37,14 @@ def oracle_cfgs(g):
     kind = {"volume-radiance": "radiance", "volume-dual-color": "dual"}[c["tex"]["name"]]
     T = dict(kind=kind, n_layers=c["tex"]["n_hidden_layers"] + 1)
     return G, T
+
+
+def model_config(g, fused=False, **extra):
+    """The reference model config the golden was made with (the keys of
+    make_golden.model_config), as a plain dict for the drop-in NeuSModel."""
+    from golden.make_golden import model_config as mc
+    from angelo_gb.config import to_primitive
+    cfg = to_primitive(mc(g["cfg"]))
+    cfg["fused"] = fused
+    cfg.update(extra)
+    return cfg

@@ -1,0 +1,76 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports
+every symbol its header declares, the host-only layout call matches the
+oracle bit for bit, and the drop-in modules build with the reference's
+configuration keys and parameter names."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import cref
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "angelo_gb.h")).read()
+    return sorted(set(re.findall(r"\b(angelo_[a-z0-9_]+)\s*\(", txt)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from angelo_gb import build, _lib
+    build.build()
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    syms = _declared_symbols()
+    assert len(syms) >= 18
+    for s in syms:
+        assert hasattr(lib, s), s
+    from angelo_gb import _lib
+    assert set(_lib.SIGNATURES) == set(syms)
+
+
+@pytest.mark.parametrize("cfg", [(8, 16, 16, 1.5), (16, 22, 32, 1.3195079107728942),
+                                 (16, 19, 32, 1.3195079107728942), (16, 10, 4, 1.3195079107728942)])
+def test_layout_matches_oracle(lib, cfg):
+    from angelo_gb.ops import HashGridSpec
+    L, log2T, base, b = cfg
+    spec = HashGridSpec(L, 2, log2T, base, b)
+    off, res, sc = cref.hashgrid_layout(L, log2T, base, b)
+    assert spec.offsets == [int(v) for v in off]
+    assert spec.resolutions == [int(v) for v in res]
+    assert np.array_equal(np.array(spec.scales, np.float32), sc)
+
+
+def test_layout_rejects_bad_config(lib):
+    from angelo_gb import _lib
+    from angelo_gb.ops import HashGridSpec
+    with pytest.raises(_lib.AngeloError) as e:
+        HashGridSpec(40, 2, 19, 16, 1.5)
+    assert e.value.code == _lib.ANGELO_E_INVALID
+    with pytest.raises(_lib.AngeloError):
+        HashGridSpec(8, 4, 19, 16, 1.5)
+
+
+def test_workspace_queries(lib):
+    assert lib.angelo_scan_workspace_size(0) >= 8
+    assert lib.angelo_scan_workspace_size(10 ** 6) >= 8 * (10 ** 6 // 1024)
+    assert lib.angelo_occ_workspace_size(128 ** 3) >= 4 * 128 ** 3
+
+
+def test_dropins_build_with_reference_keys(lib):
+    from angelo_gb import models
+    from golden_util import load
+    g = load("neus_dual_grid")
+    from golden_util import model_config
+    m = models.make("neus", model_config(g))
+    names = set(m.state_dict().keys())
+    ref = {k[len("param/"):] for k in g if k.startswith("param/")}
+    assert ref <= names, ref - names
+    for k in ref:
+        assert tuple(m.state_dict()[k].shape) == g["param/" + k].shape, k
