@@ -1,0 +1,474 @@
+#!/usr/bin/env python
+"""Benchmark of the NeuS / Neuralangelo training step on GB300.
+
+Workload ("full"): the Neuralangelo sparse training step -- 16-level 2^22 hash
+grid (base 32, finest 2048, all 16 levels active: global step 6000 of the
+band schedule, FD eps 1/2048), 128^3 occupancy grid, marching step
+sqrt(3)*2*0.5/512, rays resized toward 2^18 samples (at most 8192), eikonal
+0.1 + curvature 5e-4 + rgb MSE, AdamW -- on 1600x1200 synthetic views of an
+analytic torus/box/sphere union (seeded; Gaussian noise 0.01).  A step is one
+full training iteration: update_step (occupancy refresh every 16 steps),
+forward, losses, backward, optimizer step.
+
+value : rays/s with the target views resident in HBM (rays sampled on device)
+e2e   : rays/s through NeuSModel / NeuSTrainer with each step's rays and
+        colours sampled on the host and copied from pinned memory, the loss
+        read back.
+Both forms of the path are run: "plain" (the reference's structure with the
+library's encode / march / composite kernels) and, when built, "fused".
+
+--impl reference times the oracle's CPU restatement of the same step on the
+host cores (the reference itself is Python over tcnn/nerfacc CUDA kernels,
+none of which exists here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "instant-angelo_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+GLOBAL_STEP = 6000
+INV_S_VARIANCE = 0.7          # inv_s = exp(7) ~ 1097, a mid-training sharpness
+N_VIEWS, W, H, FOV, CAM_R = 8, 1600, 1200, 40.0, 1.5
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--forms", default="auto", help="comma list of plain,fused (auto: all built)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ plumbing
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            self.proc.wait(timeout=10)
+
+    def summary(self):
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+                for nm, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs"), d.get("bf16_tflops"), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+# --------------------------------------------------------------- the workload
+
+
+def make_views(dev):
+    from angelo_gb import scenes
+    return scenes.TargetViews(scenes.UnionScene(), N_VIEWS, W, H, FOV, CAM_R, seed=0, device=dev)
+
+
+def make_trainer(form, dev, seed=0):
+    from angelo_gb import models, scenes, workloads
+    from angelo_gb.system import NeuSTrainer
+    torch.manual_seed(seed)
+    cfg = workloads.model_config("full", fused=(form == "fused"))
+    model = models.make("neus", cfg).to(dev)
+    model.train()
+    with torch.no_grad():
+        model.variance.variance.fill_(INV_S_VARIANCE)
+        occ = scenes.analytic_occupancy(scenes.UnionScene(), 128, device=dev)
+        g = model.occupancy_grid
+        g.occs.copy_(occ.float())
+        bits = torch.zeros(g.bits.numel() * 32, dtype=torch.int64, device=dev)
+        bits[: occ.numel()] = occ.long()
+        w = (bits.view(-1, 32) << torch.arange(32, device=dev)).sum(-1)
+        g.bits.copy_(w.to(torch.int64).bitwise_and(0xFFFFFFFF).to(torch.int32))
+    tr = NeuSTrainer(model, workloads.SYSTEM, train_num_rays=8192, max_train_num_rays=8192,
+                     train_num_samples=1 << 18)
+    tr.global_step = GLOBAL_STEP
+    return model, tr
+
+
+def step_device(tr, views, gen):
+    rays, rgb = views.sample_rays(tr.train_num_rays, generator=gen)
+    bg = torch.rand(3, device=rays.device, generator=gen)
+    n_rays = rays.shape[0]
+    loss, n_samples = tr.step(rays, rgb, bg)
+    return n_rays, n_samples
+
+
+class HostFeed:
+    """Host-side copy of the views; rays are built on the CPU per step and copied
+    from pinned memory (the reference samples on the CPU: systems/neus.py:35-118)."""
+
+    def __init__(self, views, seed=1):
+        self.images = views.images.cpu()
+        self.c2w = views.c2w.cpu()
+        self.dirs = views.dirs.cpu()
+        self.rng = np.random.default_rng(seed)
+        self.W, self.H = views.W, views.H
+
+    def batch(self, n):
+        from angelo_gb.scenes import rays_from
+        idx = torch.from_numpy(self.rng.integers(0, self.images.shape[0], n))
+        pix = torch.from_numpy(self.rng.integers(0, self.W * self.H, n))
+        rays = rays_from(self.dirs[pix], self.c2w[idx]).contiguous().pin_memory()
+        rgb = self.images[idx, pix].contiguous().pin_memory()
+        bg = torch.from_numpy(self.rng.random(3).astype(np.float32)).pin_memory()
+        return rays, rgb, bg
+
+
+def step_host(tr, feed, dev):
+    rays_h, rgb_h, bg_h = feed.batch(tr.train_num_rays)
+    rays = rays_h.to(dev, non_blocking=True)
+    rgb = rgb_h.to(dev, non_blocking=True)
+    bg = bg_h.to(dev, non_blocking=True)
+    loss, n_samples = tr.step(rays, rgb, bg)
+    loss_h = loss.to("cpu")                    # the step's result read back
+    h2d = rays_h.numel() * 4 + rgb_h.numel() * 4 + bg_h.numel() * 4
+    return rays.shape[0], n_samples, h2d, loss_h.numel() * 4
+
+
+def timed(fn, steps, dev, world):
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    acc = [fn() for _ in range(steps)]
+    e1.record()
+    torch.cuda.synchronize(dev)
+    if world > 1:
+        torch.distributed.barrier()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, acc
+
+
+# ------------------------------------------------------------------ roofline
+
+
+def algorithmic_bytes(name, u):
+    """Algorithmic bytes of one call (each input read once, each output
+    written once, table atomics counted as read + write)."""
+    if u is None:
+        return None
+    if name == "angelo_hashgrid_fwd":
+        return u["n"] * (12 + u["active"] * 8 * 2 * u["tbytes"] + (u["L"] * 2 + 3 * u["xyz"]) * 4)
+    if name == "angelo_hashgrid_bwd":
+        b = 12 + (u["L"] * 2 + 3) * 4
+        if u["dtable"]:
+            b += u["active"] * 8 * 2 * 4 * 2
+        if u["dx"]:
+            b += u["active"] * 8 * 2 * u["tbytes"] + 12
+        return u["n"] * b
+    if name.startswith("angelo_sdf_stencil") or name.startswith("angelo_radiance") or \
+            name.startswith("angelo_composite"):
+        return u.get("bytes")
+    return None
+
+
+def roofline(summary, hbm_peak, peak_kind):
+    best = None
+    for name, (calls, ms, units) in summary.items():
+        if best is None or ms > best[2]:
+            best = (name, calls, ms, units)
+    if best is None:
+        return None, None
+    name, calls, ms, units = best
+    total_bytes = 0
+    for u in units:
+        b = algorithmic_bytes(name, u)
+        if b is None:
+            total_bytes = None
+            break
+        total_bytes += b
+    shares = {k: round(v[1], 3) for k, v in sorted(summary.items(), key=lambda kv: -kv[1][1])}
+    if total_bytes is None:
+        return {"kernel": name, "bound": "hbm", "achieved": None, "peak": hbm_peak,
+                "unit": "GB/s", "frac": None, "traffic": None,
+                "peak_source": peak_kind}, shares
+    gbs = total_bytes / (ms * 1e-3) / 1e9
+    return {"kernel": name, "bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_peak,
+            "unit": "GB/s", "frac": round(gbs / hbm_peak, 4), "traffic": None,
+            "bytes_per_launch": int(total_bytes / calls), "launches": calls,
+            "ms_per_launch": round(ms / calls, 4), "peak_source": peak_kind}, shares
+
+
+# -------------------------------------------------------------- CPU baseline
+
+
+def cpu_step(model, views_cpu, n_rays, seed):
+    """One training forward + backward of the same step, in the oracle's
+    float32 CPU restatement (oracle/neus_fp64.py), on n_rays rays."""
+    from oracle import cref
+    from oracle import neus_fp64 as O
+    g = np.random.default_rng(seed)
+    images, c2w, dirs, Wd, Hd = views_cpu
+    from angelo_gb.scenes import rays_from
+    idx = torch.from_numpy(g.integers(0, images.shape[0], n_rays))
+    pix = torch.from_numpy(g.integers(0, Wd * Hd, n_rays))
+    rays = rays_from(dirs[pix], c2w[idx]).float()
+    rgb = images[idx, pix].float()
+    cfg = model.config
+    h = cfg.geometry.xyz_encoding_config
+    lay = O.HashGridLayout(h.n_levels, h.n_features_per_level, h.log2_hashmap_size,
+                           h.base_resolution, h.per_level_scale)
+    G = dict(radius=cfg.radius, eps=model.geometry._finite_difference_eps, lay=lay,
+             active_levels=model.geometry.encoding.encoding.mask_levels,
+             n_layers=cfg.geometry.mlp_network_config.n_hidden_layers + 1,
+             feature_dim=cfg.geometry.feature_dim, hg=h)
+    T = dict(kind="dual" if cfg.texture.name == "volume-dual-color" else "radiance",
+             n_layers=cfg.texture.mlp_network_config.n_hidden_layers + 1)
+    P = {k: v.detach().cpu().float().clone().requires_grad_(v.dtype.is_floating_point)
+         for k, v in model.state_dict().items() if not k.startswith("occupancy_grid")}
+    grid = model.occupancy_grid
+    binary = grid.binary.cpu().numpy().astype(np.uint8)
+    aabb = model.scene_aabb.cpu().numpy()
+    t0c = time.perf_counter()
+    tmin, tmax = cref.ray_aabb(rays[:, :3].numpy(), rays[:, 3:].numpy(), aabb)
+    tmin = (tmin + g.random(n_rays, dtype=np.float32) * np.float32(model.render_step_size))
+    _, off, ri, t0, t1, _ = cref.march(rays[:, :3].numpy(), rays[:, 3:].numpy(),
+                                       tmin.astype(np.float32), tmax, aabb, binary,
+                                       model.render_step_size)
+    rd = torch.randn(len(t0), 3)
+    out = O.neus_render(rays, P, G, T, (off, ri, t0, t1), rd, model.cos_anneal_ratio,
+                        torch.rand(3))
+    loss = O.neus_losses(out, rgb)
+    loss.backward()
+    return time.perf_counter() - t0c, len(t0)
+
+
+def cpu_baseline(model, views, budget_s=15.0):
+    views_cpu = (views.images.cpu(), views.c2w.cpu(), views.dirs.cpu(), views.W, views.H)
+    torch.set_num_threads(os.cpu_count() or 1)
+    dt, _ = cpu_step(model, views_cpu, 16, 123)
+    per_ray = dt / 16
+    n = int(max(16, min(2048, (budget_s / 3) / max(per_ray, 1e-6))))
+    tot_t, tot_r, tot_s = 0.0, 0, 0
+    k = 0
+    while tot_t < budget_s * 0.6 and k < 3:
+        dt, s = cpu_step(model, views_cpu, n, 200 + k)
+        tot_t += dt
+        tot_r += n
+        tot_s += s
+        k += 1
+    return {"value": round(tot_r / tot_t, 2), "unit": "rays/s", "cores": torch.get_num_threads(),
+            "kind": "port",
+            "sample": f"{k} step(s) of {n} rays ({tot_s} samples) of the same workload, "
+                      "forward+backward in the oracle's float32 CPU restatement"}
+
+
+# ---------------------------------------------------------------------- arms
+
+
+def available_forms():
+    forms = ["plain"]
+    try:
+        from angelo_gb import fused  # noqa: F401
+        if fused.available():
+            forms.append("fused")
+    except ImportError:
+        pass
+    return forms
+
+
+def run_ours(args):
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    from angelo_gb import build, _lib
+    build.build()
+    views = make_views(dev)
+    forms = available_forms() if args.forms == "auto" else args.forms.split(",")
+    results = {}
+    hbm_peak, _, peak_kind = measured_peaks()
+    for form in forms:
+        model, tr = make_trainer(form, dev)
+        gen = torch.Generator(device=dev).manual_seed(1234 + rank)
+        for _ in range(args.warmup):
+            step_device(tr, views, gen)
+        with Clocks(local) as clk:
+            _lib.PROFILER.start()
+            torch.cuda.nvtx.range_push(f"timed_{form}")
+            ms, acc = timed(lambda: step_device(tr, views, gen), args.steps, dev, world)
+            torch.cuda.nvtx.range_pop()
+            _lib.PROFILER.stop()
+        torch.cuda.synchronize(dev)
+        summ = _lib.PROFILER.summary()
+        launches = _lib.PROFILER.launches
+        rays = sum(a[0] for a in acc)
+        samples = sum(a[1] for a in acc)
+        rl, shares = roofline(summ, hbm_peak, peak_kind)
+        # host-fed end-to-end through the public API
+        feed = HostFeed(views, seed=77 + rank)
+        for _ in range(max(1, args.warmup // 2)):
+            step_host(tr, feed, dev)
+        ms_e2e, acc_e = timed(lambda: step_host(tr, feed, dev), args.steps, dev, world)
+        rays_e = sum(a[0] for a in acc_e)
+        if world > 1:
+            t = torch.tensor([rays, rays_e, samples], device=dev, dtype=torch.float64)
+            torch.distributed.all_reduce(t)
+            rays, rays_e, samples = (int(v) for v in t.tolist())
+        results[form] = dict(
+            value=rays / (ms * 1e-3), ms_per_step=ms / args.steps, rays_per_step=rays / args.steps
+            / world, samples_per_step=samples / args.steps / world, roofline=rl,
+            kernel_ms=shares, gpu_launches=launches, clocks=clk.summary(),
+            e2e=dict(value=round(rays_e / (ms_e2e * 1e-3), 1), unit="rays/s",
+                     h2d_bytes_per_step=int(np.mean([a[2] for a in acc_e])),
+                     d2h_bytes_per_step=int(np.mean([a[3] for a in acc_e])),
+                     ms_per_step=round(ms_e2e / args.steps, 3)))
+        del model, tr
+        torch.cuda.empty_cache()
+    head = "fused" if "fused" in results else forms[0]
+    R = results[head]
+    line = {
+        "metric": "train rays/s", "value": round(R["value"], 1), "unit": "rays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(R["ms_per_step"], 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: 8 seeded 1600x1200 views of an "
+        "analytic torus/box/sphere union, Gaussian noise 0.01",
+        "config": {"workload": "neuralangelo-sparse-train (16 lv x 2^22, 128^3 grid, 2^18 "
+                   "samples/step target, FD + curvature)", "form": head,
+                   "rays_per_step": round(R["rays_per_step"], 1),
+                   "samples_per_step": round(R["samples_per_step"], 1),
+                   "global_step": GLOBAL_STEP, "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (hash table 0.43 GB + AdamW state)"},
+        "e2e": R["e2e"], "roofline": R["roofline"], "clocks": R["clocks"],
+        "gpu_launches": R["gpu_launches"], "kernel_ms": R["kernel_ms"],
+        "forms": {f: {"value": round(v["value"], 1), "ms_per_step": round(v["ms_per_step"], 3),
+                      "e2e": v["e2e"]["value"]} for f, v in results.items()},
+    }
+    if "fused" in results and "plain" in results:
+        line["fused_vs_plain"] = round(results["fused"]["value"] / results["plain"]["value"], 3)
+    if rank == 0 and not args.no_cpu_baseline:
+        model, tr = make_trainer("plain", dev)
+        model.update_step(0, GLOBAL_STEP)
+        line["cpu_baseline"] = cpu_baseline(model, views)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    """The reference arm: the oracle's CPU restatement of the same training
+    step (forward + backward) on the host cores, bounded samples per step."""
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    dev = torch.device("cuda:0") if torch.cuda.is_available() else None
+    if dev is None:
+        print(json.dumps({"impl": "reference", "unavailable": "needs a GPU to build the views"}))
+        return
+    from angelo_gb import build
+    build.build()
+    views = make_views(dev)
+    model, tr = make_trainer("plain", dev)
+    model.update_step(0, GLOBAL_STEP)
+    views_cpu = (views.images.cpu(), views.c2w.cpu(), views.dirs.cpu(), views.W, views.H)
+    torch.set_num_threads(os.cpu_count() or 1)
+    dt, _ = cpu_step(model, views_cpu, 16, 5)
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    n = int(max(16, min(2048, budget / max(dt / 16, 1e-6))))
+    for k in range(min(args.warmup, 1)):
+        cpu_step(model, views_cpu, n, 10 + k)
+    t_tot, r_tot, s_tot = 0.0, 0, 0
+    for k in range(args.steps):
+        dt, s = cpu_step(model, views_cpu, n, 100 + k)
+        t_tot += dt
+        r_tot += n
+        s_tot += s
+    v = r_tot / t_tot
+    print(json.dumps({
+        "impl": "reference", "metric": "train rays/s", "value": round(v, 2), "unit": "rays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * t_tot / args.steps, 2), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "neuralangelo-sparse-train (16 lv x 2^22, 128^3 grid, 2^18 "
+                   "samples/step target, FD + curvature)", "rays_per_step": n},
+        "cpu_baseline": {"value": round(v, 2), "unit": "rays/s", "cores": torch.get_num_threads(),
+                         "kind": "port", "sample": f"{args.steps} steps of {n} rays "
+                         f"({s_tot} samples) in the oracle's float32 CPU restatement"},
+        "e2e": {"value": round(v, 2), "unit": "rays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

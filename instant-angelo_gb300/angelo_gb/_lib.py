@@ -96,13 +96,55 @@ def load(path: str = LIB_PATH):
     return _lib
 
 
-def call(name, *args):
-    """Call an int-status entry point; raise AngeloError on a non-zero status."""
+class Profiler:
+    """Opt-in record of library calls: CUDA events on the launching stream
+    around each call, the kernel launches it made and its work units.  Used
+    by bench.py to time the dominant kernel inside the timed region."""
+
+    def __init__(self):
+        self.active = False
+        self.records = []      # (name, start_event, end_event, units)
+        self.launches = 0
+
+    def start(self):
+        self.records, self.launches, self.active = [], 0, True
+
+    def stop(self):
+        self.active = False
+
+    def summary(self):
+        """{name: (calls, total_ms, [units...])} after synchronisation."""
+        out = {}
+        for name, s, e, units in self.records:
+            c, t, u = out.get(name, (0, 0.0, []))
+            u.append(units)
+            out[name] = (c + 1, t + s.elapsed_time(e), u)
+        return out
+
+
+PROFILER = Profiler()
+
+
+def call(name, *args, launches=1, units=None, stream=None):
+    """Call an int-status entry point; raise AngeloError on a non-zero status.
+    ``launches`` is the number of kernels the call puts on the stream and
+    ``units`` its work description, both only recorded while profiling."""
     L = load()
+    prof = PROFILER.active
+    if prof:
+        import torch
+        s = torch.cuda.current_stream()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(s)
     rc = getattr(L, name)(*args)
     if rc != ANGELO_OK:
         msg = L.angelo_last_error_string().decode(errors="replace")
         raise AngeloError(name, rc, msg)
+    if prof:
+        ev1.record(s)
+        PROFILER.records.append((name, ev0, ev1, units))
+        PROFILER.launches += launches
     return rc
 
 

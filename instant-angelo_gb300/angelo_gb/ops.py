@@ -87,7 +87,9 @@ def hashgrid_encode_raw(x, table, spec: HashGridSpec, active_levels, include_xyz
         out_col = 0
     call("angelo_hashgrid_fwd", ctypes.byref(spec.layout), int(active_levels), _p(x), n,
          _p(table), _table_dtype(table), int(bool(include_xyz)), _p(out), out.stride(0),
-         int(out_col), _s(x.device))
+         int(out_col), _s(x.device),
+         units=dict(n=n, active=int(active_levels), L=spec.n_levels,
+                    tbytes=table.element_size(), xyz=bool(include_xyz)))
     return out
 
 
@@ -111,7 +113,10 @@ class _HashGridEncode(torch.autograd.Function):
         if need_x or need_t:
             call("angelo_hashgrid_bwd", ctypes.byref(spec.layout), int(ctx.active), _p(x),
                  x.shape[0], _p(table), _table_dtype(table), int(bool(ctx.include_xyz)),
-                 _p(dout), dout.stride(0), 0, _p(dtable), _p(dx), _s(x.device))
+                 _p(dout), dout.stride(0), 0, _p(dtable), _p(dx), _s(x.device),
+                 launches=int(need_t and ctx.active > 0) + int(need_x),
+                 units=dict(n=x.shape[0], active=int(ctx.active), L=spec.n_levels,
+                            tbytes=table.element_size(), dtable=bool(need_t), dx=bool(need_x)))
         if dtable is not None and table.dtype != torch.float32:
             dtable = dtable.to(table.dtype)
         return dx, dtable, None, None, None
@@ -214,7 +219,7 @@ def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), 
     s = _s(dev)
     call("angelo_march_count", _p(rays_o), _p(rays_d), _p(t_min), _p(t_max), n, ctypes.byref(g),
          float(step), float(cone_angle), int(max_steps), _p(counts), _p(status), s)
-    call("angelo_scan", _p(counts), n, _p(offsets), _p(ws), s)
+    call("angelo_scan", _p(counts), n, _p(offsets), _p(ws), s, launches=3 if n else 0)
     total = int(offsets[n].item())
     ri = torch.empty(total, device=dev, dtype=torch.int32)
     t0 = torch.empty(total, device=dev)
@@ -235,7 +240,8 @@ def scan(counts):
     offsets = torch.empty(n + 1, device=counts.device, dtype=torch.int64)
     ws = torch.empty(_lib.raw("angelo_scan_workspace_size")(n), device=counts.device,
                      dtype=torch.uint8)
-    call("angelo_scan", _p(counts), n, _p(offsets), _p(ws), _s(counts.device))
+    call("angelo_scan", _p(counts), n, _p(offsets), _p(ws), _s(counts.device),
+         launches=3 if n else 0)
     return offsets
 
 
@@ -249,7 +255,7 @@ def occ_update(occs, cells, occ, decay, thre, bits):
     ws = torch.empty(_lib.raw("angelo_occ_workspace_size")(n_cells), device=occs.device,
                      dtype=torch.uint8)
     call("angelo_occ_update", _p(occs), n_cells, _p(cells), _p(occ), cells.numel(), float(decay),
-         float(thre), _p(bits), _p(ws), _s(occs.device))
+         float(thre), _p(bits), _p(ws), _s(occs.device), launches=4 if cells.numel() else 3)
 
 
 # ---------------------------------------------------------------- compositing
@@ -258,6 +264,7 @@ def occ_update(occs, cells, occ, decay, thre, bits):
 class _WeightsFromAlpha(torch.autograd.Function):
     @staticmethod
     def forward(ctx, alpha, offsets, early_stop_eps):
+        ctx.in_shape = alpha.shape
         alpha = _cuda(alpha, "alpha").reshape(-1)
         offsets = _cuda(offsets, "offsets", dtype=torch.int64)
         n_rays = offsets.numel() - 1
@@ -276,7 +283,7 @@ class _WeightsFromAlpha(torch.autograd.Function):
         da = torch.empty_like(alpha)
         call("angelo_weights_bwd", _p(alpha), _p(trans), _p(offsets), offsets.numel() - 1,
              float(ctx.eps), _p(dw), _p(da), _s(alpha.device))
-        return da, None, None
+        return da.view(ctx.in_shape), None, None
 
 
 def render_weight_from_alpha(alpha, offsets, early_stop_eps=1e-4):
@@ -286,6 +293,7 @@ def render_weight_from_alpha(alpha, offsets, early_stop_eps=1e-4):
 class _Accumulate(torch.autograd.Function):
     @staticmethod
     def forward(ctx, weights, values, offsets):
+        ctx.in_shape = weights.shape
         weights = _cuda(weights, "weights").reshape(-1)
         offsets = _cuda(offsets, "offsets", dtype=torch.int64)
         n_rays = offsets.numel() - 1
@@ -307,7 +315,7 @@ class _Accumulate(torch.autograd.Function):
         dv = torch.empty_like(values) if (values is not None and ctx.needs_input_grad[1]) else None
         call("angelo_accumulate_bwd", _p(weights), _p(values), ctx.C, _p(offsets),
              offsets.numel() - 1, _p(dout), _p(dw), _p(dv), _s(weights.device))
-        return dw, dv, None
+        return dw.view(ctx.in_shape), dv, None
 
 
 def accumulate_along_rays(weights, offsets, values=None):

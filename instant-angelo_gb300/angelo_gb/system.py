@@ -1,0 +1,81 @@
+"""The hot-path part of NeuSSystem.training_step (systems/neus.py:120-206):
+loss seeds (rgb MSE on valid rays, eikonal, curvature), dynamic ray-count
+update (:126-128) and the AdamW step of the reference's optimizer config
+(systems/utils.py:314-325).  Data loading, logging, validation and the
+Lightning loop are outside the path."""
+from __future__ import annotations
+
+import torch
+import torch.nn.functional as F
+
+from .config import scheduled_value, to_config
+
+
+def loss_terms(out, rgb, eikonal_weight=0.1, curvature_weight=5e-4, rgb_mse_weight=10.0):
+    """Weighted loss terms of systems/neus.py:130-159 (the ones the hot path
+    seeds).  Returns (total, dict of unweighted terms)."""
+    valid = out["rays_valid_full"][..., 0]
+    l_rgb = F.mse_loss(out["comp_rgb_full"][valid], rgb[valid])
+    l_eik = ((torch.linalg.norm(out["sdf_grad_samples"], ord=2, dim=-1) - 1.0) ** 2).mean()
+    total = l_rgb * rgb_mse_weight + l_eik * eikonal_weight
+    terms = {"rgb_mse": l_rgb, "eikonal": l_eik}
+    if curvature_weight > 0:
+        l_curv = out["sdf_laplace_samples"].abs().mean()
+        total = total + l_curv * curvature_weight
+        terms["curvature"] = l_curv
+    return total, terms
+
+
+class NeuSTrainer:
+    """One training step = update_step (band mask, FD eps, cosine anneal,
+    occupancy refresh every 16 steps) -> forward -> losses -> backward ->
+    AdamW.  Ray counts follow the reference's dynamic sampling rule."""
+
+    def __init__(self, model, system_config=None, train_num_rays=256, max_train_num_rays=8192,
+                 train_num_samples=1 << 18, dynamic_ray_sampling=True):
+        self.model = model
+        sc = to_config(system_config or {})
+        self.loss_cfg = to_config(sc.get("loss", {}))
+        opt = to_config(sc.get("optimizer", {}))
+        args = dict(opt.get("args", {"lr": 0.01, "betas": [0.9, 0.99], "eps": 1e-15}))
+        groups = []
+        per = opt.get("params", {"geometry": {"lr": 0.01}, "texture": {"lr": 0.01},
+                                 "variance": {"lr": 0.001}})
+        for name, a in per.items():
+            mod = getattr(model, name, None)
+            if mod is None:
+                continue
+            params = list(mod.parameters()) if isinstance(mod, torch.nn.Module) else [mod]
+            groups.append({"params": params, "name": name, **a})
+        args["betas"] = tuple(args.get("betas", (0.9, 0.99)))
+        fused = all(p.is_cuda for g in groups for p in g["params"])
+        self.optimizer = torch.optim.AdamW(groups, fused=fused, **args)
+        self.train_num_rays = int(train_num_rays)
+        self.max_train_num_rays = int(max_train_num_rays)
+        self.train_num_samples = int(train_num_samples)
+        self.dynamic = dynamic_ray_sampling
+        self.global_step = 0
+
+    def C(self, v):
+        return scheduled_value(v, self.global_step)
+
+    def step(self, rays, rgb, background_color):
+        m = self.model
+        m.update_step(0, self.global_step)
+        m.background_color = background_color
+        out = m(rays)
+        n_samples = int(out["num_samples_full"].sum().item())
+        if self.dynamic:
+            new = int(self.train_num_rays * (self.train_num_samples / max(n_samples, 1)))
+            self.train_num_rays = min(int(self.train_num_rays * 0.9 + new * 0.1),
+                                      self.max_train_num_rays)
+        lc = self.loss_cfg
+        loss, terms = loss_terms(out, rgb,
+                                 eikonal_weight=self.C(lc.get("lambda_eikonal", 0.1)),
+                                 curvature_weight=self.C(lc.get("lambda_curvature", 5e-4)),
+                                 rgb_mse_weight=self.C(lc.get("lambda_rgb_mse", 10.0)))
+        self.optimizer.zero_grad(set_to_none=True)
+        loss.backward()
+        self.optimizer.step()
+        self.global_step += 1
+        return loss.detach(), n_samples

@@ -105,8 +105,11 @@ def test_encode_backward_against_fp64(dev):
         (o64 * torch.tensor(gout, dtype=torch.float64)).sum().backward()
         # table gradient: float32 atomics of w*g, order not fixed
         np.testing.assert_allclose(tt.grad.cpu().numpy(), t64.grad.numpy(), rtol=1e-4, atol=1e-4)
-        # input gradient: sums of scale * table differences (scale up to ~30)
-        np.testing.assert_allclose(xt.grad.cpu().numpy(), x64.grad.numpy(), rtol=1e-3, atol=2e-3)
+        # input gradient: sums over levels of scale * table differences, with
+        # cancellation; compared relative to the largest component
+        ref = x64.grad.numpy()
+        np.testing.assert_allclose(xt.grad.cpu().numpy(), ref, rtol=1e-4,
+                                   atol=2e-5 * np.abs(ref).max())
 
 
 def test_sh4(dev):
