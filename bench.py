@@ -228,9 +228,22 @@ def algorithmic_bytes(name, u):
         if u["dx"]:
             b += u["active"] * 8 * 2 * u["tbytes"] + 12
         return u["n"] * b
-    if name.startswith("angelo_sdf_stencil") or name.startswith("angelo_radiance") or \
-            name.startswith("angelo_composite"):
-        return u.get("bytes")
+    if name == "angelo_sdf_stencil_fwd":
+        # per sample: position + curvature direction, the gathers of every
+        # evaluation (8 corners x 2 features per active level), outputs
+        # (sdf, grad, feature [od + 3], laplace) and, in training, the stash
+        # (13 x 36 encodings + 13 sdf values)
+        per = (24 + u["evals"] * u["active"] * 16 * u["tbytes"] + 4 + 12 + (u["od"] + 3) * 4 + 4
+               + (13 * 36 * 4 + 13 * 4 if u["train"] else 0))
+        return u["n"] * per
+    if name == "angelo_sdf_stencil_bwd":
+        # per sample: position, direction, stash, incoming gradients, table
+        # atomics (read + write) of every evaluation, and the re-gathered
+        # corners of the 6 shifted evaluations (positional derivative)
+        shifted = 6 if u["evals"] == 13 else 0
+        per = (24 + 13 * 36 * 4 + 13 * 4 + 4 + 12 + u["od"] * 4 + 4
+               + u["evals"] * u["active"] * 16 * 4 * 2 + shifted * u["active"] * 16 * u["tbytes"])
+        return u["n"] * per
     return None
 
 
@@ -358,9 +371,13 @@ def run_ours(args):
             step_device(tr, views, gen)
         with Clocks(local) as clk:
             _lib.PROFILER.start()
-            torch.cuda.nvtx.range_push(f"timed_{form}")
+            # profiler range (cudaProfilerStart/Stop) marks the timed steps
+            # for a capture started with --profile-from-start off; the
+            # backward kernels launch from autograd's own thread, which an
+            # NVTX range of this thread would not cover
+            torch.cuda.profiler.start()
             ms, acc = timed(lambda: step_device(tr, views, gen), args.steps, dev, world)
-            torch.cuda.nvtx.range_pop()
+            torch.cuda.profiler.stop()
             _lib.PROFILER.stop()
         torch.cuda.synchronize(dev)
         summ = _lib.PROFILER.summary()

@@ -175,6 +175,62 @@ int angelo_accumulate_bwd(const float *weights, const float *values, int32_t cha
                           const int64_t *offsets, int64_t n_rays, const float *dout,
                           float *dweights, float *dvalues, void *stream);
 
+/* ------------------------------------------------------------ fused VolumeSDF */
+
+/* Prepared geometry-MLP operands: bf16 hi/lo tensor-core fragments of every
+ * layer (forward and backward order), fp32 biases.  Layout by query. */
+typedef struct {
+    int32_t k_tiles1, n_hidden, n_tiles3, k_tiles3b, out_dim;
+    int64_t off_w1f, off_w2f, off_w3f, off_w1b, off_w2b, off_w3b;
+    int64_t off_b1, off_b2, off_b3, off_w3row0;
+    int64_t bytes;
+} angelo_sdf_net_layout;
+
+int angelo_sdf_net_layout_query(int32_t n_levels, int32_t n_hidden, int32_t out_dim,
+                                angelo_sdf_net_layout *out);
+
+/* Convert the effective fp32 weights of the reference's VanillaMLP
+ * (models/network_utils.py:96-140, after weight normalisation; W row-major
+ * (out, in), reference input order [x*2-1, hash]) into the prepared buffer.
+ * W2/b2 are ignored with one hidden layer. */
+int angelo_sdf_prep(const angelo_sdf_net_layout *lay, int32_t n_levels, int32_t in_dim,
+                    const float *W1, const float *b1, const float *W2, const float *b2,
+                    const float *W3, const float *b3, void *net, void *stream);
+
+/* Number of floats of the flat weight gradient written by the backward:
+ * [dW1 (64 x 16*k_tiles1, kernel column order: hash, xyz, pad), dW2 (64 x 64),
+ *  dW3 (16*k_tiles3b x 64), db1 (64), db2 (64), db3 (16*k_tiles3b)]. */
+int64_t angelo_sdf_grad_size(const angelo_sdf_net_layout *lay);
+
+/* Fused VolumeSDF.forward with grad_type='finite_difference'
+ * (models/geometry.py:195-287): per sample the point, the 6-tap FD stencil
+ * and the 6-tap curvature stencil (13 hash-grid + MLP evaluations), with the
+ * reference's quirks (clamped stencil divided by 2 eps; curvature shift in
+ * contracted coordinates then clamped as world coordinates).  pos: (n,3)
+ * world points; rand_dirs: (n,3), the randn of models/geometry.py:238.
+ * Outputs sdf (n), grad (n,3), feature (n, feat_stride >= out_dim+3:
+ * [MLP output, x*2-1]), laplace (n).  stash_x (n,13,36) and stash_s (n,13)
+ * (both or neither) keep what the backward needs. */
+int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32_t active_levels,
+                           const void *table, int32_t table_dtype, const angelo_sdf_net_layout *nl,
+                           const void *net, const float *pos, const float *rand_dirs, int64_t n,
+                           float radius, float eps, int32_t with_grad, int32_t with_laplace,
+                           int32_t with_feature, float *sdf, float *grad, float *feature,
+                           int64_t feat_stride, float *laplace, float *stash_x, float *stash_s,
+                           void *stream);
+
+/* Backward of the fused VolumeSDF: from dL/dsdf, dL/dgrad, dL/dfeature
+ * (any may be NULL), dL/dlaplace, ACCUMULATES dL/dtable (float32, atomic)
+ * and dL/dnet (angelo_sdf_grad_size floats, atomic).  The curvature path
+ * includes the hash grid's positional derivative at the shifted stencil. */
+int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32_t active_levels,
+                           const void *table, int32_t table_dtype, const angelo_sdf_net_layout *nl,
+                           const void *net, const float *pos, const float *rand_dirs, int64_t n,
+                           float radius, float eps, int32_t with_grad, int32_t with_laplace,
+                           const float *stash_x, const float *stash_s, const float *g_sdf,
+                           const float *g_grad, const float *g_feature, int64_t gfeat_stride,
+                           const float *g_laplace, float *d_table, float *d_net, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,15 @@ class GridDesc(ctypes.Structure):
     _fields_ = [("roi", c_f32 * 6), ("res", c_i32 * 3), ("bits", c_vp)]
 
 
+class SdfNetLayout(ctypes.Structure):
+    _fields_ = [("k_tiles1", c_i32), ("n_hidden", c_i32), ("n_tiles3", c_i32),
+                ("k_tiles3b", c_i32), ("out_dim", c_i32),
+                ("off_w1f", c_i64), ("off_w2f", c_i64), ("off_w3f", c_i64),
+                ("off_w1b", c_i64), ("off_w2b", c_i64), ("off_w3b", c_i64),
+                ("off_b1", c_i64), ("off_b2", c_i64), ("off_b3", c_i64),
+                ("off_w3row0", c_i64), ("bytes", c_i64)]
+
+
 class AngeloError(RuntimeError):
     def __init__(self, fn, code, msg):
         super().__init__(f"{fn} failed with status {code}: {msg}")
@@ -72,6 +81,16 @@ SIGNATURES = {
     "angelo_weights_bwd": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_f32, c_vp, c_vp, c_vp]),
     "angelo_accumulate_fwd": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp]),
     "angelo_accumulate_bwd": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_sdf_net_layout_query": (c_i32, [c_i32, c_i32, c_i32, _P(SdfNetLayout)]),
+    "angelo_sdf_prep": (c_i32, [_P(SdfNetLayout), c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                c_vp, c_vp, c_vp]),
+    "angelo_sdf_grad_size": (c_i64, [_P(SdfNetLayout)]),
+    "angelo_sdf_stencil_fwd": (c_i32, [_P(HashGridLayout), c_i32, c_vp, c_i32, _P(SdfNetLayout),
+                                       c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_i32, c_i32, c_i32,
+                                       c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_sdf_stencil_bwd": (c_i32, [_P(HashGridLayout), c_i32, c_vp, c_i32, _P(SdfNetLayout),
+                                       c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_i32, c_i32, c_vp,
+                                       c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
 }
 
 _lock = threading.Lock()
