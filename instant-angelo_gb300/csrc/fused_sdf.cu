@@ -1057,7 +1057,7 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
     ANGELO_REQUIRE(lay && nl && net && table, "sdf_stencil_fwd: null argument");
     ANGELO_REQUIRE(n >= 0, "sdf_stencil_fwd: negative n");
     if (n == 0) return ANGELO_OK;
-    ANGELO_REQUIRE(lay->n_levels == 2 * 8 * (nl->k_tiles1 - 1), "sdf_stencil_fwd: levels vs net");
+    ANGELO_REQUIRE(lay->n_levels == 8 * (nl->k_tiles1 - 1), "sdf_stencil_fwd: levels vs net");
     ANGELO_REQUIRE(active_levels >= 0 && active_levels <= lay->n_levels, "sdf_stencil_fwd: active");
     ANGELO_REQUIRE(pos && sdf, "sdf_stencil_fwd: null pos/sdf");
     ANGELO_REQUIRE(!with_laplace || with_grad, "sdf_stencil_fwd: laplace needs the gradient");
@@ -1152,7 +1152,7 @@ extern "C" int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32
                    "sdf_stencil_bwd: null argument");
     ANGELO_REQUIRE(n >= 0, "sdf_stencil_bwd: negative n");
     if (n == 0) return ANGELO_OK;
-    ANGELO_REQUIRE(lay->n_levels == 2 * 8 * (nl->k_tiles1 - 1), "sdf_stencil_bwd: levels vs net");
+    ANGELO_REQUIRE(lay->n_levels == 8 * (nl->k_tiles1 - 1), "sdf_stencil_bwd: levels vs net");
     ANGELO_REQUIRE(!with_laplace || (with_grad && rand_dirs), "sdf_stencil_bwd: laplace inputs");
     ANGELO_REQUIRE(g_feature == nullptr || gfeat_stride >= nl->out_dim, "sdf_stencil_bwd: stride");
     SdfParams P{};
