@@ -134,6 +134,19 @@ int64_t angelo_scan_workspace_size(int64_t n);
 int angelo_scan(const int32_t *counts, int64_t n, int64_t *offsets, void *workspace,
                 void *stream);
 
+/* Allocation-free exclusive scan: same result as angelo_scan, for callers
+ * that cannot allocate device memory (a host that gives the library only
+ * fixed, pre-sized buffers from its own pool, or code that may not call
+ * cudaMalloc where it runs).  This entry point has no counterpart in the
+ * reference.  Its workspace is a fixed 128 KiB array inside the library that
+ * every GPU loading the library keeps until the process exits; n may be at
+ * most ANGELO_SCAN_NOALLOC_MAX_N (larger n returns ANGELO_E_INVALID).  All
+ * calls share that array: calls whose kernels overlap on the GPU race, so
+ * order them on one stream.  The first call on a device looks up the array's
+ * address with that device current; make it before any stream capture. */
+#define ANGELO_SCAN_NOALLOC_MAX_N (1LL << 24)
+int angelo_scan_noalloc(const int32_t *counts, int64_t n, int64_t *offsets, void *stream);
+
 /* Pass 2: writes ray_indices (int32), t_starts, t_ends at offsets[i] + j.
  * Samples at or past capacity are dropped and status bit 1 is set. */
 int angelo_march_fill(const float *rays_o, const float *rays_d, const float *t_min,

@@ -72,6 +72,7 @@ SIGNATURES = {
                                    c_i64, c_vp, c_vp, c_vp]),
     "angelo_scan_workspace_size": (c_i64, [c_i64]),
     "angelo_scan": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "angelo_scan_noalloc": (c_i32, [c_vp, c_i64, c_vp, c_vp]),
     "angelo_march_fill": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, _P(GridDesc), c_f32, c_f32,
                                   c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "angelo_occ_workspace_size": (c_i64, [c_i64]),
