@@ -184,3 +184,218 @@ def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
 def sdf_query(geom, points):
     """forward_level: SDF only, one evaluation per point."""
     return volume_sdf_forward(geom, points, False, False, False)[0]
+
+
+# ----------------------------------------------------------------- radiance
+
+
+class RadNet:
+    """Prepared tensor-core operands of a 2-hidden-layer ReLU radiance MLP
+    (VolumeRadiance / VolumeDualColor, models/texture.py:10-64)."""
+
+    def __init__(self, feat_dim, device):
+        self.feat_dim = int(feat_dim)
+        nbytes = _lib.raw("angelo_radiance_net_bytes")(self.feat_dim)
+        if nbytes < 0:
+            raise ValueError(f"radiance feature width {feat_dim} not supported by the fused kernel")
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, device=device)
+        self.grad_size = _lib.raw("angelo_radiance_grad_size")(self.feat_dim)
+        self.in_dim = self.feat_dim + 19
+        self.k1cols = 16 * ((self.in_dim + 15) // 16)
+
+    def prepare(self, Ws):
+        ts = [t.detach().float().contiguous() for W, b in Ws for t in (W, b)]
+        call("angelo_radiance_prep", self.feat_dim, *[_p(t) for t in ts], _p(self.buf),
+             _s(self.buf.device))
+
+    def unpack_grads(self, g):
+        k1 = self.k1cols
+        o = 0
+        dW1 = g[o:o + 64 * k1].view(64, k1)[:, :self.in_dim]
+        o += 64 * k1
+        dW2 = g[o:o + 4096].view(64, 64)
+        o += 4096
+        dW3 = g[o:o + 16 * 64].view(16, 64)[:3]
+        o += 16 * 64
+        return [(dW1, g[o:o + 64]), (dW2, g[o + 64:o + 128]), (dW3, g[o + 128:o + 131])]
+
+
+class _FusedRadiance(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, feature, grad, ray_idx, rays_d, meta, *weights):
+        net, dual = meta["net"], meta["dual"]
+        net.prepare([(weights[2 * i], weights[2 * i + 1]) for i in range(3)])
+        feature = feature.contiguous()
+        grad = grad.contiguous()
+        S = feature.shape[0]
+        rgb = torch.empty(S, 3, device=feature.device)
+        call("angelo_radiance_fwd", net.feat_dim, _p(net.buf), _p(feature), feature.stride(0),
+             _p(grad), _p(ray_idx), _p(rays_d), S, int(dual), _p(rgb), _s(feature.device),
+             units=dict(n=S, F=net.feat_dim, bwd=False))
+        ctx.save_for_backward(feature, grad, ray_idx, rays_d)
+        ctx.meta = meta
+        return rgb
+
+    @staticmethod
+    def backward(ctx, g_rgb):
+        feature, grad, ray_idx, rays_d = ctx.saved_tensors
+        net, dual = ctx.meta["net"], ctx.meta["dual"]
+        S = feature.shape[0]
+        g_rgb = g_rgb.contiguous().float()
+        d_feature = torch.zeros_like(feature)
+        d_grad = torch.empty_like(grad)
+        d_net = torch.zeros(net.grad_size, device=feature.device)
+        call("angelo_radiance_bwd", net.feat_dim, _p(net.buf), _p(feature), feature.stride(0),
+             _p(grad), _p(ray_idx), _p(rays_d), S, int(dual), _p(g_rgb), _p(d_feature),
+             _p(d_grad), _p(d_net), _s(feature.device),
+             units=dict(n=S, F=net.feat_dim, bwd=True))
+        flat = []
+        for dW, db in net.unpack_grads(d_net):
+            flat += [dW, db]
+        return (d_feature, d_grad, None, None, None, *flat)
+
+
+def radiance_forward(texture, feature, grad, ray_idx, rays_d):
+    net = getattr(texture, "_fused_net", None)
+    F_ = feature.shape[-1]
+    if net is None or net.feat_dim != F_ or net.buf.device != feature.device:
+        net = RadNet(F_, feature.device)
+        texture._fused_net = net
+    weights = []
+    for W, b in texture.network.effective_weights():
+        weights += [W, b]
+    meta = dict(net=net, dual=bool(getattr(texture, "dual", False)))
+    return _FusedRadiance.apply(feature, grad, ray_idx, rays_d, meta, *weights)
+
+
+# --------------------------------------------------------------- compositing
+
+FP64_ALPHA_GATE = 2048.0
+# the fused radiance / compositing kernels are used by neus_forward when set
+FUSED_RENDER = False
+
+
+class _FusedComposite(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, sdf, grad, rgb, variance, t0, t1, offsets, rays_d, bg, meta):
+        n_rays = offsets.numel() - 1
+        S = sdf.numel()
+        dev = sdf.device
+        sdf, grad, rgb = sdf.contiguous(), grad.contiguous(), rgb.contiguous()
+        opacity = torch.empty(n_rays, 1, device=dev)
+        depth = torch.empty(n_rays, 1, device=dev)
+        comp_rgb = torch.empty(n_rays, 3, device=dev)
+        comp_normal = torch.empty(n_rays, 3, device=dev)
+        comp_full = torch.empty(n_rays, 3, device=dev)
+        acc_n = torch.empty(n_rays, 3, device=dev)
+        weights = torch.empty(S, device=dev)
+        trans = torch.empty(S, device=dev)
+        call("angelo_composite_fwd", _p(offsets), n_rays, _p(sdf), _p(grad), _p(t0), _p(t1),
+             _p(rays_d), _p(rgb), _p(variance), float(meta["cos_ratio"]), _p(bg),
+             float(meta["eps"]), float(meta["gate"]), _p(opacity), _p(depth), _p(comp_rgb),
+             _p(comp_normal), _p(comp_full), _p(acc_n), _p(weights), _p(trans), _p(None),
+             _s(dev), units=dict(n=S, rays=n_rays, bwd=False))
+        ctx.save_for_backward(sdf, grad, rgb, variance, t0, t1, offsets, rays_d, bg, opacity,
+                              acc_n, weights, trans)
+        ctx.meta = meta
+        ctx.mark_non_differentiable(weights)
+        return opacity, depth, comp_rgb, comp_normal, comp_full, weights
+
+    @staticmethod
+    def backward(ctx, g_op, g_depth, g_rgb, g_normal, g_full, g_weights):
+        (sdf, grad, rgb, variance, t0, t1, offsets, rays_d, bg, opacity, acc_n, weights,
+         trans) = ctx.saved_tensors
+        meta = ctx.meta
+        n_rays = offsets.numel() - 1
+        S = sdf.numel()
+        dev = sdf.device
+
+        def c(t):
+            return t.contiguous().float() if t is not None else None
+        d_sdf = torch.empty_like(sdf)
+        d_grad = torch.empty_like(grad)
+        d_rgb = torch.empty_like(rgb)
+        d_var = torch.zeros(1, device=dev)
+        call("angelo_composite_bwd", _p(offsets), n_rays, _p(sdf), _p(grad), _p(t0), _p(t1),
+             _p(rays_d), _p(rgb), _p(variance), float(meta["cos_ratio"]), _p(bg),
+             float(meta["eps"]), float(meta["gate"]), _p(opacity), _p(acc_n), _p(weights),
+             _p(trans), _p(c(g_op)), _p(c(g_depth)), _p(c(g_rgb)), _p(c(g_normal)),
+             _p(c(g_full)), _p(d_sdf), _p(d_grad), _p(d_rgb), _p(d_var), _s(dev),
+             units=dict(n=S, rays=n_rays, bwd=True))
+        return (d_sdf, d_grad, d_rgb, d_var.view(variance.shape), None, None, None, None, None,
+                None)
+
+
+def neus_forward(model, rays_o, rays_d, ri, t0, t1, offsets, n_rays):
+    """NeuSModel.forward_ (models/neus.py:205-283) on the fused kernels:
+    fused VolumeSDF -> fused radiance (VolumeRadiance / VolumeDualColor) ->
+    fused compositing; VolumeDualColorV3 runs its own module between them."""
+    ray_indices = ri.long()
+    mid = (t0 + t1) * 0.5
+    positions = rays_o[ray_indices] + rays_d[ray_indices] * mid[:, None]
+    sdf, sdf_grad, feature, sdf_laplace = model.geometry(positions, with_grad=True,
+                                                         with_feature=True, with_laplace=True)
+    tex = model.texture
+    if not FUSED_RENDER:
+        return _plain_render(model, rays_o, rays_d, ray_indices, t0, t1, offsets, sdf, sdf_grad,
+                             feature, sdf_laplace)
+    if type(tex).__name__ in ("VolumeRadiance", "VolumeDualColor") and \
+            tex.config.get("color_activation") == "sigmoid":
+        rgb = radiance_forward(tex, feature, sdf_grad, ri, rays_d)
+    else:
+        normal = torch.nn.functional.normalize(sdf_grad, p=2, dim=-1)
+        rgb = tex(feature, rays_d[ray_indices], normal)
+    bg = model.background_color
+    if bg is None:
+        raise RuntimeError("set model.background_color before rendering")
+    meta = dict(cos_ratio=model.cos_anneal_ratio, eps=1e-4, gate=FP64_ALPHA_GATE)
+    variance = model.variance.variance.view(1)
+    opacity, depth, comp_rgb, comp_normal, comp_full, weights = _FusedComposite.apply(
+        sdf, sdf_grad, rgb, variance, t0, t1, offsets, rays_d, bg.float().contiguous(), meta)
+    out = {
+        "comp_rgb": comp_rgb, "comp_normal": comp_normal, "opacity": opacity, "depth": depth,
+        "rays_valid": opacity > 0,
+        "num_samples": torch.as_tensor([len(t0)], dtype=torch.int32, device=rays_o.device),
+    }
+    if model.training:
+        out.update({"sdf_samples": sdf, "sdf_grad_samples": sdf_grad, "weights": weights,
+                    "points": mid, "intervals": t1 - t0, "ray_indices": ray_indices,
+                    "sdf_laplace_samples": sdf_laplace})
+    out_bg = {"comp_rgb": bg[None, :].expand(*comp_rgb.shape),
+              "num_samples": torch.zeros_like(out["num_samples"]),
+              "rays_valid": torch.zeros_like(out["rays_valid"])}
+    out_full = {"comp_rgb": comp_full,
+                "num_samples": out["num_samples"] + out_bg["num_samples"],
+                "rays_valid": out["rays_valid"] | out_bg["rays_valid"]}
+    return {**out, **{k + "_bg": v for k, v in out_bg.items()},
+            **{k + "_full": v for k, v in out_full.items()}}
+
+
+def _plain_render(model, rays_o, rays_d, ray_indices, t0, t1, offsets, sdf, sdf_grad, feature,
+                  sdf_laplace):
+    """The reference's texture / alpha / compositing steps on the library's
+    plain kernels, after the fused geometry."""
+    from . import ops
+    F = torch.nn.functional
+    t_dirs = rays_d[ray_indices]
+    mid = ((t0 + t1) / 2.0)[:, None]
+    dists = (t1 - t0)[:, None]
+    normal = F.normalize(sdf_grad, p=2, dim=-1)
+    alpha = model.get_alpha(sdf, normal, t_dirs, dists)[..., None]
+    rgb = model.texture(feature, t_dirs, normal)
+    weights = ops.render_weight_from_alpha(alpha, offsets)[:, None]
+    opacity = ops.accumulate_along_rays(weights, offsets)
+    depth = ops.accumulate_along_rays(weights, offsets, mid)
+    comp_rgb = ops.accumulate_along_rays(weights, offsets, rgb)
+    rays_fg = opacity > 0.1
+    comp_normal = F.normalize(ops.accumulate_along_rays(weights, offsets, normal), p=2, dim=-1)
+    comp_normal = torch.where(rays_fg, comp_normal, torch.zeros_like(comp_normal))
+    out = {"comp_rgb": comp_rgb, "comp_normal": comp_normal, "opacity": opacity, "depth": depth,
+           "rays_valid": opacity > 0,
+           "num_samples": torch.as_tensor([len(t0)], dtype=torch.int32, device=rays_o.device)}
+    if model.training:
+        out.update({"sdf_samples": sdf, "sdf_grad_samples": sdf_grad,
+                    "weights": weights.view(-1), "points": mid.view(-1),
+                    "intervals": dists.view(-1), "ray_indices": ray_indices.view(-1),
+                    "sdf_laplace_samples": sdf_laplace})
+    return model._with_background(out, comp_rgb)

@@ -98,6 +98,39 @@ __device__ __forceinline__ uint32_t corner_index(const angelo_hashgrid_layout_t 
                       p.g[2] + ((c >> 2) & 1));
 }
 
+// Warp-aggregated float2 atomic add into a hash table.  The lanes of one
+// group (lane % STRIDE equal) are visited in lane order; a run of consecutive
+// group lanes with the same entry is summed by a segmented suffix scan and
+// only the run's first lane issues the atomic.  Consecutive samples along a
+// ray fall into the same coarse cells, so at coarse levels a run covers most
+// of the group.  Every lane of the warp must call this (warp-collective).
+template <int STRIDE>
+__device__ __forceinline__ void aggregated_add2(float2 *table, uint64_t entry, float v0, float v1,
+                                                bool active) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t key = active ? entry : ~0ull;
+    const uint64_t prev = __shfl_up_sync(0xffffffffu, key, STRIDE);
+    const bool head = lane < STRIDE || prev != key;
+    const uint32_t heads = __ballot_sync(0xffffffffu, head);
+    uint32_t group = 0;
+#pragma unroll
+    for (int i = 0; i < 32; i += STRIDE) group |= 1u << i;
+    group <<= (lane % STRIDE);
+    const uint32_t upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+    const int run = __popc(heads & group & upto);
+#pragma unroll
+    for (int o = STRIDE; o < 32; o <<= 1) {
+        const float a = __shfl_down_sync(0xffffffffu, v0, o);
+        const float b = __shfl_down_sync(0xffffffffu, v1, o);
+        const int r2 = __shfl_down_sync(0xffffffffu, run, o);
+        if (lane + o < 32 && r2 == run) {
+            v0 += a;
+            v1 += b;
+        }
+    }
+    if (active && head && (v0 != 0.0f || v1 != 0.0f)) atomicAdd(table + entry, make_float2(v0, v1));
+}
+
 __device__ __forceinline__ float2 load_entry(const void *table, int dtype, uint64_t entry) {
     if (dtype == ANGELO_DTYPE_F32) {
         return __ldg(reinterpret_cast<const float2 *>(table) + entry);

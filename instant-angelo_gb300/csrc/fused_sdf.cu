@@ -19,7 +19,7 @@
 #include <math.h>
 
 #include "common.cuh"
-#include "mma.cuh"
+#include "mlp.cuh"
 
 using namespace angelo;
 
@@ -37,8 +37,6 @@ struct NetSmem {
     const uint2 *w1f, *w2f, *w3f;  // hi at [0, n), lo at [n, 2n)
     const float *b1, *b2, *b3;
 };
-
-__host__ __device__ inline int64_t frag_count(int kt, int nt) { return (int64_t)kt * nt * 32; }
 
 // ------------------------------------------------------------------- prep
 // Effective fp32 weights (after weight normalisation) -> bf16 hi/lo B
@@ -291,49 +289,7 @@ __device__ __forceinline__ void load_rows(const float *st0, const float *st1, in
 }
 
 // Hidden layer: D (8 n-tiles) = A (KT k-tiles) x W + b, fp32 C layout.
-template <int KT>
-__device__ __forceinline__ void hidden_layer(const uint32_t (&ah)[KT][4], const uint32_t (&al)[KT][4],
-                                             const uint2 *wf, const float *bias, int lane,
-                                             float (&D)[8][4]) {
-    const int c = (lane & 3) * 2;
-    const int64_t n_frag = frag_count(KT, 8);
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt) {
-        const float b0 = bias[nt * 8 + c], b1 = bias[nt * 8 + c + 1];
-        D[nt][0] = 0.f;
-        D[nt][1] = 0.f;
-        D[nt][2] = 0.f;
-        D[nt][3] = 0.f;
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) {
-            const int64_t i = (int64_t)(kt * 8 + nt) * 32 + lane;
-            mma_x3(D[nt], ah[kt], al[kt], wf[i], wf[n_frag + i]);
-        }
-        D[nt][0] += b0;
-        D[nt][1] += b1;
-        D[nt][2] += b0;
-        D[nt][3] += b1;
-    }
-}
-
 // C layout (8 n-tiles) -> softplus -> split A fragments (4 k-tiles)
-__device__ __forceinline__ void activate(const float (&Z)[8][4], uint32_t (&hh)[4][4],
-                                         uint32_t (&hl)[4][4]) {
-#pragma unroll
-    for (int kt = 0; kt < 4; ++kt) {
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const float(&z)[4] = Z[2 * kt + half];
-            const Split s0 = split2(softplus100(z[0]), softplus100(z[1]));
-            const Split s1 = split2(softplus100(z[2]), softplus100(z[3]));
-            hh[kt][2 * half] = s0.hi;
-            hl[kt][2 * half] = s0.lo;
-            hh[kt][2 * half + 1] = s1.hi;
-            hl[kt][2 * half + 1] = s1.lo;
-        }
-    }
-}
-
 // Output layer restricted to the first NTO n-tiles
 template <int NTO>
 __device__ __forceinline__ void out_layer(const uint32_t (&hh)[4][4], const uint32_t (&hl)[4][4],
@@ -522,96 +478,12 @@ struct BwdSmem {
     int K1cols, out_pad;                         // 16*k_tiles1, 16*k_tiles3b
 };
 
-__device__ __forceinline__ void red_add(float *p, float v) {
-    asm volatile("red.shared.add.f32 [%0], %1;\n" ::"r"((unsigned)__cvta_generic_to_shared(p)), "f"(v)
-                 : "memory");
-}
-
 // C layout -> split A fragments, no activation
-__device__ __forceinline__ void c_to_a(const float (&C)[8][4], uint32_t (&h)[4][4], uint32_t (&l)[4][4]) {
-#pragma unroll
-    for (int kt = 0; kt < 4; ++kt)
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const float(&z)[4] = C[2 * kt + half];
-            const Split s0 = split2(z[0], z[1]), s1 = split2(z[2], z[3]);
-            h[kt][2 * half] = s0.hi;
-            l[kt][2 * half] = s0.lo;
-            h[kt][2 * half + 1] = s1.hi;
-            l[kt][2 * half + 1] = s1.lo;
-        }
-}
-
 // dW[n][k] += sum_m dZ[m][n] X[m][k] for a 16-row tile.  dZ given as split A
 // fragments over n (KTN k-tiles), X as split A fragments over k (KTK k-tiles);
 // both are transposed 8x8-blockwise with movmatrix.
-template <int KTN, int KTK>
-__device__ __forceinline__ void accumulate_dw(const uint32_t (&zh)[KTN][4], const uint32_t (&zl)[KTN][4],
-                                              const uint32_t (&xh)[KTK][4], const uint32_t (&xl)[KTK][4],
-                                              float *dW, int ld, int lane) {
-    const int r = lane >> 2, c = (lane & 3) * 2;
-#pragma unroll
-    for (int mt = 0; mt < KTN; ++mt) {
-        uint32_t ah[4], al[4];
-        ah[0] = movmatrix_t(zh[mt][0]);
-        ah[1] = movmatrix_t(zh[mt][2]);
-        ah[2] = movmatrix_t(zh[mt][1]);
-        ah[3] = movmatrix_t(zh[mt][3]);
-        al[0] = movmatrix_t(zl[mt][0]);
-        al[1] = movmatrix_t(zl[mt][2]);
-        al[2] = movmatrix_t(zl[mt][1]);
-        al[3] = movmatrix_t(zl[mt][3]);
-#pragma unroll
-        for (int ntp = 0; ntp < 2 * KTK; ++ntp) {
-            const int kt = ntp >> 1, hf = (ntp & 1) * 2;
-            const uint2 bh = make_uint2(movmatrix_t(xh[kt][hf]), movmatrix_t(xh[kt][hf + 1]));
-            const uint2 bl = make_uint2(movmatrix_t(xl[kt][hf]), movmatrix_t(xl[kt][hf + 1]));
-            float d[4] = {0.f, 0.f, 0.f, 0.f};
-            mma_x3(d, ah, al, bh, bl);
-            float *row0 = dW + (mt * 16 + r) * ld + ntp * 8 + c;
-            float *row1 = row0 + 8 * ld;
-            red_add(row0, d[0]);
-            red_add(row0 + 1, d[1]);
-            red_add(row1, d[2]);
-            red_add(row1 + 1, d[3]);
-        }
-    }
-}
-
 // db[n] += sum over the 16 rows of a C-layout tile set (8 n-tiles)
-template <int NT>
-__device__ __forceinline__ void accumulate_db(const float (&C)[NT][4], float *db, int lane) {
-#pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-        float a = C[nt][0] + C[nt][2], b = C[nt][1] + C[nt][3];
-#pragma unroll
-        for (int o = 4; o < 32; o <<= 1) {
-            a += __shfl_xor_sync(0xffffffffu, a, o);
-            b += __shfl_xor_sync(0xffffffffu, b, o);
-        }
-        if (lane < 4) {
-            red_add(db + nt * 8 + lane * 2, a);
-            red_add(db + nt * 8 + lane * 2 + 1, b);
-        }
-    }
-}
-
 // D (NTO n-tiles) = A (4 k-tiles) x Bfrags (KT=4, NT=NT) without bias
-template <int KT, int NTO>
-__device__ __forceinline__ void mm_nobias(const uint32_t (&ah)[KT][4], const uint32_t (&al)[KT][4],
-                                          const uint2 *wf, int NT, int lane, float (&D)[NTO][4]) {
-    const int64_t n_frag = frag_count(KT, NT);
-#pragma unroll
-    for (int nt = 0; nt < NTO; ++nt) {
-        D[nt][0] = D[nt][1] = D[nt][2] = D[nt][3] = 0.f;
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) {
-            const int64_t i = (int64_t)(kt * NT + nt) * 32 + lane;
-            mma_x3(D[nt], ah[kt], al[kt], wf[i], wf[n_frag + i]);
-        }
-    }
-}
-
 // Backward of one evaluation (rows r, r+8 of the tile).  MODE 0: main point
 // (full output gradient from dL/dsdf and dL/dfeature), 1: FD stencil point
 // (SDF gradient only), 2: shifted stencil point (SDF gradient only, plus the
@@ -743,23 +615,29 @@ __device__ __forceinline__ void eval_bwd(const SdfParams &P, const BwdSmem &S, W
 #pragma unroll
     for (int j = 0; j < 2 * KH; ++j) {
         const int l = q + 4 * j;
-        if (l >= P.active) continue;
+        const bool lvl_on = l < P.active;
         const uint64_t base = P.lay.offsets[l];
         const float sc = P.lay.scales[l];
 #pragma unroll
         for (int rr = 0; rr < 2; ++rr) {
-            const bool valid = rr ? v1 : v0;
+            const bool valid = (rr ? v1 : v0) && lvl_on;
             const float g0 = dX[j][2 * rr], g1 = dX[j][2 * rr + 1];
-            if (!valid || (g0 == 0.f && g1 == 0.f)) continue;
+            const bool live = valid && (g0 != 0.f || g1 != 0.f);
             const float *xc = rr ? xc1 : xc0;
             const LevelPos p = level_pos(xc[0], xc[1], xc[2], sc);
             float dl[3] = {0.f, 0.f, 0.f};
 #pragma unroll
             for (int cc = 0; cc < 8; ++cc) {
                 const float w = corner_weight(p, cc);
-                const uint64_t ent = base + corner_index(P.lay, l, p, cc);
-                if (dt) atomicAdd(dt + ent, make_float2(w * g0, w * g1));
-                if (MODE == 2) {
+                const uint64_t ent = live ? base + corner_index(P.lay, l, p, cc) : 0;
+                // levels 0..7 (j < 2) are coarse: the 16 rows of the tile are
+                // consecutive samples and mostly share corners, so aggregate
+                // over the 8 lanes of a level group (lane stride 4) first
+                if (dt) {
+                    if (j < 2) aggregated_add2<4>(dt, ent, w * g0, w * g1, live);
+                    else if (live) atomicAdd(dt + ent, make_float2(w * g0, w * g1));
+                }
+                if (MODE == 2 && live) {
                     const float2 v = load_entry(P.table, P.tdtype, ent);
                     const float gv = g0 * v.x + g1 * v.y;
 #pragma unroll
@@ -806,16 +684,6 @@ __device__ __forceinline__ void eval_bwd(const SdfParams &P, const BwdSmem &S, W
                 if ((m1 >> d) & 1) ws.dshift[r + 8][d] += dxc1[d] * inv;
             }
         }
-    }
-}
-
-__device__ __forceinline__ void normalize_bwd(const float x[3], float xn, const float y[3],
-                                              const float dy[3], float dx[3]) {
-    if (xn >= 1e-12f) {
-        const float yd = y[0] * dy[0] + y[1] * dy[1] + y[2] * dy[2];
-        for (int d = 0; d < 3; ++d) dx[d] = (dy[d] - y[d] * yd) / xn;
-    } else {
-        for (int d = 0; d < 3; ++d) dx[d] = dy[d] / 1e-12f;
     }
 }
 

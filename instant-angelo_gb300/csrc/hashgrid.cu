@@ -87,17 +87,31 @@ __global__ void __launch_bounds__(256) hashgrid_bwd_table_kernel(
     int64_t dout_col, float *__restrict__ dtable) {
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const int l = blockIdx.y;
-    if (i >= n || l >= active) return;
-    const float *g = dout + i * dout_stride + dout_col + (include_xyz ? 3 : 0) + l * 2;
-    const float g0 = g[0], g1 = g[1];
-    if (g0 == 0.0f && g1 == 0.0f) return;
-    const LevelPos p = level_pos(x[i * 3 + 0], x[i * 3 + 1], x[i * 3 + 2], lay.scales[l]);
+    if (l >= active) return;  // uniform over the block
+    const bool valid = i < n;
+    float g0 = 0.0f, g1 = 0.0f;
+    LevelPos p{};
+    if (valid) {
+        const float *g = dout + i * dout_stride + dout_col + (include_xyz ? 3 : 0) + l * 2;
+        g0 = g[0];
+        g1 = g[1];
+        p = level_pos(x[i * 3 + 0], x[i * 3 + 1], x[i * 3 + 2], lay.scales[l]);
+    }
+    const bool live = valid && (g0 != 0.0f || g1 != 0.0f);
     const uint64_t base = lay.offsets[l];
     float2 *dt = reinterpret_cast<float2 *>(dtable);
+    // coarse levels: consecutive points share corners, so aggregate in the
+    // warp first (the level, hence the branch, is uniform over the block)
+    const bool coarse = lay.resolutions[l] <= 300u;
 #pragma unroll
     for (int c = 0; c < 8; ++c) {
-        const float w = corner_weight(p, c);
-        atomicAdd(dt + base + corner_index(lay, l, p, c), make_float2(w * g0, w * g1));
+        const float w = live ? corner_weight(p, c) : 0.0f;
+        const uint64_t e = live ? base + corner_index(lay, l, p, c) : 0;
+        if (coarse) {
+            aggregated_add2<1>(dt, e, w * g0, w * g1, live);
+        } else if (live) {
+            atomicAdd(dt + e, make_float2(w * g0, w * g1));
+        }
     }
 }
 

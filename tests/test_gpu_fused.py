@@ -54,18 +54,19 @@ def test_fused_volume_sdf_matches_plain(dev, name):
         outs.append(([t.detach().cpu().numpy() for t in (sdf, grad, feat, lap)], grads))
     (sp, gp_, fp, lp), grp = outs[0]
     (sf, gf_, ff, lf), grf = outs[1]
-    np.testing.assert_allclose(sf, sp, rtol=1e-5, atol=2e-6)
-    np.testing.assert_allclose(ff, fp, rtol=1e-5, atol=2e-6)
+    # bf16x3 keeps ~2^-18 of each operand: ~1e-5 on an SDF value of order 1
+    np.testing.assert_allclose(sf, sp, rtol=1e-4, atol=3e-5)
+    np.testing.assert_allclose(ff, fp, rtol=1e-4, atol=3e-5)
     eps = gf._finite_difference_eps
     # FD gradient: SDF differences over 2 eps
-    np.testing.assert_allclose(gf_, gp_, rtol=1e-4, atol=4e-6 / eps)
-    assert np.mean(np.abs(lf - lp)) < 1e-4
+    np.testing.assert_allclose(gf_, gp_, rtol=1e-3, atol=6e-5 / eps)
+    assert np.mean(np.abs(lf - lp)) < 2e-3
     assert set(grf) == set(grp)
     for k in grp:
         ref, got = grp[k], grf[k]
         scale = max(np.abs(ref).max(), 1e-8)
         err = np.abs(got - ref).max() / scale
-        assert err < 5e-3, (k, err)
+        assert err < 1e-2, (k, err)
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -85,4 +86,110 @@ def test_fused_sdf_query_matches_forward_level(dev):
     with torch.no_grad():
         a = gp.forward_level(pts)
         b = gf.forward_level(pts)
-    np.testing.assert_allclose(b.cpu().numpy(), a.cpu().numpy(), rtol=1e-5, atol=2e-6)
+    np.testing.assert_allclose(b.cpu().numpy(), a.cpu().numpy(), rtol=1e-4, atol=3e-5)
+
+
+def _render_inputs(g, dev):
+    """Plain-path per-sample inputs of the radiance and compositing steps for
+    the golden rays (march with the golden's jitter)."""
+    m = build_model(g, dev, fused=False)
+    m.update_step(0, g["cfg"]["global_step"])
+    if g["cfg"]["grid_prune"]:
+        m.occupancy_grid.bits.copy_(torch.from_numpy(g["occ_bits"].view(np.int32)).to(dev))
+    jit = torch.from_numpy(g["jitter"]).to(dev)
+    m.stratified_fn = lambda t: jit
+    rays = torch.from_numpy(g["rays"]).to(dev)
+    o, d = rays[:, :3].contiguous(), rays[:, 3:].contiguous()
+    ri, t0, t1, off = m.march_rays(o, d)
+    idx = ri.long()
+    mid = (t0 + t1) * 0.5
+    pos = o[idx] + d[idx] * mid[:, None]
+    rd = torch.from_numpy(g["rand_dirs"]).to(dev)
+    m.geometry.curvature_dirs_fn = lambda t: rd
+    with torch.no_grad():
+        sdf, grad, feat, lap = m.geometry(pos, True, True, True)
+    return m, o, d, ri, t0, t1, off, sdf.detach(), grad.detach(), feat.detach()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_fused_radiance_matches_plain(dev, name):
+    from angelo_gb import fused
+    g = load(name)
+    m, o, d, ri, t0, t1, off, sdf, grad, feat = _render_inputs(g, dev)
+    tex = m.texture
+    outs = []
+    for use_fused in (False, True):
+        tex.zero_grad()
+        f_ = feat.clone().requires_grad_(True)
+        g_ = grad.clone().requires_grad_(True)
+        if use_fused:
+            rgb = fused.radiance_forward(tex, f_, g_, ri, d)
+        else:
+            normal = torch.nn.functional.normalize(g_, p=2, dim=-1)
+            rgb = tex(f_, d[ri.long()], normal)
+        w = torch.from_numpy(np.random.default_rng(1).normal(size=tuple(rgb.shape))
+                             .astype(np.float32)).to(dev)
+        (rgb * w).sum().backward()
+        outs.append((rgb.detach().cpu().numpy(), f_.grad.cpu().numpy(), g_.grad.cpu().numpy(),
+                     {k: p.grad.cpu().numpy().copy() for k, p in tex.named_parameters()
+                      if p.grad is not None}))
+    (rp, fp, gp, wp), (rf, ff, gf, wf) = outs
+    np.testing.assert_allclose(rf, rp, rtol=1e-4, atol=2e-5)
+    np.testing.assert_allclose(ff, fp, rtol=1e-3, atol=1e-5 * max(1.0, np.abs(fp).max()))
+    np.testing.assert_allclose(gf, gp, rtol=1e-3, atol=1e-4 * max(1.0, np.abs(gp).max()))
+    for k in wp:
+        err = np.abs(wf[k] - wp[k]).max() / max(np.abs(wp[k]).max(), 1e-8)
+        assert err < 5e-3, (k, err)
+
+
+@pytest.mark.parametrize("name", NAMES)
+@pytest.mark.parametrize("inv_s_var", [0.3, 0.8])   # inv_s 20 and 2981 (fp64-gated alpha)
+def test_fused_composite_matches_plain(dev, name, inv_s_var):
+    from angelo_gb import fused, ops
+    F = torch.nn.functional
+    g = load(name)
+    m, o, d, ri, t0, t1, off, sdf, grad, feat = _render_inputs(g, dev)
+    with torch.no_grad():
+        m.variance.variance.fill_(inv_s_var)
+        normal0 = F.normalize(grad, p=2, dim=-1)
+        rgb0 = m.texture(feat, d[ri.long()], normal0).detach()
+    bg = torch.tensor([0.3, 0.5, 0.7], device=dev)
+    m.background_color = bg
+    rng = np.random.default_rng(5)
+    R = off.numel() - 1
+    gw = {k: torch.from_numpy(rng.normal(size=s).astype(np.float32)).to(dev)
+          for k, s in (("op", (R, 1)), ("dep", (R, 1)), ("rgb", (R, 3)), ("n", (R, 3)),
+                       ("full", (R, 3)))}
+    res = []
+    for use_fused in (False, True):
+        m.zero_grad()
+        s_ = sdf.clone().requires_grad_(True)
+        g_ = grad.clone().requires_grad_(True)
+        c_ = rgb0.clone().requires_grad_(True)
+        if use_fused:
+            meta = dict(cos_ratio=m.cos_anneal_ratio, eps=1e-4, gate=fused.FP64_ALPHA_GATE)
+            op, dep, comp, cn, full, w = fused._FusedComposite.apply(
+                s_, g_, c_, m.variance.variance.view(1), t0, t1, off, d, bg, meta)
+        else:
+            nrm = F.normalize(g_, p=2, dim=-1)
+            alpha = m.get_alpha(s_, nrm, d[ri.long()], (t1 - t0)[:, None])[..., None]
+            w = ops.render_weight_from_alpha(alpha, off)[:, None]
+            op = ops.accumulate_along_rays(w, off)
+            dep = ops.accumulate_along_rays(w, off, ((t0 + t1) / 2)[:, None])
+            comp = ops.accumulate_along_rays(w, off, c_)
+            cn = F.normalize(ops.accumulate_along_rays(w, off, nrm), p=2, dim=-1)
+            cn = torch.where(op > 0.1, cn, torch.zeros_like(cn))
+            full = comp + bg[None] * (1.0 - op)
+        loss = ((op * gw["op"]).sum() + (dep * gw["dep"]).sum() + (comp * gw["rgb"]).sum() +
+                (cn * gw["n"]).sum() + (full * gw["full"]).sum())
+        loss.backward()
+        res.append(([t.detach().cpu().numpy() for t in (op, dep, comp, cn, full)],
+                    [s_.grad.cpu().numpy(), g_.grad.cpu().numpy(), c_.grad.cpu().numpy(),
+                     m.variance.variance.grad.cpu().numpy()]))
+    (outs_p, grads_p), (outs_f, grads_f) = res
+    for a, b in zip(outs_f, outs_p):
+        # log-space transmittance vs the sequential product: ~1e-6 relative
+        np.testing.assert_allclose(a, b, rtol=1e-4, atol=2e-5)
+    for name_, a, b in zip(("sdf", "grad", "rgb", "variance"), grads_f, grads_p):
+        scale = max(np.abs(b).max(), 1e-6)
+        assert np.abs(a - b).max() / scale < 2e-3, (name_, np.abs(a - b).max() / scale)
