@@ -244,6 +244,65 @@ int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32_t active_l
                            const float *g_grad, const float *g_feature, int64_t gfeat_stride,
                            const float *g_laplace, float *d_table, float *d_net, void *stream);
 
+/* ----------------------------------------------------- fused radiance network */
+
+/* Bytes of the prepared radiance-MLP buffer for a feature input of feat_dim
+ * columns (the MLP input is [feature, SH4 (16), normal (3)] = feat_dim + 19
+ * <= 96); -1 when unsupported. */
+int64_t angelo_radiance_net_bytes(int32_t feat_dim);
+/* Floats of the flat weight gradient: [dW1 (64 x 16*ceil(in/16)), dW2 (64x64),
+ * dW3 (16 x 64), db1 (64), db2 (64), db3 (16)]. */
+int64_t angelo_radiance_grad_size(int32_t feat_dim);
+/* Effective fp32 weights of VanillaMLP(in, 3, 2 hidden ReLU layers of 64)
+ * (models/texture.py:19,47) -> prepared buffer. */
+int angelo_radiance_prep(int32_t feat_dim, const float *W1, const float *b1, const float *W2,
+                         const float *b2, const float *W3, const float *b3, void *net,
+                         void *stream);
+/* VolumeRadiance / VolumeDualColor forward (models/texture.py:23-30,50-58):
+ * rgb = sigmoid(MLP([feature, SH4((d+1)/2), normalize(grad)])) (+ sigmoid of
+ * feature[1:4] when dual), d = rays_d[ray_idx].  precision 0: bf16x3, 1:
+ * single-pass bf16. */
+int angelo_radiance_fwd(int32_t feat_dim, const void *net, const float *feature,
+                        int64_t feat_stride, const float *grad, const int32_t *ray_idx,
+                        const float *rays_d, int64_t n, int32_t dual, float *rgb, void *stream);
+/* Backward: d_feature (written, n x feat_stride), d_grad (written, n x 3),
+ * d_net (accumulated). */
+int angelo_radiance_bwd(int32_t feat_dim, const void *net, const float *feature,
+                        int64_t feat_stride, const float *grad, const int32_t *ray_idx,
+                        const float *rays_d, int64_t n, int32_t dual, const float *g_rgb,
+                        float *d_feature, float *d_grad, float *d_net, void *stream);
+
+/* ------------------------------------------------------------ fused compositing */
+
+/* NeuSModel.get_alpha + render_weight_from_alpha + accumulate_along_rays + the
+ * background blend (models/neus.py:117-139,234-248,273-277), one warp per ray:
+ * alpha from sdf / normalize(grad) / ray direction / interval with inv_s =
+ * clip(exp(10*variance)) read on the device (fp64 when inv_s > fp64_gate),
+ * log-space transmittance by a warp prefix sum, weights zero once
+ * T < early_stop_eps; per-ray opacity, depth, comp_rgb, comp_normal
+ * (normalised, zero where opacity <= 0.1), comp_rgb_full = comp_rgb +
+ * bg*(1-opacity).  acc_normal (unnormalised sum), weights and trans (per
+ * sample) are kept for the backward; alpha may be NULL. */
+int angelo_composite_fwd(const int64_t *offsets, int64_t n_rays, const float *sdf,
+                         const float *grad, const float *t_starts, const float *t_ends,
+                         const float *rays_d, const float *rgb, const float *variance,
+                         float cos_anneal_ratio, const float *bg, float early_stop_eps,
+                         float fp64_gate, float *opacity, float *depth, float *comp_rgb,
+                         float *comp_normal, float *comp_rgb_full, float *acc_normal,
+                         float *weights, float *trans, float *alpha, void *stream);
+/* Backward by a reverse affine warp scan R_{j-1} = (1-a_j) R_j + g_j a_j,
+ * dL/dalpha_j = T_j (g_j - R_j): writes d_sdf, d_grad (n x 3), d_rgb (n x 3)
+ * and ACCUMULATES d_variance (1 float).  Any output gradient may be NULL. */
+int angelo_composite_bwd(const int64_t *offsets, int64_t n_rays, const float *sdf,
+                         const float *grad, const float *t_starts, const float *t_ends,
+                         const float *rays_d, const float *rgb, const float *variance,
+                         float cos_anneal_ratio, const float *bg, float early_stop_eps,
+                         float fp64_gate, const float *opacity, const float *acc_normal,
+                         const float *weights, const float *trans, const float *g_opacity,
+                         const float *g_depth, const float *g_comp_rgb,
+                         const float *g_comp_normal, const float *g_comp_rgb_full, float *d_sdf,
+                         float *d_grad, float *d_rgb, float *d_variance, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -92,6 +92,19 @@ SIGNATURES = {
     "angelo_sdf_stencil_bwd": (c_i32, [_P(HashGridLayout), c_i32, c_vp, c_i32, _P(SdfNetLayout),
                                        c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_i32, c_i32, c_vp,
                                        c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_radiance_net_bytes": (c_i64, [c_i32]),
+    "angelo_radiance_grad_size": (c_i64, [c_i32]),
+    "angelo_radiance_prep": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_radiance_fwd": (c_i32, [c_i32, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i64, c_i32, c_vp,
+                                    c_vp]),
+    "angelo_radiance_bwd": (c_i32, [c_i32, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i64, c_i32, c_vp,
+                                    c_vp, c_vp, c_vp, c_vp]),
+    "angelo_composite_fwd": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_f32,
+                                     c_vp, c_f32, c_f32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                     c_vp, c_vp, c_vp]),
+    "angelo_composite_bwd": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_f32,
+                                     c_vp, c_f32, c_f32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                     c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
 }
 
 _lock = threading.Lock()
@@ -150,6 +163,10 @@ def call(name, *args, launches=1, units=None, stream=None):
     ``launches`` is the number of kernels the call puts on the stream and
     ``units`` its work description, both only recorded while profiling."""
     L = load()
+    if name not in SIGNATURES:
+        # a function without declared argument types would receive Python
+        # ints as 32-bit C ints: refuse instead of launching with garbage
+        raise AngeloError(name, ANGELO_E_INVALID, "entry point has no registered signature")
     prof = PROFILER.active
     if prof:
         import torch

@@ -272,7 +272,7 @@ def radiance_forward(texture, feature, grad, ray_idx, rays_d):
 
 FP64_ALPHA_GATE = 2048.0
 # the fused radiance / compositing kernels are used by neus_forward when set
-FUSED_RENDER = False
+FUSED_RENDER = True
 
 
 class _FusedComposite(torch.autograd.Function):

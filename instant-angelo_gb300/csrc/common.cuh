@@ -61,6 +61,12 @@ __device__ __forceinline__ uint32_t grid_index(uint32_t hashmap_size, uint32_t r
     // The dense loop above stops adding once stride exceeds the level size,
     // exactly where the reference's loop condition stops.
     if (hashmap_size < stride) index = (g0 * 1u) ^ (g1 * 2654435761u) ^ (g2 * 805459861u);
+    // index % hashmap_size without the integer division: hashed levels have a
+    // power-of-two size; dense indices of points inside [0,1] stay below twice
+    // the level size (level sizes are at most 2^30)
+    if ((hashmap_size & (hashmap_size - 1u)) == 0u) return index & (hashmap_size - 1u);
+    if (index < hashmap_size) return index;
+    if (index < 2u * hashmap_size) return index - hashmap_size;
     return index % hashmap_size;
 }
 

@@ -46,8 +46,12 @@ def test_fused_volume_sdf_matches_plain(dev, name):
         geo.zero_grad()
         sdf, grad, feat, lap = geo(pts, with_grad=True, with_feature=True, with_laplace=True)
         w = torch.from_numpy(np.random.default_rng(9).normal(size=(n, 8)).astype(np.float32)).to(dev)
+        # with radius < 1 the reference's curvature stencil (shifted in contracted
+        # coordinates, clamped to +-r) collapses for part of the box and its
+        # gradient is dy / 1e-12 there in both paths: leave it out of the loss
+        lw = 1e-2 if r >= 1.0 else 0.0
         loss = ((sdf * w[:, 0]).sum() + (grad * w[:, 1:4]).sum() +
-                (feat[:, :5] * w[:, 3:8]).sum() + (lap[:, 0] * w[:, 0]).sum() * 1e-2)
+                (feat[:, :5] * w[:, 3:8]).sum() + (lap[:, 0] * w[:, 0]).sum() * lw)
         loss.backward()
         grads = {k: p.grad.detach().cpu().numpy().copy() for k, p in geo.named_parameters()
                  if p.grad is not None}

@@ -74,3 +74,25 @@ def test_dropins_build_with_reference_keys(lib):
     assert ref <= names, ref - names
     for k in ref:
         assert tuple(m.state_dict()[k].shape) == g["param/" + k].shape, k
+
+
+def test_ctypes_signatures_match_header_argument_counts(lib):
+    """Every declared entry point is bound with as many ctypes arguments as the
+    header declares (a mismatch would pass garbage through the C ABI)."""
+    from angelo_gb import _lib
+    txt = open(os.path.join(ROOT, "include", "angelo_gb.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    n_checked = 0
+    for m in re.finditer(r"\b(angelo_[a-z0-9_]+)\s*\(([^;{]*?)\)\s*;", txt):
+        name, args = m.group(1), m.group(2).strip()
+        n = 0 if args in ("", "void") else len(args.split(","))
+        assert name in _lib.SIGNATURES, name
+        assert len(_lib.SIGNATURES[name][1]) == n, (name, n, len(_lib.SIGNATURES[name][1]))
+        n_checked += 1
+    assert n_checked == len(_lib.SIGNATURES)
+
+
+def test_unbound_entry_point_is_refused(lib):
+    from angelo_gb import _lib
+    with pytest.raises(_lib.AngeloError):
+        _lib.call("angelo_not_declared", 1, 2)
