@@ -76,7 +76,7 @@ def run_golden(g, dev, fused=False, check_occupancy=True, **extra):
 
 
 def check_against_golden(g, out, grads, grads_curv, out_tol=(2e-4, 2e-5), grad_tol=2e-3,
-                         fd_tol=2e-3):
+                         fd_tol=2e-3, curv_tol=2e-2):
     np.testing.assert_array_equal(out["ray_indices"].cpu().numpy(), g["out/ray_indices"])
     for k in ("comp_rgb", "opacity", "depth", "comp_rgb_full", "sdf_samples", "weights",
               "points", "intervals"):
@@ -104,7 +104,7 @@ def check_against_golden(g, out, grads, grads_curv, out_tol=(2e-4, 2e-5), grad_t
                 continue
             scale = max(np.abs(ref).max(), 1e-4 * gmax)
             err = np.abs(v.reshape(ref.shape) - ref).max() / scale
-            assert err < 2e-2, ("curv", k, err)
+            assert err < curv_tol, ("curv", k, err)
 
 
 @pytest.mark.parametrize("name", NAMES)
