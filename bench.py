@@ -54,6 +54,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--forms", default="auto", help="comma list of plain,fused (auto: all built)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sdf-case", type=int, default=0, metavar="N",
+                    help="profiling case: 3 fused VolumeSDF training passes (16 levels x 2^22, "
+                         "FD + curvature) on N points of the full model, then exit")
     return ap.parse_args()
 
 
@@ -229,21 +232,18 @@ def algorithmic_bytes(name, u):
             b += u["active"] * 8 * 2 * u["tbytes"] + 12
         return u["n"] * b
     if name == "angelo_sdf_stencil_fwd":
-        # per sample: position + curvature direction, the gathers of every
-        # evaluation (8 corners x 2 features per active level), outputs
-        # (sdf, grad, feature [od + 3], laplace) and, in training, the stash
-        # (13 x 36 encodings + 13 sdf values)
-        per = (24 + u["evals"] * u["active"] * 16 * u["tbytes"] + 4 + 12 + (u["od"] + 3) * 4 + 4
-               + (13 * 36 * 4 + 13 * 4 if u["train"] else 0))
-        return u["n"] * per
+        # per sample: position + curvature direction, outputs (sdf, grad,
+        # feature [od + 3], laplace), and per evaluation one encoded point
+        # (x 12 B, 8 corner gathers and the F features of every active level);
+        # the stencil taps share corner gathers, so the kernel moves less
+        per_eval = 12 + u["active"] * 2 * u["tbytes"] * (8 + 1)
+        return u["n"] * (24 + 4 + 12 + (u["od"] + 3) * 4 + 4 + u["evals"] * per_eval)
     if name == "angelo_sdf_stencil_bwd":
-        # per sample: position, direction, stash, incoming gradients, table
-        # atomics (read + write) of every evaluation, and the re-gathered
-        # corners of the 6 shifted evaluations (positional derivative)
-        shifted = 6 if u["evals"] == 13 else 0
-        per = (24 + 13 * 36 * 4 + 13 * 4 + 4 + 12 + u["od"] * 4 + 4
-               + u["evals"] * u["active"] * 16 * 4 * 2 + shifted * u["active"] * 16 * u["tbytes"])
-        return u["n"] * per
+        # per sample: position, direction, incoming gradients, and per
+        # evaluation the fp32 table-gradient atomics of one encoded point
+        # (8 corners x F features per active level, read + write)
+        per_eval = u["active"] * 8 * 2 * 4 * 2
+        return u["n"] * (24 + 4 + 12 + u["od"] * 4 + 4 + u["evals"] * per_eval)
     return None
 
 
@@ -479,8 +479,33 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}), flush=True)
 
 
+def run_sdf_case(n):
+    """A small standalone case of the fused VolumeSDF forward + backward of the
+    full model (for kernel captures): N points in the inner box, table and
+    first-layer weights randomised so that every gradient path is non-zero."""
+    from angelo_gb import models, workloads
+    torch.manual_seed(0)
+    dev = torch.device("cuda:0")
+    m = models.make("neus", workloads.model_config("full", fused=True)).to(dev).train()
+    m.update_step(0, GLOBAL_STEP)
+    g = m.geometry
+    with torch.no_grad():
+        g.hashgrid.encoding.params.uniform_(-0.05, 0.05)
+        g.network.layers[0].weight_v[:, 3:].normal_(0, 0.05)
+    pts = (torch.rand(n, 3, device=dev) - 0.5) * 0.8
+    for _ in range(3):
+        g.zero_grad()
+        sdf, grad, feat, lap = g(pts, True, True, True)
+        (sdf.sum() + grad.sum() + feat.sum() + lap.sum()).backward()
+    torch.cuda.synchronize()
+    print(json.dumps({"sdf_case": n, "ok": True}), flush=True)
+
+
 def main():
     args = parse()
+    if args.sdf_case:
+        run_sdf_case(args.sdf_case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

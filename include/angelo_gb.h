@@ -215,6 +215,14 @@ int angelo_sdf_prep(const angelo_sdf_net_layout *lay, int32_t n_levels, int32_t 
  *  dW3 (16*k_tiles3b x 64), db1 (64), db2 (64), db3 (16*k_tiles3b)]. */
 int64_t angelo_sdf_grad_size(const angelo_sdf_net_layout *lay);
 
+/* Floats of device workspace of the fused VolumeSDF for n samples: the
+ * forward's (backward = 0: the hash encodings of every evaluation, level-major
+ * float2, and 16 floats of stencil state per sample) or the backward's
+ * (backward = 1: dL/d(encodings), same layout, and 8 floats per sample).
+ * -1 on invalid arguments.  Both must be 8-byte aligned. */
+int64_t angelo_sdf_workspace_floats(const angelo_hashgrid_layout_t *lay, int64_t n,
+                                    int32_t with_grad, int32_t with_laplace, int32_t backward);
+
 /* Fused VolumeSDF.forward with grad_type='finite_difference'
  * (models/geometry.py:195-287): per sample the point, the 6-tap FD stencil
  * and the 6-tap curvature stencil (13 hash-grid + MLP evaluations), with the
@@ -222,25 +230,29 @@ int64_t angelo_sdf_grad_size(const angelo_sdf_net_layout *lay);
  * contracted coordinates then clamped as world coordinates).  pos: (n,3)
  * world points; rand_dirs: (n,3), the randn of models/geometry.py:238.
  * Outputs sdf (n), grad (n,3), feature (n, feat_stride >= out_dim+3:
- * [MLP output, x*2-1]), laplace (n).  stash_x (n,13,36) and stash_s (n,13)
- * (both or neither) keep what the backward needs. */
+ * [MLP output, x*2-1]), laplace (n).  workspace: the forward workspace
+ * (angelo_sdf_workspace_floats(.., 0) floats); a training forward keeps it,
+ * unmodified, for the backward.  Instantiated network shapes: 8 levels /
+ * 1 hidden layer / 9..16 outputs and 16 levels / 2 hidden layers / 65..72
+ * outputs (angelo_sdf_net_layout_query refuses others). */
 int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32_t active_levels,
                            const void *table, int32_t table_dtype, const angelo_sdf_net_layout *nl,
                            const void *net, const float *pos, const float *rand_dirs, int64_t n,
                            float radius, float eps, int32_t with_grad, int32_t with_laplace,
                            int32_t with_feature, float *sdf, float *grad, float *feature,
-                           int64_t feat_stride, float *laplace, float *stash_x, float *stash_s,
-                           void *stream);
+                           int64_t feat_stride, float *laplace, float *workspace, void *stream);
 
 /* Backward of the fused VolumeSDF: from dL/dsdf, dL/dgrad, dL/dfeature
  * (any may be NULL), dL/dlaplace, ACCUMULATES dL/dtable (float32, atomic)
  * and dL/dnet (angelo_sdf_grad_size floats, atomic).  The curvature path
- * includes the hash grid's positional derivative at the shifted stencil. */
+ * includes the hash grid's positional derivative at the shifted stencil.
+ * workspace: the forward's, read only (the backward may run more than once);
+ * bwd_workspace: angelo_sdf_workspace_floats(.., 1) floats of scratch. */
 int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32_t active_levels,
                            const void *table, int32_t table_dtype, const angelo_sdf_net_layout *nl,
                            const void *net, const float *pos, const float *rand_dirs, int64_t n,
                            float radius, float eps, int32_t with_grad, int32_t with_laplace,
-                           const float *stash_x, const float *stash_s, const float *g_sdf,
+                           const float *workspace, float *bwd_workspace, const float *g_sdf,
                            const float *g_grad, const float *g_feature, int64_t gfeat_stride,
                            const float *g_laplace, float *d_table, float *d_net, void *stream);
 

@@ -86,9 +86,10 @@ SIGNATURES = {
     "angelo_sdf_prep": (c_i32, [_P(SdfNetLayout), c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp,
                                 c_vp, c_vp, c_vp]),
     "angelo_sdf_grad_size": (c_i64, [_P(SdfNetLayout)]),
+    "angelo_sdf_workspace_floats": (c_i64, [_P(HashGridLayout), c_i64, c_i32, c_i32, c_i32]),
     "angelo_sdf_stencil_fwd": (c_i32, [_P(HashGridLayout), c_i32, c_vp, c_i32, _P(SdfNetLayout),
                                        c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_i32, c_i32, c_i32,
-                                       c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+                                       c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "angelo_sdf_stencil_bwd": (c_i32, [_P(HashGridLayout), c_i32, c_vp, c_i32, _P(SdfNetLayout),
                                        c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_i32, c_i32, c_vp,
                                        c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),

@@ -1,10 +1,12 @@
 """Fused forms of the hot path (libangelo_gb.so fused kernels).
 
-* VolumeSDF: one kernel evaluates, per sample, the point, its 6-tap
-  finite-difference stencil and the 6-tap curvature stencil (13 hash-grid +
-  MLP evaluations, MLP on tensor cores in bf16x3) and writes sdf, grad,
-  feature and laplace; the backward kernel recomputes the MLP activations from
-  the stashed encodings and returns dL/dtable and dL/dW of every layer.
+* VolumeSDF: per sample the point, its 6-tap finite-difference stencil and
+  the 6-tap curvature stencil (13 hash-grid + MLP evaluations): a
+  shared-gather stencil encode per (sample, level), the MLP on tensor cores
+  in bf16x3 with the stencil arithmetic fused, and in the backward the MLP
+  recomputed from the kept encodings, dL/dW as a per-CTA staged GEMM and a
+  shared-corner scatter of dL/dtable (the curvature taps also carry the hash
+  grid's positional derivative).
 """
 from __future__ import annotations
 
@@ -74,6 +76,16 @@ class SdfNet:
         return out
 
 
+def workspace_floats(spec, n, with_grad, with_laplace, backward):
+    """Floats of the fused VolumeSDF forward (backward=False) or backward
+    workspace for n samples."""
+    k = _lib.raw("angelo_sdf_workspace_floats")(ctypes.byref(spec.layout), int(n), int(with_grad),
+                                                 int(with_laplace), int(backward))
+    if k < 0:
+        raise ValueError("angelo_sdf_workspace_floats: invalid arguments")
+    return k
+
+
 class _FusedSdf(torch.autograd.Function):
     @staticmethod
     def forward(ctx, pos, rand_dirs, table, meta, *weights):
@@ -91,27 +103,28 @@ class _FusedSdf(torch.autograd.Function):
         feature = torch.empty(S, od + 3, device=dev) if with_feature else None
         lap = torch.empty(S, 1, device=dev) if with_laplace else None
         training = any(ctx.needs_input_grad[2:])
-        stash_x = torch.empty(S, 13, 36, device=dev) if training else None
-        stash_s = torch.empty(S, 13, device=dev) if training else None
+        work = torch.empty(workspace_floats(spec, S, with_grad, with_laplace, False), device=dev)
         rd = rand_dirs.contiguous() if rand_dirs is not None else None
+        n_ev = 13 if with_laplace else (7 if with_grad else 1)
         call("angelo_sdf_stencil_fwd", ctypes.byref(spec.layout), int(active), _p(table),
              _table_dtype(table), ctypes.byref(net.layout), _p(net.buf), _p(pos), _p(rd), S,
              float(geom.radius), float(geom._finite_difference_eps or 1.0), int(with_grad),
              int(with_laplace), int(with_feature), _p(sdf), _p(grad), _p(feature),
-             od + 3, _p(lap), _p(stash_x), _p(stash_s), _s(dev),
-             units=dict(n=S, od=net.out_dim, evals=13 if with_laplace else (7 if with_grad else 1),
-                        active=int(active), tbytes=table.element_size(), train=training))
+             od + 3, _p(lap), _p(work), _s(dev),
+             launches=4 if with_laplace else 2,
+             units=dict(n=S, od=net.out_dim, evals=n_ev, active=int(active),
+                        levels=spec.layout.n_levels, tbytes=table.element_size(), train=training))
         ctx.meta = meta
         ctx.in_dim = weights[0].shape[1]
         ctx.n_w = len(weights)
         if training:
-            ctx.save_for_backward(pos, rd, table, stash_x, stash_s)
+            ctx.save_for_backward(pos, rd, table, work)
         outs = [sdf, grad, feature, lap]
         return tuple(t if t is not None else torch.empty(0, device=dev) for t in outs)
 
     @staticmethod
     def backward(ctx, g_sdf, g_grad, g_feat, g_lap):
-        pos, rd, table, stash_x, stash_s = ctx.saved_tensors
+        pos, rd, table, work = ctx.saved_tensors
         geom, net, flags = ctx.meta["geom"], ctx.meta["net"], ctx.meta["flags"]
         with_grad, with_laplace, with_feature = flags
         spec = geom.hashgrid.encoding.spec
@@ -128,13 +141,16 @@ class _FusedSdf(torch.autograd.Function):
         gg = c(g_grad, with_grad and g_grad is not None and g_grad.numel() == 3 * S)
         gf = c(g_feat, with_feature and g_feat is not None and g_feat.numel() > 0)
         gl = c(g_lap, with_laplace and g_lap is not None and g_lap.numel() == S)
+        bwork = torch.empty(workspace_floats(spec, S, with_grad, with_laplace, True), device=dev)
+        n_ev = 13 if with_laplace else (7 if with_grad else 1)
         call("angelo_sdf_stencil_bwd", ctypes.byref(spec.layout), int(active), _p(table),
              _table_dtype(table), ctypes.byref(net.layout), _p(net.buf), _p(pos), _p(rd), S,
              float(geom.radius), float(geom._finite_difference_eps or 1.0), int(with_grad),
-             int(with_laplace), _p(stash_x), _p(stash_s), _p(gs), _p(gg), _p(gf),
+             int(with_laplace), _p(work), _p(bwork), _p(gs), _p(gg), _p(gf),
              gf.stride(0) if gf is not None else 0, _p(gl), _p(d_table), _p(d_net), _s(dev),
-             units=dict(n=S, od=net.out_dim, evals=13 if with_laplace else (7 if with_grad else 1),
-                        active=int(active), tbytes=table.element_size(), train=True))
+             launches=4 if with_laplace else 2,
+             units=dict(n=S, od=net.out_dim, evals=n_ev, active=int(active),
+                        levels=spec.layout.n_levels, tbytes=table.element_size(), train=True))
         grads = net.unpack_grads(d_net, ctx.in_dim)
         flat = []
         for dW, db in grads:

@@ -1,22 +1,37 @@
 // Fused VolumeSDF (models/geometry.py:195-287 with grad_type finite_difference):
-// per sample, 13 evaluations of hash grid + geometry MLP (the point, the 6-tap
-// finite-difference stencil, the 6-tap curvature stencil around the
-// tangent-shifted point), all in one kernel, with the MLP on tensor cores
-// (bf16x3 split, fp32 accumulation) and the stencil arithmetic in fp32.
+// per sample 13 evaluations of hash grid + geometry MLP -- the point, the
+// 6-tap finite-difference stencil around it and the 6-tap curvature stencil
+// around the tangent-shifted point -- in four kinds of kernels:
 //
-// Work split: a warp owns 16 samples at a time; evaluation e of those 16
-// samples is one m16 tile.  Lane (r = lane/4, q = lane%4) encodes rows r and
-// r+8 at hash levels q + 4j, which are exactly the A-fragment entries it
-// feeds to mma.sync (the encoding input is reordered [hash levels..., xyz,
-// zero pad]; the first-layer weights are permuted to match on the host).
+//   stencil_encode   thread per (sample, level).  The taps of one level share
+//                    the 8 corner gathers of the stencil centre: a tap moved by
+//                    eps along axis d keeps the corners of the centre's cell,
+//                    or, when it crosses a cell face, the 4 corners of the face
+//                    it shares and 4 new ones.  Each tap's features are
+//                    computed exactly as encoding that tap alone (same cell,
+//                    fraction, weights and summation order).  Output: the
+//                    encodings X[e][l][s] (float2, level-major).
+//   sdf_mlp_fwd      warp per 16 samples: the geometry MLP of every evaluation
+//                    on tensor cores (bf16x3 split, fp32 accumulation) from X,
+//                    then the stencil arithmetic (sdf, FD gradient, tangent
+//                    shift, curvature) in fp32.
+//   sdf_mlp_bwd      warp per 16 samples: recomputes the activations from X,
+//                    back-propagates the stencil arithmetic and the MLP and
+//                    writes dL/dX.  dL/dW is a GEMM whose reduction dimension
+//                    is the sample: each CTA stages 128 rows of (dZ, layer
+//                    input) in shared memory, every warp owns a slice of the
+//                    dW tiles and keeps it in registers for the whole kernel;
+//                    one atomic flush per CTA at the end.
+//   stencil_scatter  thread per (sample, level): dL/dtable of the taps with the
+//                    same corner sharing (one atomic per distinct corner, warp-
+//                    aggregated at coarse levels), and for the curvature taps
+//                    the hash grid's positional derivative into dL/d(shifted).
 //
-// Training: the forward kernel stashes the 13 encodings (fp32) and the 13 SDF
-// values of each sample; the backward kernel recomputes the MLP activations
-// from them, back-propagates through the stencil arithmetic (curvature ->
-// shifted stencil -> tangent -> normal -> FD gradient -> FD stencil -> point),
-// scatters dL/dtable with vector atomics, and accumulates dL/dW in shared
-// memory (one global flush per CTA).
+// Order: forward   encode(FD) -> mlp_fwd(FD) -> encode(curv) -> mlp_fwd(curv)
+//        backward  mlp_bwd(curv) -> scatter(curv) -> mlp_bwd(FD) -> scatter(FD)
 #include <math.h>
+
+#include <algorithm>
 
 #include "common.cuh"
 #include "mlp.cuh"
@@ -32,6 +47,14 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
+constexpr int kEncThreads = 128;
+constexpr int kState = 16;      // per sample: sdf of the 13 evaluations, shifted point (3)
+constexpr int kBState = 8;      // per sample, backward: dL/dshifted (3), dL/dnormal from curvature (3)
+constexpr int kStageRows = kWarps * 16;
+constexpr int kStageLd = 72;    // bf16 row stride of staged 64-wide operands (conflict-free ldmatrix)
+constexpr uint32_t kAggregateRes = 300;  // levels up to this resolution aggregate their atomics
+
+enum Group { kPoint = 0, kFD = 1, kCurv = 2 };
 
 struct NetSmem {
     const uint2 *w1f, *w2f, *w3f;  // hi at [0, n), lo at [n, 2n)
@@ -141,48 +164,43 @@ struct SdfParams {
     // outputs
     float *sdf, *grad, *feature, *laplace;
     int64_t feat_stride;
-    // stash (training)
-    float *stash_x;   // (S, 13, 36)
-    float *stash_s;   // (S, 13)
+    // forward workspace
+    float2 *X;        // encodings, X[(e * n_levels + l) * S + s]
+    float *state;     // (S, kState): sdf of the 13 evaluations, shifted point
     // backward inputs
     const float *g_sdf, *g_grad, *g_feature, *g_laplace;
     int64_t gfeat_stride;
-    // backward outputs
+    // backward workspace and outputs
+    float2 *dX;       // dL/dX, layout of X
+    float *bstate;    // (S, kBState)
     float *d_table;   // float32 table gradient (atomic)
-    float *d_net;     // (64*K1 + 64*64 + N3*64 + 64 + 64 + N3) fp32, kernel order (atomic)
+    float *d_net;     // flat weight gradient, kernel order (atomic)
 };
 
-constexpr int kStashCols = 36;
+__device__ __forceinline__ int64_t xidx(const SdfParams &P, int e, int l, int64_t s) {
+    return ((int64_t)e * P.lay.n_levels + l) * P.S + s;
+}
 
-// per-warp scratch: 16 samples
-struct WarpScratch {
-    float pos[16][3];
-    float rd[16][3];
-    float s13[16][13];
-    float shifted[16][3];
-    float ds[16][13];       // backward: dL/d(sdf) of each of the 13 evaluations
-    float dshift[16][3];    // backward: dL/d(shifted point)
-    float n[16][3];
-};
+__device__ __forceinline__ float x2m1(float x) { return __fsub_rn(__fmul_rn(x, 2.f), 1.f); }
 
-// Position of evaluation e for a sample: e = 0 the point, 1..6 the FD
-// stencil (+x,-x,+y,-y,+z,-z) clamped to the box, 7..12 the same stencil
-// around the shifted point.  Returns contracted coordinates; mask bit d is
-// set when the clamp passed coordinate d through (its gradient is 1).
-__device__ __forceinline__ void eval_point(const SdfParams &P, const WarpScratch &ws, int row, int e,
-                                           float xc[3], int *mask) {
-    const float r = P.radius;
+// Contracted coordinates of evaluation e of a sample around `base` (the point
+// for e <= 6, the shifted point for e >= 7): e = 0 the point itself, else the
+// stencil tap (e - 1) % 6 = +x,-x,+y,-y,+z,-z moved by eps and clamped to the
+// box (models/geometry.py:224-246).  Mask bit d is set when coordinate d
+// passed the clamp (its derivative is 1).
+__device__ __forceinline__ void tap_point(float r, float eps, const float base[3], int e, float xc[3],
+                                          int *mask) {
     const float two_r = __fsub_rn(r, -r);
     int m = 0;
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
         float v;
         if (e == 0) {
-            v = ws.pos[row][d];
+            v = base[d];
         } else {
             const int k = (e - 1) % 6;
-            const float base = e <= 6 ? ws.pos[row][d] : ws.shifted[row][d];
-            const float off = (k >> 1) == d ? ((k & 1) ? -P.eps : P.eps) : 0.0f;
-            v = __fadd_rn(base, off);
+            const float off = (k >> 1) == d ? ((k & 1) ? -eps : eps) : 0.0f;
+            v = __fadd_rn(base[d], off);
             const bool inside = v >= -r && v <= r;
             v = fminf(fmaxf(v, -r), r);
             m |= inside << d;
@@ -192,9 +210,102 @@ __device__ __forceinline__ void eval_point(const SdfParams &P, const WarpScratch
     *mask = e == 0 ? 7 : m;
 }
 
-// ------------------------------------------------------------ forward eval
-// Encodes rows r, r+8 of evaluation e into A fragments (hi/lo) and runs the
-// MLP; returns the output tile(s) in C layout.  KH = hash k-tiles (L/8).
+// The stencil centre whose corners the taps share: the base clamped to the
+// box, so that the coordinates a tap does not move are bit-identical to it.
+__device__ __forceinline__ void clamped_centre(float r, const float base[3], float xc[3]) {
+    const float two_r = __fsub_rn(r, -r);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) xc[d] = __fdiv_rn(__fsub_rn(fminf(fmaxf(base[d], -r), r), -r), two_r);
+}
+
+// Cell offset of a tap along its axis d relative to the centre: the tap shares
+// the centre's corners when its other two cell coordinates equal the centre's
+// and delta is -1, 0 or +1.
+__device__ __forceinline__ bool tap_aligned(const LevelPos &p, const LevelPos &pc, int d, int *delta) {
+    const int dl = (int)(p.g[d] - pc.g[d]);
+    *delta = dl;
+    return p.g[(d + 1) % 3] == pc.g[(d + 1) % 3] && p.g[(d + 2) % 3] == pc.g[(d + 2) % 3] && dl >= -1 &&
+           dl <= 1;
+}
+
+// Does corner cc of a tap (axis d, offset delta) coincide with a centre corner?
+__device__ __forceinline__ bool corner_shared(bool aligned, int delta, int cc, int d) {
+    const int b = (cc >> d) & 1;
+    return aligned && (delta == 0 || ((delta == 1) == (b == 0)));
+}
+
+// Value of the centre corner that corner cc of the tap coincides with (given
+// corner_shared): delta 0 the same corner; +1 the tap's lower face is the
+// centre's upper face; -1 the tap's upper face is the centre's lower face.
+// cc and d are compile-time after unrolling, so this is a register select.
+__device__ __forceinline__ float2 centre_value(const float2 (&vc)[8], int delta, int cc, int d) {
+    const float2 other = ((cc >> d) & 1) == 0 ? vc[cc | (1 << d)] : vc[cc & ~(1 << d)];
+    return delta == 0 ? vc[cc] : other;
+}
+
+// ---------------------------------------------------------------- encode
+
+template <int GROUP>
+__global__ void __launch_bounds__(kEncThreads) stencil_encode_kernel(const __grid_constant__ SdfParams P) {
+    const int l = blockIdx.y;
+    const int64_t s = (int64_t)blockIdx.x * kEncThreads + threadIdx.x;
+    if (s >= P.S) return;
+    const float r = P.radius, eps = P.eps;
+    const float *src = GROUP == kCurv ? P.state + s * kState + 13 : P.pos + s * 3;
+    const float base[3] = {src[0], src[1], src[2]};
+    const float sc = P.lay.scales[l];
+    const uint64_t off = P.lay.offsets[l];
+    float xcc[3];
+    clamped_centre(r, base, xcc);
+    const LevelPos pc = level_pos(xcc[0], xcc[1], xcc[2], sc);
+    float2 vc[8];
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) vc[cc] = load_entry(P.table, P.tdtype, off + corner_index(P.lay, l, pc, cc));
+    if (GROUP != kCurv) {
+        float xc[3];
+        int m;
+        tap_point(r, eps, base, 0, xc, &m);
+        const LevelPos p = level_pos(xc[0], xc[1], xc[2], sc);
+        const bool same = p.g[0] == pc.g[0] && p.g[1] == pc.g[1] && p.g[2] == pc.g[2];
+        float2 f = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+            const float w = corner_weight(p, cc);
+            const float2 v = same ? vc[cc] : load_entry(P.table, P.tdtype, off + corner_index(P.lay, l, p, cc));
+            f.x = __fmaf_rn(w, v.x, f.x);
+            f.y = __fmaf_rn(w, v.y, f.y);
+        }
+        P.X[xidx(P, 0, l, s)] = f;
+    }
+    if (GROUP != kPoint) {
+        constexpr int e0 = GROUP == kFD ? 1 : 7;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const int d = k >> 1;
+            float xc[3];
+            int m, delta;
+            tap_point(r, eps, base, e0 + k, xc, &m);
+            const LevelPos p = level_pos(xc[0], xc[1], xc[2], sc);
+            const bool aligned = tap_aligned(p, pc, d, &delta);
+            float2 f = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc) {
+                const float w = corner_weight(p, cc);
+                const float2 v = corner_shared(aligned, delta, cc, d)
+                                     ? centre_value(vc, delta, cc, d)
+                                     : load_entry(P.table, P.tdtype, off + corner_index(P.lay, l, p, cc));
+                f.x = __fmaf_rn(w, v.x, f.x);
+                f.y = __fmaf_rn(w, v.y, f.y);
+            }
+            P.X[xidx(P, e0 + k, l, s)] = f;
+        }
+    }
+}
+
+// ------------------------------------------------------------ MLP operands
+// A fragments of the first layer for rows g, g+8 of a 16-sample tile: hash
+// levels q + 4j (k-tile j/2, upper half when j is odd) from X, the xyz k-tile
+// (columns 2L + {0,1,2} = x*2-1; q = 0 holds (x, y), q = 1 holds (z, 0)).
 
 template <int KH>
 struct AFrag {
@@ -203,93 +314,42 @@ struct AFrag {
 };
 
 template <int KH>
-__device__ __forceinline__ void encode_rows(const SdfParams &P, const float xc0[3],
-                                            const float xc1[3], int q, AFrag<KH> &A,
-                                            float *stash0, float *stash1) {
-    // hash levels q + 4j, j < 2*KH; k-tile j/2, upper half when j is odd
+__device__ __forceinline__ void load_x(const SdfParams &P, int e, int64_t s0, bool v0, bool v1, int lane,
+                                       const float xc0[3], const float xc1[3], AFrag<KH> &A) {
+    const int g = lane >> 2, q = lane & 3;
 #pragma unroll
     for (int j = 0; j < 2 * KH; ++j) {
         const int l = q + 4 * j;
-        float f0[2] = {0.f, 0.f}, f1[2] = {0.f, 0.f};
+        float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
         if (l < P.active) {
-            const uint64_t base = P.lay.offsets[l];
-            const float s = P.lay.scales[l];
-            const LevelPos p0 = level_pos(xc0[0], xc0[1], xc0[2], s);
-            const LevelPos p1 = level_pos(xc1[0], xc1[1], xc1[2], s);
-#pragma unroll
-            for (int cc = 0; cc < 8; ++cc) {
-                const float w0 = corner_weight(p0, cc), w1 = corner_weight(p1, cc);
-                const float2 v0 = load_entry(P.table, P.tdtype, base + corner_index(P.lay, l, p0, cc));
-                const float2 v1 = load_entry(P.table, P.tdtype, base + corner_index(P.lay, l, p1, cc));
-                f0[0] = __fmaf_rn(w0, v0.x, f0[0]);
-                f0[1] = __fmaf_rn(w0, v0.y, f0[1]);
-                f1[0] = __fmaf_rn(w1, v1.x, f1[0]);
-                f1[1] = __fmaf_rn(w1, v1.y, f1[1]);
-            }
+            if (v0) f0 = __ldg(P.X + xidx(P, e, l, s0 + g));
+            if (v1) f1 = __ldg(P.X + xidx(P, e, l, s0 + g + 8));
         }
-        const Split s0 = split2(f0[0], f0[1]);
-        const Split s1 = split2(f1[0], f1[1]);
+        const Split a = split2(f0.x, f0.y), b = split2(f1.x, f1.y);
         const int kt = j >> 1, h = (j & 1) * 2;
-        A.hi[kt][h] = s0.hi;
-        A.lo[kt][h] = s0.lo;
-        A.hi[kt][h + 1] = s1.hi;
-        A.lo[kt][h + 1] = s1.lo;
-        if (stash0) *reinterpret_cast<float2 *>(stash0 + 2 * l) = make_float2(f0[0], f0[1]);
-        if (stash1) *reinterpret_cast<float2 *>(stash1 + 2 * l) = make_float2(f1[0], f1[1]);
+        A.hi[kt][h] = a.hi;
+        A.lo[kt][h] = a.lo;
+        A.hi[kt][h + 1] = b.hi;
+        A.lo[kt][h + 1] = b.lo;
     }
-    // xyz k-tile: cols 2L + {0,1,2} = x*2-1; q = 0 holds (x, y), q = 1 holds (z, 0)
     float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
     if (q == 0) {
-        a0 = __fsub_rn(__fmul_rn(xc0[0], 2.f), 1.f);
-        a1 = __fsub_rn(__fmul_rn(xc0[1], 2.f), 1.f);
-        b0 = __fsub_rn(__fmul_rn(xc1[0], 2.f), 1.f);
-        b1 = __fsub_rn(__fmul_rn(xc1[1], 2.f), 1.f);
+        a0 = x2m1(xc0[0]);
+        a1 = x2m1(xc0[1]);
+        b0 = x2m1(xc1[0]);
+        b1 = x2m1(xc1[1]);
     } else if (q == 1) {
-        a0 = __fsub_rn(__fmul_rn(xc0[2], 2.f), 1.f);
-        b0 = __fsub_rn(__fmul_rn(xc1[2], 2.f), 1.f);
+        a0 = x2m1(xc0[2]);
+        b0 = x2m1(xc1[2]);
     }
-    const Split s0 = split2(a0, a1), s1 = split2(b0, b1);
-    A.hi[KH][0] = s0.hi;
-    A.lo[KH][0] = s0.lo;
-    A.hi[KH][1] = s1.hi;
-    A.lo[KH][1] = s1.lo;
-    A.hi[KH][2] = A.hi[KH][3] = A.lo[KH][2] = A.lo[KH][3] = 0u;
-    if (q < 2) {
-        if (stash0) *reinterpret_cast<float2 *>(stash0 + 16 * KH + 2 * q) = make_float2(a0, a1);
-        if (stash1) *reinterpret_cast<float2 *>(stash1 + 16 * KH + 2 * q) = make_float2(b0, b1);
-    }
-}
-
-// A fragments from stashed fp32 encodings (same positions as encode_rows)
-template <int KH>
-__device__ __forceinline__ void load_rows(const float *st0, const float *st1, int q, AFrag<KH> &A) {
-#pragma unroll
-    for (int j = 0; j < 2 * KH; ++j) {
-        const int l = q + 4 * j;
-        const float2 v0 = st0 ? *reinterpret_cast<const float2 *>(st0 + 2 * l) : make_float2(0.f, 0.f);
-        const float2 v1 = st1 ? *reinterpret_cast<const float2 *>(st1 + 2 * l) : make_float2(0.f, 0.f);
-        const Split s0 = split2(v0.x, v0.y), s1 = split2(v1.x, v1.y);
-        const int kt = j >> 1, h = (j & 1) * 2;
-        A.hi[kt][h] = s0.hi;
-        A.lo[kt][h] = s0.lo;
-        A.hi[kt][h + 1] = s1.hi;
-        A.lo[kt][h + 1] = s1.lo;
-    }
-    float2 v0 = make_float2(0.f, 0.f), v1 = make_float2(0.f, 0.f);
-    if (q < 2) {
-        if (st0) v0 = *reinterpret_cast<const float2 *>(st0 + 16 * KH + 2 * q);
-        if (st1) v1 = *reinterpret_cast<const float2 *>(st1 + 16 * KH + 2 * q);
-    }
-    const Split s0 = split2(v0.x, v0.y), s1 = split2(v1.x, v1.y);
-    A.hi[KH][0] = s0.hi;
-    A.lo[KH][0] = s0.lo;
-    A.hi[KH][1] = s1.hi;
-    A.lo[KH][1] = s1.lo;
+    const Split sa = split2(a0, a1), sb = split2(b0, b1);
+    A.hi[KH][0] = sa.hi;
+    A.lo[KH][0] = sa.lo;
+    A.hi[KH][1] = sb.hi;
+    A.lo[KH][1] = sb.lo;
     A.hi[KH][2] = A.hi[KH][3] = A.lo[KH][2] = A.lo[KH][3] = 0u;
 }
 
-// Hidden layer: D (8 n-tiles) = A (KT k-tiles) x W + b, fp32 C layout.
-// C layout (8 n-tiles) -> softplus -> split A fragments (4 k-tiles)
 // Output layer restricted to the first NTO n-tiles
 template <int NTO>
 __device__ __forceinline__ void out_layer(const uint32_t (&hh)[4][4], const uint32_t (&hl)[4][4],
@@ -313,39 +373,33 @@ __device__ __forceinline__ void out_layer(const uint32_t (&hh)[4][4], const uint
     }
 }
 
-template <int KH, int NH>
-struct Fwd {
-    // hidden activations of the last hidden layer (A fragments) after the MLP
-    uint32_t hh[4][4], hl[4][4];
+// unit FD normal from the six stencil SDFs s[0..5] = (+x,-x,+y,-y,+z,-z)
+__device__ __forceinline__ float fd_grad(const float *s6, float eps, float g[3]) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) g[d] = __fdiv_rn(0.5f * __fsub_rn(s6[2 * d], s6[2 * d + 1]), eps);
+    return sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+}
 
-    __device__ __forceinline__ void run(const AFrag<KH> &A, const NetSmem &net, int lane) {
-        float Z[8][4];
-        hidden_layer<KH + 1>(A.hi, A.lo, net.w1f, net.b1, lane, Z);
-        activate(Z, hh, hl);
-        if (NH == 2) {
-            hidden_layer<4>(hh, hl, net.w2f, net.b2, lane, Z);
-            activate(Z, hh, hl);
-        }
-    }
+// --------------------------------------------------------------- MLP forward
+
+struct FwdWarp {
+    float base[16][3];
+    float s13[16][13];
 };
 
-// ------------------------------------------------------------ forward kernel
-
-template <int KH, int NH, int NT3>
-__global__ void __launch_bounds__(kThreads, 1) sdf_fwd_kernel(const __grid_constant__ SdfParams P) {
+template <int KH, int NH, int NT3, int GROUP>
+__global__ void __launch_bounds__(kThreads) sdf_mlp_fwd_kernel(const __grid_constant__ SdfParams P) {
     extern __shared__ __align__(16) char smem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const angelo_sdf_net_layout &nl = P.nl;
-    // network fragments -> shared memory (forward set + biases)
-    const int64_t fwd_bytes = nl.off_w1b;                   // forward fragments come first
+    const int64_t fwd_bytes = nl.off_w1b;  // forward fragments come first
     const int64_t bias_bytes = nl.bytes - nl.off_b1;
     for (int64_t i = tid * 16; i < fwd_bytes; i += kThreads * 16)
         *reinterpret_cast<uint4 *>(smem + i) = *reinterpret_cast<const uint4 *>(P.net + i);
     for (int64_t i = tid * 4; i < bias_bytes; i += kThreads * 4)
-        *reinterpret_cast<float *>(smem + fwd_bytes + i) =
-            *reinterpret_cast<const float *>(P.net + nl.off_b1 + i);
-    WarpScratch *wsa = reinterpret_cast<WarpScratch *>(smem + fwd_bytes + ((bias_bytes + 15) / 16) * 16);
-    WarpScratch &ws = wsa[warp];
+        *reinterpret_cast<float *>(smem + fwd_bytes + i) = *reinterpret_cast<const float *>(P.net + nl.off_b1 + i);
+    FwdWarp *wsa = reinterpret_cast<FwdWarp *>(smem + fwd_bytes + ((bias_bytes + 15) / 16) * 16);
+    FwdWarp &ws = wsa[warp];
     __syncthreads();
     NetSmem net;
     net.w1f = reinterpret_cast<const uint2 *>(smem + nl.off_w1f);
@@ -355,479 +409,684 @@ __global__ void __launch_bounds__(kThreads, 1) sdf_fwd_kernel(const __grid_const
     net.b2 = reinterpret_cast<const float *>(smem + fwd_bytes + (nl.off_b2 - nl.off_b1));
     net.b3 = reinterpret_cast<const float *>(smem + fwd_bytes + (nl.off_b3 - nl.off_b1));
 
-    const int r = lane >> 2, q = lane & 3;
+    constexpr int e0 = GROUP == kCurv ? 7 : 0;
+    constexpr int ne = GROUP == kPoint ? 1 : (GROUP == kFD ? 7 : 6);
+    const int g = lane >> 2, q = lane & 3;
+    const float r_ = P.radius, eps = P.eps;
     const int64_t n_tiles = (P.S + 15) / 16;
-    const int n_evals = P.with_laplace ? 13 : (P.with_grad ? 7 : 1);
     for (int64_t t = (int64_t)blockIdx.x * kWarps + warp; t < n_tiles; t += (int64_t)gridDim.x * kWarps) {
         const int64_t s0 = t * 16;
         if (lane < 16) {
             const int64_t s = s0 + lane;
-            for (int d = 0; d < 3; ++d) {
-                ws.pos[lane][d] = s < P.S ? P.pos[s * 3 + d] : 0.f;
-                ws.rd[lane][d] = (s < P.S && P.rdir) ? P.rdir[s * 3 + d] : 1.f;
-            }
+            const bool v = s < P.S;
+            const float *src = GROUP == kCurv ? P.state + s * kState + 13 : P.pos + s * 3;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) ws.base[lane][d] = v ? src[d] : 0.f;
+            if (GROUP == kCurv)
+                for (int e = 1; e < 7; ++e) ws.s13[lane][e] = v ? P.state[s * kState + e] : 0.f;
         }
         __syncwarp();
-        const bool v0 = s0 + r < P.S, v1 = s0 + r + 8 < P.S;
-        for (int e = 0; e < n_evals; ++e) {
-            if (e == 7) {
-                // tangent-shifted points (models/geometry.py:236-246)
-                if (lane < 16) {
-                    const float eps = P.eps;
-                    float g[3];
-                    for (int d = 0; d < 3; ++d)
-                        g[d] = __fdiv_rn(0.5f * __fsub_rn(ws.s13[lane][1 + 2 * d], ws.s13[lane][2 + 2 * d]), eps);
-                    const float gn = fmaxf(sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]), 1e-12f);
-                    float nrm[3], rd[3];
-                    const float rn = fmaxf(sqrtf(ws.rd[lane][0] * ws.rd[lane][0] + ws.rd[lane][1] * ws.rd[lane][1] +
-                                                 ws.rd[lane][2] * ws.rd[lane][2]), 1e-12f);
-                    for (int d = 0; d < 3; ++d) {
-                        nrm[d] = g[d] / gn;
-                        rd[d] = ws.rd[lane][d] / rn;
-                        ws.n[lane][d] = nrm[d];
-                    }
-                    const float tg[3] = {nrm[1] * rd[2] - nrm[2] * rd[1], nrm[2] * rd[0] - nrm[0] * rd[2],
-                                         nrm[0] * rd[1] - nrm[1] * rd[0]};
-                    const float r_ = P.radius;
-                    for (int d = 0; d < 3; ++d) {
-                        const float xc = __fdiv_rn(__fsub_rn(ws.pos[lane][d], -r_), __fsub_rn(r_, -r_));
-                        ws.shifted[lane][d] = __fadd_rn(xc, __fmul_rn(tg[d], eps));
-                    }
-                }
-                __syncwarp();
-            }
+        const bool v0 = s0 + g < P.S, v1 = s0 + g + 8 < P.S;
+#pragma unroll 1
+        for (int i = 0; i < ne; ++i) {
+            const int e = e0 + i;
             float xc0[3], xc1[3];
             int m0, m1;
-            eval_point(P, ws, r, e, xc0, &m0);
-            eval_point(P, ws, r + 8, e, xc1, &m1);
+            tap_point(r_, eps, ws.base[g], e, xc0, &m0);
+            tap_point(r_, eps, ws.base[g + 8], e, xc1, &m1);
             AFrag<KH> A;
-            float *st0 = (P.stash_x && v0) ? P.stash_x + ((s0 + r) * 13 + e) * kStashCols : nullptr;
-            float *st1 = (P.stash_x && v1) ? P.stash_x + ((s0 + r + 8) * 13 + e) * kStashCols : nullptr;
-            encode_rows<KH>(P, xc0, xc1, q, A, st0, st1);
-            Fwd<KH, NH> f;
-            f.run(A, net, lane);
-            if (e == 0 && P.with_feature) {
+            load_x<KH>(P, e, s0, v0, v1, lane, xc0, xc1, A);
+            uint32_t hh[4][4], hl[4][4];
+            {
+                float Z[8][4];
+                hidden_layer<KH + 1>(A.hi, A.lo, net.w1f, net.b1, lane, Z);
+                activate(Z, hh, hl);
+                if (NH == 2) {
+                    hidden_layer<4>(hh, hl, net.w2f, net.b2, lane, Z);
+                    activate(Z, hh, hl);
+                }
+            }
+            if (GROUP != kCurv && e == 0 && P.with_feature) {
                 float D[NT3][4];
-                out_layer<NT3>(f.hh, f.hl, net.w3f, NT3, net.b3, lane, D);
+                out_layer<NT3>(hh, hl, net.w3f, NT3, net.b3, lane, D);
                 const int od = nl.out_dim;
 #pragma unroll
                 for (int nt = 0; nt < NT3; ++nt) {
                     const int col = nt * 8 + q * 2;
                     if (v0) {
-                        float *o = P.feature + (s0 + r) * P.feat_stride;
+                        float *o = P.feature + (s0 + g) * P.feat_stride;
                         if (col < od) o[col] = D[nt][0];
                         if (col + 1 < od) o[col + 1] = D[nt][1];
                     }
                     if (v1) {
-                        float *o = P.feature + (s0 + r + 8) * P.feat_stride;
+                        float *o = P.feature + (s0 + g + 8) * P.feat_stride;
                         if (col < od) o[col] = D[nt][2];
                         if (col + 1 < od) o[col + 1] = D[nt][3];
                     }
                 }
                 if (q == 0) {
-                    ws.s13[r][0] = D[0][0];
-                    ws.s13[r + 8][0] = D[0][2];
+                    ws.s13[g][0] = D[0][0];
+                    ws.s13[g + 8][0] = D[0][2];
+#pragma unroll
                     for (int d = 0; d < 3; ++d) {
-                        if (v0) P.feature[(s0 + r) * P.feat_stride + od + d] = __fsub_rn(__fmul_rn(xc0[d], 2.f), 1.f);
-                        if (v1) P.feature[(s0 + r + 8) * P.feat_stride + od + d] = __fsub_rn(__fmul_rn(xc1[d], 2.f), 1.f);
+                        if (v0) P.feature[(s0 + g) * P.feat_stride + od + d] = x2m1(xc0[d]);
+                        if (v1) P.feature[(s0 + g + 8) * P.feat_stride + od + d] = x2m1(xc1[d]);
                     }
                 }
             } else {
                 float D[1][4];
-                out_layer<1>(f.hh, f.hl, net.w3f, NT3, net.b3, lane, D);
+                out_layer<1>(hh, hl, net.w3f, NT3, net.b3, lane, D);
                 if (q == 0) {
-                    ws.s13[r][e] = D[0][0];
-                    ws.s13[r + 8][e] = D[0][2];
+                    ws.s13[g][e] = D[0][0];
+                    ws.s13[g + 8][e] = D[0][2];
                 }
             }
-            __syncwarp();
         }
-        // per-sample outputs
+        __syncwarp();
         if (lane < 16 && s0 + lane < P.S) {
             const int64_t s = s0 + lane;
-            const float eps = P.eps;
-            P.sdf[s] = ws.s13[lane][0];
-            if (P.with_grad) {
-                for (int d = 0; d < 3; ++d)
-                    P.grad[s * 3 + d] =
-                        __fdiv_rn(0.5f * __fsub_rn(ws.s13[lane][1 + 2 * d], ws.s13[lane][2 + 2 * d]), eps);
+            float *st = P.state + s * kState;
+            if (GROUP != kCurv) {
+                P.sdf[s] = ws.s13[lane][0];
+                st[0] = ws.s13[lane][0];
             }
-            if (P.with_laplace) {
-                float g[3];
-                for (int d = 0; d < 3; ++d)
-                    g[d] = __fdiv_rn(0.5f * __fsub_rn(ws.s13[lane][7 + 2 * d], ws.s13[lane][8 + 2 * d]), eps);
-                const float gn = fmaxf(sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]), 1e-12f);
+            if (GROUP == kFD) {
+                float gr[3];
+                const float gn = fmaxf(fd_grad(&ws.s13[lane][1], eps, gr), 1e-12f);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    P.grad[s * 3 + d] = gr[d];
+                    st[1 + 2 * d] = ws.s13[lane][1 + 2 * d];
+                    st[2 + 2 * d] = ws.s13[lane][2 + 2 * d];
+                }
+                if (P.with_laplace) {
+                    // tangent-shifted point (models/geometry.py:236-246): the
+                    // unit normal crossed with the unit random direction, added
+                    // in contracted coordinates
+                    const float *rd = P.rdir + s * 3;
+                    const float rn = fmaxf(sqrtf(rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2]), 1e-12f);
+                    float nrm[3], rdn[3];
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        nrm[d] = gr[d] / gn;
+                        rdn[d] = rd[d] / rn;
+                    }
+                    const float tg[3] = {nrm[1] * rdn[2] - nrm[2] * rdn[1], nrm[2] * rdn[0] - nrm[0] * rdn[2],
+                                         nrm[0] * rdn[1] - nrm[1] * rdn[0]};
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        const float xc = __fdiv_rn(__fsub_rn(ws.base[lane][d], -r_), __fsub_rn(r_, -r_));
+                        st[13 + d] = __fadd_rn(xc, __fmul_rn(tg[d], eps));
+                    }
+                }
+            }
+            if (GROUP == kCurv) {
+                float gr[3], gs[3];
+                const float gn = fmaxf(fd_grad(&ws.s13[lane][1], eps, gr), 1e-12f);
+                const float gsn = fmaxf(fd_grad(&ws.s13[lane][7], eps, gs), 1e-12f);
                 float dot = 0.f;
-                for (int d = 0; d < 3; ++d) dot += ws.n[lane][d] * (g[d] / gn);
+#pragma unroll
+                for (int d = 0; d < 3; ++d) dot += (gr[d] / gn) * (gs[d] / gsn);
                 dot = fminf(fmaxf(dot, -1.0f + 1e-6f), 1.0f - 1e-6f);
                 P.laplace[s] = acosf(dot) / 3.14159265358979f;
+                for (int e = 7; e < 13; ++e) st[e] = ws.s13[lane][e];
             }
-            if (P.stash_s)
-                for (int e = 0; e < 13; ++e) P.stash_s[s * 13 + e] = e < n_evals ? ws.s13[lane][e] : 0.f;
         }
         __syncwarp();
     }
 }
 
-// ----------------------------------------------------------- backward eval
+// -------------------------------------------------------------- MLP backward
 
-struct BwdSmem {
-    const uint2 *w1f, *w2f, *w3f, *w1b, *w2b, *w3b;
-    const float *b1, *b2, *b3, *w3row0;
-    float *dW1, *dW2, *dW3, *db1, *db2, *db3;  // fp32 accumulators, kernel order
-    int K1cols, out_pad;                         // 16*k_tiles1, 16*k_tiles3b
-};
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
 
-// C layout -> split A fragments, no activation
-// dW[n][k] += sum_m dZ[m][n] X[m][k] for a 16-row tile.  dZ given as split A
-// fragments over n (KTN k-tiles), X as split A fragments over k (KTK k-tiles);
-// both are transposed 8x8-blockwise with movmatrix.
-// db[n] += sum over the 16 rows of a C-layout tile set (8 n-tiles)
-// D (NTO n-tiles) = A (4 k-tiles) x Bfrags (KT=4, NT=NT) without bias
-// Backward of one evaluation (rows r, r+8 of the tile).  MODE 0: main point
-// (full output gradient from dL/dsdf and dL/dfeature), 1: FD stencil point
-// (SDF gradient only), 2: shifted stencil point (SDF gradient only, plus the
-// positional gradient into ws.dshift).
-template <int KH, int NH, int NT3, int MODE>
-__device__ __forceinline__ void eval_bwd(const SdfParams &P, const BwdSmem &S, WarpScratch &ws,
-                                         int64_t s0, int e, int lane) {
-    const int r = lane >> 2, q = lane & 3, c = q * 2;
-    const bool v0 = s0 + r < P.S, v1 = s0 + r + 8 < P.S;
-    const float *st0 = v0 ? P.stash_x + ((s0 + r) * 13 + e) * kStashCols : nullptr;
-    const float *st1 = v1 ? P.stash_x + ((s0 + r + 8) * 13 + e) * kStashCols : nullptr;
-    AFrag<KH> X;
-    load_rows<KH>(st0, st1, q, X);
-    // recompute the activations
-    float Z1[8][4];
-    hidden_layer<KH + 1>(X.hi, X.lo, S.w1f, S.b1, lane, Z1);
-    uint32_t h1h[4][4], h1l[4][4];
-    activate(Z1, h1h, h1l);
-    float Z2[8][4];
-    uint32_t h2h[4][4], h2l[4][4];
-    if (NH == 2) {
-        hidden_layer<4>(h1h, h1l, S.w2f, S.b2, lane, Z2);
-        activate(Z2, h2h, h2l);
-    }
-    const uint32_t(&hlh)[4][4] = NH == 2 ? h2h : h1h;
-    const uint32_t(&hll)[4][4] = NH == 2 ? h2l : h1l;
-    float(&Zl)[8][4] = NH == 2 ? Z2 : Z1;
-    // dL/dH_last
-    float dH[8][4];
-    if (MODE == 0) {
-        constexpr int KT3 = (NT3 + 1) / 2;
-        uint32_t yh[KT3][4], yl[KT3][4];
-        const int od = P.nl.out_dim;
-        auto gval = [&](int row, int col, bool valid) -> float {
-            if (!valid || col >= od) return 0.f;
-            float v = P.g_feature ? P.g_feature[(s0 + row) * P.gfeat_stride + col] : 0.f;
-            if (col == 0) v += ws.ds[row][0];
-            return v;
-        };
+__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(smem_u32(p)));
+}
+
+__device__ __forceinline__ void ldsm_x2_t(uint32_t (&r)[2], const void *p) {
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
+                 : "=r"(r[0]), "=r"(r[1])
+                 : "r"(smem_u32(p)));
+}
+
+// Store split A fragments (KT k-tiles, rows g and g+8 of this warp's 16) into
+// row-major bf16 staging arrays hi/lo with row stride ld.
+template <int KT>
+__device__ __forceinline__ void stage_a(const uint32_t (&h)[KT][4], const uint32_t (&l)[KT][4], uint16_t *hi,
+                                        uint16_t *lo, int ld, int row0, int lane) {
+    const int g = lane >> 2, c = (lane & 3) * 2;
 #pragma unroll
-        for (int kt = 0; kt < KT3; ++kt) {
+    for (int kt = 0; kt < KT; ++kt) {
 #pragma unroll
-            for (int hf = 0; hf < 2; ++hf) {
-                const int col = kt * 16 + hf * 8 + c;
-                const Split a = split2(gval(r, col, v0), gval(r, col + 1, v0));
-                const Split b = split2(gval(r + 8, col, v1), gval(r + 8, col + 1, v1));
-                yh[kt][hf * 2] = a.hi;
-                yl[kt][hf * 2] = a.lo;
-                yh[kt][hf * 2 + 1] = b.hi;
-                yl[kt][hf * 2 + 1] = b.lo;
-            }
-        }
-        mm_nobias<KT3, 8>(yh, yl, S.w3b, 8, lane, dH);
-        accumulate_dw<KT3, 4>(yh, yl, hlh, hll, S.dW3, 64, lane);
-        // db3 from the fp32 values
-        float Y[2 * KT3][4];
-#pragma unroll
-        for (int nt = 0; nt < 2 * KT3; ++nt) {
-            const int col = nt * 8 + c;
-            Y[nt][0] = gval(r, col, v0);
-            Y[nt][1] = gval(r, col + 1, v0);
-            Y[nt][2] = gval(r + 8, col, v1);
-            Y[nt][3] = gval(r + 8, col + 1, v1);
-        }
-        accumulate_db<2 * KT3>(Y, S.db3, lane);
-    } else {
-        const float dy0 = v0 ? ws.ds[r][e] : 0.f, dy1 = v1 ? ws.ds[r + 8][e] : 0.f;
-        float part[8][2];
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-            const int col = nt * 8 + c;
-            const float w0 = S.w3row0[col], w1 = S.w3row0[col + 1];
-            dH[nt][0] = dy0 * w0;
-            dH[nt][1] = dy0 * w1;
-            dH[nt][2] = dy1 * w0;
-            dH[nt][3] = dy1 * w1;
-            part[nt][0] = dy0 * softplus100(Zl[nt][0]) + dy1 * softplus100(Zl[nt][2]);
-            part[nt][1] = dy0 * softplus100(Zl[nt][1]) + dy1 * softplus100(Zl[nt][3]);
-        }
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt) {
-#pragma unroll
-            for (int o = 4; o < 32; o <<= 1) {
-                part[nt][0] += __shfl_xor_sync(0xffffffffu, part[nt][0], o);
-                part[nt][1] += __shfl_xor_sync(0xffffffffu, part[nt][1], o);
-            }
-        }
-        float sdy = dy0 + dy1;
-#pragma unroll
-        for (int o = 4; o < 32; o <<= 1) sdy += __shfl_xor_sync(0xffffffffu, sdy, o);
-        if (lane < 4) {
-#pragma unroll
-            for (int nt = 0; nt < 8; ++nt) {
-                red_add(S.dW3 + nt * 8 + lane * 2, part[nt][0]);
-                red_add(S.dW3 + nt * 8 + lane * 2 + 1, part[nt][1]);
-            }
-        }
-        if (lane == 0) red_add(S.db3, sdy);
-    }
-    // through the last hidden activation
-#pragma unroll
-    for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-        for (int i = 0; i < 4; ++i) dH[nt][i] *= softplus100_grad(Zl[nt][i]);
-    uint32_t dzh[4][4], dzl[4][4];
-    c_to_a(dH, dzh, dzl);
-    if (NH == 2) {
-        accumulate_dw<4, 4>(dzh, dzl, h1h, h1l, S.dW2, 64, lane);
-        accumulate_db<8>(dH, S.db2, lane);
-        mm_nobias<4, 8>(dzh, dzl, S.w2b, 8, lane, dH);
-#pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-            for (int i = 0; i < 4; ++i) dH[nt][i] *= softplus100_grad(Z1[nt][i]);
-        c_to_a(dH, dzh, dzl);
-    }
-    accumulate_dw<4, KH + 1>(dzh, dzl, X.hi, X.lo, S.dW1, S.K1cols, lane);
-    accumulate_db<8>(dH, S.db1, lane);
-    // dL/dX: hash columns (n-tiles 0 .. 2KH-1) and, for MODE 2, the xyz tile
-    constexpr int NTX = 2 * KH + (MODE == 2 ? 1 : 0);
-    float dX[NTX][4];
-    mm_nobias<4, NTX>(dzh, dzl, S.w1b, 2 * (KH + 1), lane, dX);
-    float xc0[3], xc1[3];
-    int m0, m1;
-    eval_point(P, ws, r, e, xc0, &m0);
-    eval_point(P, ws, r + 8, e, xc1, &m1);
-    float dxc0[3] = {0.f, 0.f, 0.f}, dxc1[3] = {0.f, 0.f, 0.f};
-    float2 *dt = reinterpret_cast<float2 *>(P.d_table);
-#pragma unroll
-    for (int j = 0; j < 2 * KH; ++j) {
-        const int l = q + 4 * j;
-        const bool lvl_on = l < P.active;
-        const uint64_t base = P.lay.offsets[l];
-        const float sc = P.lay.scales[l];
-#pragma unroll
-        for (int rr = 0; rr < 2; ++rr) {
-            const bool valid = (rr ? v1 : v0) && lvl_on;
-            const float g0 = dX[j][2 * rr], g1 = dX[j][2 * rr + 1];
-            const bool live = valid && (g0 != 0.f || g1 != 0.f);
-            const float *xc = rr ? xc1 : xc0;
-            const LevelPos p = level_pos(xc[0], xc[1], xc[2], sc);
-            float dl[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-            for (int cc = 0; cc < 8; ++cc) {
-                const float w = corner_weight(p, cc);
-                const uint64_t ent = live ? base + corner_index(P.lay, l, p, cc) : 0;
-                // levels 0..7 (j < 2) are coarse: the 16 rows of the tile are
-                // consecutive samples and mostly share corners, so aggregate
-                // over the 8 lanes of a level group (lane stride 4) first
-                if (dt) {
-                    if (j < 2) aggregated_add2<4>(dt, ent, w * g0, w * g1, live);
-                    else if (live) atomicAdd(dt + ent, make_float2(w * g0, w * g1));
-                }
-                if (MODE == 2 && live) {
-                    const float2 v = load_entry(P.table, P.tdtype, ent);
-                    const float gv = g0 * v.x + g1 * v.y;
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        float wd = 1.f;
-#pragma unroll
-                        for (int k = 0; k < 3; ++k)
-                            if (k != d) wd *= (cc >> k) & 1 ? p.f[k] : 1.f - p.f[k];
-                        dl[d] += ((cc >> d) & 1 ? wd : -wd) * gv;
-                    }
-                }
-            }
-            if (MODE == 2) {
-                float *dxc = rr ? dxc1 : dxc0;
-#pragma unroll
-                for (int d = 0; d < 3; ++d) dxc[d] += sc * dl[d];
-            }
-        }
-    }
-    if (MODE == 2) {
-        // xyz columns: q = 0 holds (x, y), q = 1 holds z, of d(x*2-1)
-        if (q == 0) {
-            dxc0[0] += 2.f * dX[2 * KH][0];
-            dxc0[1] += 2.f * dX[2 * KH][1];
-            dxc1[0] += 2.f * dX[2 * KH][2];
-            dxc1[1] += 2.f * dX[2 * KH][3];
-        } else if (q == 1) {
-            dxc0[2] += 2.f * dX[2 * KH][0];
-            dxc1[2] += 2.f * dX[2 * KH][2];
-        }
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-#pragma unroll
-            for (int o = 1; o < 4; o <<= 1) {
-                dxc0[d] += __shfl_xor_sync(0xffffffffu, dxc0[d], o);
-                dxc1[d] += __shfl_xor_sync(0xffffffffu, dxc1[d], o);
-            }
-        }
-        if (q == 0) {
-            const float inv = 1.0f / __fsub_rn(P.radius, -P.radius);
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-                if ((m0 >> d) & 1) ws.dshift[r][d] += dxc0[d] * inv;
-                if ((m1 >> d) & 1) ws.dshift[r + 8][d] += dxc1[d] * inv;
-            }
+        for (int i = 0; i < 4; ++i) {
+            const int row = row0 + g + ((i & 1) << 3);
+            const int col = kt * 16 + ((i >> 1) << 3) + c;
+            *reinterpret_cast<uint32_t *>(hi + row * ld + col) = h[kt][i];
+            *reinterpret_cast<uint32_t *>(lo + row * ld + col) = l[kt][i];
         }
     }
 }
 
+// acc[i] += dZ^T B over the kStageRows staged rows, for output tile (mt, nt0 + i):
+// A = dZ^T (m = unit, k = row) read transposed from the row-major dZ staging,
+// B (k = row, n = input column) read transposed from the row-major input staging.
+template <int NTW>
+__device__ __forceinline__ void staged_dw(float (&acc)[NTW][4], const uint16_t *zh, const uint16_t *zl,
+                                          const uint16_t *bh, const uint16_t *bl, int ldb, int mt, int nt0,
+                                          int lane) {
+    const int i8 = lane >> 3, j8 = lane & 7;
+#pragma unroll 2
+    for (int k0 = 0; k0 < kStageRows; k0 += 16) {
+        const int arow = k0 + j8 + ((i8 >> 1) << 3), acol = mt * 16 + ((i8 & 1) << 3);
+        uint32_t ah[4], al[4];
+        ldsm_x4_t(ah, zh + arow * kStageLd + acol);
+        ldsm_x4_t(al, zl + arow * kStageLd + acol);
+        const int brow = k0 + j8 + ((i8 & 1) << 3);
+#pragma unroll
+        for (int i = 0; i < NTW; ++i) {
+            uint32_t b_h[2], b_l[2];
+            ldsm_x2_t(b_h, bh + brow * ldb + (nt0 + i) * 8);
+            ldsm_x2_t(b_l, bl + brow * ldb + (nt0 + i) * 8);
+            mma_x3(acc[i], ah, al, make_uint2(b_h[0], b_h[1]), make_uint2(b_l[0], b_l[1]));
+        }
+    }
+}
+
+struct BwdWarp {
+    float base[16][3];
+    float ds[16][13];   // dL/d(sdf) of each evaluation
+};
+
+struct BwdSmem {
+    const uint2 *w1f, *w2f, *w1b, *w2b, *w3b;
+    const float *b1, *b2, *w3row0;
+    float *dW3, *db1, *db2, *db3;  // shared fp32 accumulators, kernel order
+    uint16_t *zh, *zl, *bh, *bl;   // staging
+};
+
 template <int KH, int NH, int NT3>
-__global__ void __launch_bounds__(kThreads, 1) sdf_bwd_kernel(const __grid_constant__ SdfParams P) {
+struct BwdShape {
+    static constexpr int KT3 = (NT3 + 1) / 2;
+    static constexpr int XS = 16 * (KH + 1) + 8;      // staged input row stride (bf16)
+    static constexpr int OUTP = 16 * KT3;
+    static constexpr int64_t w1f = 2 * (KH + 1) * 8 * 32 * 8;
+    static constexpr int64_t w2f = NH == 2 ? 2 * 4 * 8 * 32 * 8 : 0;
+    static constexpr int64_t w1b = 2 * 4 * (2 * (KH + 1)) * 32 * 8;
+    static constexpr int64_t w2b = NH == 2 ? 2 * 4 * 8 * 32 * 8 : 0;
+    static constexpr int64_t w3b = 2 * KT3 * 8 * 32 * 8;
+    static constexpr int64_t vec = (3 * 64) * 4;
+    static constexpr int64_t acc = (OUTP * 64 + 64 + 64 + OUTP) * 4;
+    static constexpr int64_t stage1 = (int64_t)kStageRows * (kStageLd + XS) * 2 * 2;
+    static constexpr int64_t stage2 = NH == 2 ? (int64_t)kStageRows * (kStageLd + kStageLd) * 2 * 2 : 0;
+    static constexpr int64_t stage = stage1 > stage2 ? stage1 : stage2;
+    static constexpr int64_t off_w2f = w1f, off_w1b = off_w2f + w2f, off_w2b = off_w1b + w1b,
+                             off_w3b = off_w2b + w2b, off_vec = off_w3b + w3b, off_acc = off_vec + vec,
+                             off_stage = (off_acc + acc + 15) / 16 * 16, off_warp = off_stage + stage;
+    static constexpr int64_t bytes = off_warp + kWarps * sizeof(BwdWarp);
+};
+
+template <int KH, int NH, int NT3, int GROUP>
+__global__ void __launch_bounds__(kThreads, 1) sdf_mlp_bwd_kernel(const __grid_constant__ SdfParams P) {
+    using Sh = BwdShape<KH, NH, NT3>;
+    constexpr int KT3 = Sh::KT3;
     extern __shared__ __align__(16) char smem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const angelo_sdf_net_layout &nl = P.nl;
-    const int64_t net_bytes = nl.bytes;
-    for (int64_t i = tid * 16; i < net_bytes; i += kThreads * 16)
-        *reinterpret_cast<uint4 *>(smem + i) = *reinterpret_cast<const uint4 *>(P.net + i);
+    auto copy16 = [&](int64_t dst, int64_t src, int64_t bytes) {
+        for (int64_t i = tid * 16; i < bytes; i += kThreads * 16)
+            *reinterpret_cast<uint4 *>(smem + dst + i) = *reinterpret_cast<const uint4 *>(P.net + src + i);
+    };
+    copy16(0, nl.off_w1f, Sh::w1f);
+    if (NH == 2) copy16(Sh::off_w2f, nl.off_w2f, Sh::w2f);
+    copy16(Sh::off_w1b, nl.off_w1b, Sh::w1b);
+    if (NH == 2) copy16(Sh::off_w2b, nl.off_w2b, Sh::w2b);
+    if (GROUP != kCurv) copy16(Sh::off_w3b, nl.off_w3b, Sh::w3b);
+    float *vec = reinterpret_cast<float *>(smem + Sh::off_vec);
+    for (int i = tid; i < 64; i += kThreads) {
+        vec[i] = reinterpret_cast<const float *>(P.net + nl.off_b1)[i];
+        vec[64 + i] = NH == 2 ? reinterpret_cast<const float *>(P.net + nl.off_b2)[i] : 0.f;
+        vec[128 + i] = reinterpret_cast<const float *>(P.net + nl.off_w3row0)[i];
+    }
+    float *acc = reinterpret_cast<float *>(smem + Sh::off_acc);
+    const int n_acc = Sh::OUTP * 64 + 64 + 64 + Sh::OUTP;
+    for (int i = tid; i < n_acc; i += kThreads) acc[i] = 0.f;
     BwdSmem S;
-    S.w1f = reinterpret_cast<const uint2 *>(smem + nl.off_w1f);
-    S.w2f = reinterpret_cast<const uint2 *>(smem + nl.off_w2f);
-    S.w3f = reinterpret_cast<const uint2 *>(smem + nl.off_w3f);
-    S.w1b = reinterpret_cast<const uint2 *>(smem + nl.off_w1b);
-    S.w2b = reinterpret_cast<const uint2 *>(smem + nl.off_w2b);
-    S.w3b = reinterpret_cast<const uint2 *>(smem + nl.off_w3b);
-    S.b1 = reinterpret_cast<const float *>(smem + nl.off_b1);
-    S.b2 = reinterpret_cast<const float *>(smem + nl.off_b2);
-    S.b3 = reinterpret_cast<const float *>(smem + nl.off_b3);
-    S.w3row0 = reinterpret_cast<const float *>(smem + nl.off_w3row0);
-    S.K1cols = 16 * nl.k_tiles1;
-    S.out_pad = 16 * nl.k_tiles3b;
-    float *acc = reinterpret_cast<float *>(smem + net_bytes);
-    const int n1 = 64 * S.K1cols, n2 = 64 * 64, n3 = S.out_pad * 64;
-    const int n_acc = n1 + n2 + n3 + 64 + 64 + S.out_pad;
-    S.dW1 = acc;
-    S.dW2 = acc + n1;
-    S.dW3 = acc + n1 + n2;
-    S.db1 = acc + n1 + n2 + n3;
+    S.w1f = reinterpret_cast<const uint2 *>(smem);
+    S.w2f = reinterpret_cast<const uint2 *>(smem + Sh::off_w2f);
+    S.w1b = reinterpret_cast<const uint2 *>(smem + Sh::off_w1b);
+    S.w2b = reinterpret_cast<const uint2 *>(smem + Sh::off_w2b);
+    S.w3b = reinterpret_cast<const uint2 *>(smem + Sh::off_w3b);
+    S.b1 = vec;
+    S.b2 = vec + 64;
+    S.w3row0 = vec + 128;
+    S.dW3 = acc;
+    S.db1 = acc + Sh::OUTP * 64;
     S.db2 = S.db1 + 64;
     S.db3 = S.db2 + 64;
-    for (int i = tid; i < n_acc; i += kThreads) acc[i] = 0.f;
-    WarpScratch *wsa = reinterpret_cast<WarpScratch *>(acc + ((n_acc + 3) / 4) * 4);
-    WarpScratch &ws = wsa[warp];
+    // staging: phase 2 (two hidden layers) dZ2 | H1, phase 1 dZ1 | X
+    uint16_t *zh = reinterpret_cast<uint16_t *>(smem + Sh::off_stage);
+    uint16_t *zl = zh + kStageRows * kStageLd;
+    uint16_t *b1h = zl + kStageRows * kStageLd, *b1l = b1h + kStageRows * Sh::XS;
+    uint16_t *b2h = b1h, *b2l = b2h + kStageRows * kStageLd;
+    BwdWarp &ws = reinterpret_cast<BwdWarp *>(smem + Sh::off_warp)[warp];
     __syncthreads();
 
+    // dW tiles owned by this warp: unit block mt = warp / 2, n-tiles nt1 ..
+    // nt1 + KH of the first layer and nt2 .. nt2 + 3 of the second
+    const int mt = warp >> 1, nt1 = (warp & 1) * (KH + 1), nt2 = (warp & 1) * 4;
+    float acc1[KH + 1][4], acc2[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            if (i < KH + 1) acc1[i][j] = 0.f;
+            acc2[i][j] = 0.f;
+        }
+    }
+
+    constexpr int e0 = GROUP == kCurv ? 7 : 0;
+    constexpr int ne = GROUP == kPoint ? 1 : (GROUP == kFD ? 7 : 6);
+    const int g = lane >> 2, q = lane & 3, c = q * 2;
+    const float r_ = P.radius, eps = P.eps;
+    const float inv2r = 1.0f / __fsub_rn(r_, -r_);
     const int64_t n_tiles = (P.S + 15) / 16;
-    const float eps = P.eps;
-    for (int64_t t = (int64_t)blockIdx.x * kWarps + warp; t < n_tiles; t += (int64_t)gridDim.x * kWarps) {
-        const int64_t s0 = t * 16;
+    // CTA-uniform loop (the staged dW GEMM synchronises the CTA); tiles past
+    // the end have no valid rows and contribute zeros
+    for (int64_t tb = (int64_t)blockIdx.x * kWarps; tb < n_tiles; tb += (int64_t)gridDim.x * kWarps) {
+        const int64_t s0 = (tb + warp) * 16;
         if (lane < 16) {
             const int64_t s = s0 + lane;
             const bool v = s < P.S;
-            for (int d = 0; d < 3; ++d) {
-                ws.pos[lane][d] = v ? P.pos[s * 3 + d] : 0.f;
-                ws.rd[lane][d] = (v && P.rdir) ? P.rdir[s * 3 + d] : 1.f;
-                ws.dshift[lane][d] = 0.f;
-            }
-            for (int e = 0; e < 13; ++e) {
-                ws.s13[lane][e] = v ? P.stash_s[s * 13 + e] : 0.f;
-                ws.ds[lane][e] = 0.f;
-            }
-            // forward quantities of the stencil arithmetic
-            float g[3], n[3];
-            for (int d = 0; d < 3; ++d)
-                g[d] = __fdiv_rn(0.5f * __fsub_rn(ws.s13[lane][1 + 2 * d], ws.s13[lane][2 + 2 * d]), eps);
-            const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-            for (int d = 0; d < 3; ++d) n[d] = g[d] / fmaxf(gn, 1e-12f);
-            if (P.with_laplace && v) {
-                float rd[3];
-                const float rn = fmaxf(sqrtf(ws.rd[lane][0] * ws.rd[lane][0] + ws.rd[lane][1] * ws.rd[lane][1] +
-                                             ws.rd[lane][2] * ws.rd[lane][2]), 1e-12f);
-                for (int d = 0; d < 3; ++d) rd[d] = ws.rd[lane][d] / rn;
-                const float tg[3] = {n[1] * rd[2] - n[2] * rd[1], n[2] * rd[0] - n[0] * rd[2],
-                                     n[0] * rd[1] - n[1] * rd[0]};
-                const float r_ = P.radius;
+            const float *st = P.state + s * kState;
+            const float *src = GROUP == kCurv ? st + 13 : P.pos + s * 3;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) ws.base[lane][d] = v ? src[d] : 0.f;
+            for (int e = 0; e < 13; ++e) ws.ds[lane][e] = 0.f;
+            if (v && GROUP == kCurv) {
+                // curvature (models/geometry.py:247-251) back to the six
+                // shifted-stencil SDFs; dL/dnormal from it kept for the FD pass
+                float gr[3], gs[3], n[3], ns[3], dns[3], dgs[3];
+                const float gn = fd_grad(st + 1, eps, gr);
+                const float gsn = fd_grad(st + 7, eps, gs);
+#pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    const float xc = __fdiv_rn(__fsub_rn(ws.pos[lane][d], -r_), __fsub_rn(r_, -r_));
-                    ws.shifted[lane][d] = __fadd_rn(xc, __fmul_rn(tg[d], eps));
+                    n[d] = gr[d] / fmaxf(gn, 1e-12f);
+                    ns[d] = gs[d] / fmaxf(gsn, 1e-12f);
                 }
-                float gs[3], ns[3];
-                for (int d = 0; d < 3; ++d)
-                    gs[d] = __fdiv_rn(0.5f * __fsub_rn(ws.s13[lane][7 + 2 * d], ws.s13[lane][8 + 2 * d]), eps);
-                const float gsn = sqrtf(gs[0] * gs[0] + gs[1] * gs[1] + gs[2] * gs[2]);
-                for (int d = 0; d < 3; ++d) ns[d] = gs[d] / fmaxf(gsn, 1e-12f);
                 const float dot = n[0] * ns[0] + n[1] * ns[1] + n[2] * ns[2];
                 const float lo = -1.0f + 1e-6f, hi = 1.0f - 1e-6f;
                 const float dotc = fminf(fmaxf(dot, lo), hi);
                 const float dang = P.g_laplace ? P.g_laplace[s] / 3.14159265358979f : 0.f;
                 const float ddot = (dot >= lo && dot <= hi) ? -dang / sqrtf(1.0f - dotc * dotc) : 0.f;
-                float dns[3], dgs[3];
+#pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    ws.n[lane][d] = ddot * ns[d];  // dL/dn from the curvature, completed later
+                    P.bstate[s * kBState + 3 + d] = ddot * ns[d];
                     dns[d] = ddot * n[d];
                 }
                 normalize_bwd(gs, gsn, ns, dns, dgs);
+#pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     const float h = __fdiv_rn(0.5f * dgs[d], eps);
                     ws.ds[lane][7 + 2 * d] = h;
                     ws.ds[lane][8 + 2 * d] = -h;
                 }
-            } else {
-                for (int d = 0; d < 3; ++d) ws.n[lane][d] = 0.f;
             }
-            ws.ds[lane][0] = (v && P.g_sdf) ? P.g_sdf[s] : 0.f;
-        }
-        __syncwarp();
-        if (P.with_laplace)
-            for (int e = 7; e < 13; ++e) eval_bwd<KH, NH, NT3, 2>(P, S, ws, s0, e, lane);
-        __syncwarp();
-        if (lane < 16 && P.with_grad) {
-            const int64_t s = s0 + lane;
-            const bool v = s < P.S;
-            float g[3], n[3], dn[3], dg[3];
-            for (int d = 0; d < 3; ++d)
-                g[d] = __fdiv_rn(0.5f * __fsub_rn(ws.s13[lane][1 + 2 * d], ws.s13[lane][2 + 2 * d]), eps);
-            const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-            for (int d = 0; d < 3; ++d) {
-                n[d] = g[d] / fmaxf(gn, 1e-12f);
-                dn[d] = ws.n[lane][d];
-            }
-            if (P.with_laplace && v) {
-                float rd[3], dtg[3];
-                const float rn = fmaxf(sqrtf(ws.rd[lane][0] * ws.rd[lane][0] + ws.rd[lane][1] * ws.rd[lane][1] +
-                                             ws.rd[lane][2] * ws.rd[lane][2]), 1e-12f);
-                for (int d = 0; d < 3; ++d) {
-                    rd[d] = ws.rd[lane][d] / rn;
-                    dtg[d] = ws.dshift[lane][d] * eps;
+            if (v && GROUP != kCurv) {
+                ws.ds[lane][0] = P.g_sdf ? P.g_sdf[s] : 0.f;
+                if (GROUP == kFD) {
+                    // FD gradient (and, with curvature, the normal that set the
+                    // tangent shift) back to the six stencil SDFs
+                    float gr[3], n[3], dn[3] = {0.f, 0.f, 0.f}, dg[3];
+                    const float gn = fd_grad(st + 1, eps, gr);
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) n[d] = gr[d] / fmaxf(gn, 1e-12f);
+                    if (P.with_laplace) {
+                        const float *rd = P.rdir + s * 3;
+                        const float *bs = P.bstate + s * kBState;
+                        const float rn = fmaxf(sqrtf(rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2]), 1e-12f);
+                        float rdn[3], dtg[3];
+#pragma unroll
+                        for (int d = 0; d < 3; ++d) {
+                            rdn[d] = rd[d] / rn;
+                            dtg[d] = bs[d] * eps;
+                            dn[d] = bs[3 + d];
+                        }
+                        // t = n x rd  ->  dL/dn += rd x dL/dt
+                        dn[0] += rdn[1] * dtg[2] - rdn[2] * dtg[1];
+                        dn[1] += rdn[2] * dtg[0] - rdn[0] * dtg[2];
+                        dn[2] += rdn[0] * dtg[1] - rdn[1] * dtg[0];
+                    }
+                    normalize_bwd(gr, gn, n, dn, dg);
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        const float gin = P.g_grad ? P.g_grad[s * 3 + d] : 0.f;
+                        const float h = __fdiv_rn(0.5f * (dg[d] + gin), eps);
+                        ws.ds[lane][1 + 2 * d] = h;
+                        ws.ds[lane][2 + 2 * d] = -h;
+                    }
                 }
-                // t = n x rd  ->  dL/dn += rd x dL/dt
-                dn[0] += rd[1] * dtg[2] - rd[2] * dtg[1];
-                dn[1] += rd[2] * dtg[0] - rd[0] * dtg[2];
-                dn[2] += rd[0] * dtg[1] - rd[1] * dtg[0];
-            }
-            normalize_bwd(g, gn, n, dn, dg);
-            for (int d = 0; d < 3; ++d) {
-                const float gin = (v && P.g_grad) ? P.g_grad[s * 3 + d] : 0.f;
-                const float h = __fdiv_rn(0.5f * (dg[d] + gin), eps);
-                ws.ds[lane][1 + 2 * d] = v ? h : 0.f;
-                ws.ds[lane][2 + 2 * d] = v ? -h : 0.f;
             }
         }
         __syncwarp();
-        if (P.with_grad)
-            for (int e = 1; e < 7; ++e) eval_bwd<KH, NH, NT3, 1>(P, S, ws, s0, e, lane);
-        eval_bwd<KH, NH, NT3, 0>(P, S, ws, s0, 0, lane);
+        const bool v0 = s0 + g < P.S, v1 = s0 + g + 8 < P.S;
+        float dsh0[3] = {0.f, 0.f, 0.f}, dsh1[3] = {0.f, 0.f, 0.f};
+#pragma unroll 1
+        for (int i = 0; i < ne; ++i) {
+            const int e = e0 + i;
+            float xc0[3], xc1[3];
+            int m0, m1;
+            tap_point(r_, eps, ws.base[g], e, xc0, &m0);
+            tap_point(r_, eps, ws.base[g + 8], e, xc1, &m1);
+            AFrag<KH> X;
+            load_x<KH>(P, e, s0, v0, v1, lane, xc0, xc1, X);
+            // recompute the activations
+            float Z1[8][4];
+            hidden_layer<KH + 1>(X.hi, X.lo, S.w1f, S.b1, lane, Z1);
+            uint32_t h1h[4][4], h1l[4][4];
+            activate(Z1, h1h, h1l);
+            float Z2[8][4];
+            uint32_t h2h[4][4], h2l[4][4];
+            if (NH == 2) {
+                hidden_layer<4>(h1h, h1l, S.w2f, S.b2, lane, Z2);
+                activate(Z2, h2h, h2l);
+            }
+            const uint32_t(&hlh)[4][4] = NH == 2 ? h2h : h1h;
+            const uint32_t(&hll)[4][4] = NH == 2 ? h2l : h1l;
+            const float(&Zl)[8][4] = NH == 2 ? Z2 : Z1;
+            // dL/dH of the last hidden layer
+            float dH[8][4];
+            if (GROUP != kCurv && e == 0) {
+                // the point: the whole output row (dL/dfeature; column 0 also dL/dsdf)
+                const int od = nl.out_dim;
+                auto gval = [&](int row, int col, bool valid) -> float {
+                    if (!valid || col >= od) return 0.f;
+                    float v = P.g_feature ? P.g_feature[(s0 + row) * P.gfeat_stride + col] : 0.f;
+                    if (col == 0) v += ws.ds[row][0];
+                    return v;
+                };
+                uint32_t yh[KT3][4], yl[KT3][4];
+#pragma unroll
+                for (int kt = 0; kt < KT3; ++kt) {
+#pragma unroll
+                    for (int hf = 0; hf < 2; ++hf) {
+                        const int col = kt * 16 + hf * 8 + c;
+                        const Split a = split2(gval(g, col, v0), gval(g, col + 1, v0));
+                        const Split b = split2(gval(g + 8, col, v1), gval(g + 8, col + 1, v1));
+                        yh[kt][hf * 2] = a.hi;
+                        yl[kt][hf * 2] = a.lo;
+                        yh[kt][hf * 2 + 1] = b.hi;
+                        yl[kt][hf * 2 + 1] = b.lo;
+                    }
+                }
+                mm_nobias<KT3, 8>(yh, yl, S.w3b, 8, lane, dH);
+                accumulate_dw<KT3, 4>(yh, yl, hlh, hll, S.dW3, 64, lane);
+                float Y[2 * KT3][4];
+#pragma unroll
+                for (int nt = 0; nt < 2 * KT3; ++nt) {
+                    const int col = nt * 8 + c;
+                    Y[nt][0] = gval(g, col, v0);
+                    Y[nt][1] = gval(g, col + 1, v0);
+                    Y[nt][2] = gval(g + 8, col, v1);
+                    Y[nt][3] = gval(g + 8, col + 1, v1);
+                }
+                accumulate_db<2 * KT3>(Y, S.db3, lane);
+            } else {
+                // a stencil tap: only the SDF column carries a gradient
+                const float dy0 = v0 ? ws.ds[g][e] : 0.f, dy1 = v1 ? ws.ds[g + 8][e] : 0.f;
+                float part[8][2];
+#pragma unroll
+                for (int nt = 0; nt < 8; ++nt) {
+                    const int col = nt * 8 + c;
+                    const float w0 = S.w3row0[col], w1 = S.w3row0[col + 1];
+                    dH[nt][0] = dy0 * w0;
+                    dH[nt][1] = dy0 * w1;
+                    dH[nt][2] = dy1 * w0;
+                    dH[nt][3] = dy1 * w1;
+                    part[nt][0] = dy0 * softplus100(Zl[nt][0]) + dy1 * softplus100(Zl[nt][2]);
+                    part[nt][1] = dy0 * softplus100(Zl[nt][1]) + dy1 * softplus100(Zl[nt][3]);
+                }
+#pragma unroll
+                for (int nt = 0; nt < 8; ++nt) {
+#pragma unroll
+                    for (int o = 4; o < 32; o <<= 1) {
+                        part[nt][0] += __shfl_xor_sync(0xffffffffu, part[nt][0], o);
+                        part[nt][1] += __shfl_xor_sync(0xffffffffu, part[nt][1], o);
+                    }
+                }
+                float sdy = dy0 + dy1;
+#pragma unroll
+                for (int o = 4; o < 32; o <<= 1) sdy += __shfl_xor_sync(0xffffffffu, sdy, o);
+                if (lane < 4) {
+#pragma unroll
+                    for (int nt = 0; nt < 8; ++nt) {
+                        red_add(S.dW3 + nt * 8 + lane * 2, part[nt][0]);
+                        red_add(S.dW3 + nt * 8 + lane * 2 + 1, part[nt][1]);
+                    }
+                }
+                if (lane == 0) red_add(S.db3, sdy);
+            }
+#pragma unroll
+            for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                for (int k = 0; k < 4; ++k) dH[nt][k] *= softplus100_grad(Zl[nt][k]);
+            uint32_t dzh[4][4], dzl[4][4];
+            c_to_a(dH, dzh, dzl);
+            if (NH == 2) {
+                accumulate_db<8>(dH, S.db2, lane);
+                stage_a<4>(dzh, dzl, zh, zl, kStageLd, warp * 16, lane);
+                stage_a<4>(h1h, h1l, b2h, b2l, kStageLd, warp * 16, lane);
+                __syncthreads();
+                staged_dw<4>(acc2, zh, zl, b2h, b2l, kStageLd, mt, nt2, lane);
+                __syncthreads();
+                mm_nobias<4, 8>(dzh, dzl, S.w2b, 8, lane, dH);
+#pragma unroll
+                for (int nt = 0; nt < 8; ++nt)
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) dH[nt][k] *= softplus100_grad(Z1[nt][k]);
+                c_to_a(dH, dzh, dzl);
+            }
+            accumulate_db<8>(dH, S.db1, lane);
+            stage_a<4>(dzh, dzl, zh, zl, kStageLd, warp * 16, lane);
+            stage_a<KH + 1>(X.hi, X.lo, b1h, b1l, Sh::XS, warp * 16, lane);
+            __syncthreads();
+            staged_dw<KH + 1>(acc1, zh, zl, b1h, b1l, Sh::XS, mt, nt1, lane);
+            __syncthreads();
+            // dL/dX: hash columns (n-tiles 0 .. 2KH-1; lane q holds level 4 nt + q)
+            // and, for the curvature taps, the xyz n-tile
+            constexpr int NTX = 2 * KH + (GROUP == kCurv ? 1 : 0);
+            float dX[NTX][4];
+            mm_nobias<4, NTX>(dzh, dzl, S.w1b, 2 * (KH + 1), lane, dX);
+#pragma unroll
+            for (int nt = 0; nt < 2 * KH; ++nt) {
+                const int l = nt * 4 + q;
+                if (l < P.active) {
+                    if (v0) P.dX[xidx(P, e, l, s0 + g)] = make_float2(dX[nt][0], dX[nt][1]);
+                    if (v1) P.dX[xidx(P, e, l, s0 + g + 8)] = make_float2(dX[nt][2], dX[nt][3]);
+                }
+            }
+            if (GROUP == kCurv) {
+                // xyz columns x*2-1: q = 0 holds (x, y), q = 1 holds z
+                float d0[3] = {0.f, 0.f, 0.f}, d1[3] = {0.f, 0.f, 0.f};
+                if (q == 0) {
+                    d0[0] = 2.f * dX[NTX - 1][0];
+                    d0[1] = 2.f * dX[NTX - 1][1];
+                    d1[0] = 2.f * dX[NTX - 1][2];
+                    d1[1] = 2.f * dX[NTX - 1][3];
+                } else if (q == 1) {
+                    d0[2] = 2.f * dX[NTX - 1][0];
+                    d1[2] = 2.f * dX[NTX - 1][2];
+                }
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    if ((m0 >> d) & 1) dsh0[d] += d0[d] * inv2r;
+                    if ((m1 >> d) & 1) dsh1[d] += d1[d] * inv2r;
+                }
+            }
+        }
+        if (GROUP == kCurv) {
+            // dL/dshifted from the xyz columns; the scatter pass adds the hash
+            // grid's positional derivative atomically
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+#pragma unroll
+                for (int o = 1; o < 4; o <<= 1) {
+                    dsh0[d] += __shfl_xor_sync(0xffffffffu, dsh0[d], o);
+                    dsh1[d] += __shfl_xor_sync(0xffffffffu, dsh1[d], o);
+                }
+            }
+            if (q == 0) {
+#pragma unroll
+                for (int d = 0; d < 3; ++d) {
+                    if (v0) P.bstate[(s0 + g) * kBState + d] = dsh0[d];
+                    if (v1) P.bstate[(s0 + g + 8) * kBState + d] = dsh1[d];
+                }
+            }
+        }
         __syncwarp();
     }
+    // one flush per CTA: register-held dW1 / dW2 tiles, shared dW3 and biases
     __syncthreads();
+    const int K1c = 16 * (KH + 1);
+#pragma unroll
+    for (int i = 0; i < KH + 1; ++i) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const int row = mt * 16 + g + ((j >> 1) << 3), col = (nt1 + i) * 8 + c + (j & 1);
+            if (acc1[i][j] != 0.f) atomicAdd(P.d_net + row * K1c + col, acc1[i][j]);
+        }
+    }
+    if (NH == 2) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int row = mt * 16 + g + ((j >> 1) << 3), col = (nt2 + i) * 8 + c + (j & 1);
+                if (acc2[i][j] != 0.f) atomicAdd(P.d_net + 64 * K1c + row * 64 + col, acc2[i][j]);
+            }
+        }
+    }
     for (int i = tid; i < n_acc; i += kThreads) {
         const float v = acc[i];
-        if (v != 0.f) atomicAdd(P.d_net + i, v);
+        if (v != 0.f) atomicAdd(P.d_net + 64 * K1c + 64 * 64 + i, v);
+    }
+}
+
+// ------------------------------------------------------------------ scatter
+
+__device__ __forceinline__ void centre_add(float2 (&acc)[8], int delta, int cc, int d, float2 v) {
+    const int o = ((cc >> d) & 1) == 0 ? (cc | (1 << d)) : (cc & ~(1 << d));
+    const bool z = delta == 0;
+    acc[cc].x += z ? v.x : 0.f;
+    acc[cc].y += z ? v.y : 0.f;
+    acc[o].x += z ? 0.f : v.x;
+    acc[o].y += z ? 0.f : v.y;
+}
+
+template <int GROUP>
+__global__ void __launch_bounds__(kEncThreads) stencil_scatter_kernel(const __grid_constant__ SdfParams P) {
+    const int l = blockIdx.y;
+    const int64_t s = (int64_t)blockIdx.x * kEncThreads + threadIdx.x;
+    const bool valid = s < P.S;
+    const int64_t sv = valid ? s : P.S - 1;   // lanes past the end stay for the warp-collective adds
+    const float r = P.radius, eps = P.eps;
+    const float *src = GROUP == kCurv ? P.state + sv * kState + 13 : P.pos + sv * 3;
+    const float base[3] = {src[0], src[1], src[2]};
+    const float sc = P.lay.scales[l];
+    const uint64_t off = P.lay.offsets[l];
+    float2 *dt = reinterpret_cast<float2 *>(P.d_table);
+    float xcc[3];
+    clamped_centre(r, base, xcc);
+    const LevelPos pc = level_pos(xcc[0], xcc[1], xcc[2], sc);
+    float2 acc[8], vc[8];
+#pragma unroll
+    for (int cc = 0; cc < 8; ++cc) {
+        acc[cc] = make_float2(0.f, 0.f);
+        vc[cc] = make_float2(0.f, 0.f);
+        if (GROUP == kCurv && valid) vc[cc] = load_entry(P.table, P.tdtype, off + corner_index(P.lay, l, pc, cc));
+    }
+    float dsh[3] = {0.f, 0.f, 0.f};
+    if (GROUP != kCurv) {
+        const float2 gx = valid ? P.dX[xidx(P, 0, l, s)] : make_float2(0.f, 0.f);
+        const bool live = valid && (gx.x != 0.f || gx.y != 0.f);
+        float xc[3];
+        int m;
+        tap_point(r, eps, base, 0, xc, &m);
+        const LevelPos p = level_pos(xc[0], xc[1], xc[2], sc);
+        const bool same = p.g[0] == pc.g[0] && p.g[1] == pc.g[1] && p.g[2] == pc.g[2];
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+            const float w = corner_weight(p, cc);
+            const float2 v = make_float2(w * gx.x, w * gx.y);
+            if (same) {
+                acc[cc].x += v.x;
+                acc[cc].y += v.y;
+            } else if (live && dt) {
+                atomicAdd(dt + off + corner_index(P.lay, l, p, cc), v);
+            }
+        }
+    }
+    if (GROUP != kPoint) {
+        constexpr int e0 = GROUP == kFD ? 1 : 7;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) {
+            const int d = k >> 1;
+            const float2 gx = valid ? P.dX[xidx(P, e0 + k, l, s)] : make_float2(0.f, 0.f);
+            const bool live = valid && (gx.x != 0.f || gx.y != 0.f);
+            float xc[3];
+            int m, delta;
+            tap_point(r, eps, base, e0 + k, xc, &m);
+            const LevelPos p = level_pos(xc[0], xc[1], xc[2], sc);
+            const bool aligned = tap_aligned(p, pc, d, &delta);
+            float dl[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int cc = 0; cc < 8; ++cc) {
+                const float w = corner_weight(p, cc);
+                const float2 v = make_float2(w * gx.x, w * gx.y);
+                const bool shared = corner_shared(aligned, delta, cc, d);
+                if (shared) centre_add(acc, delta, cc, d, v);
+                else if (live && dt) atomicAdd(dt + off + corner_index(P.lay, l, p, cc), v);
+                if (GROUP == kCurv && live) {
+                    // positional derivative of the interpolation (d w / d frac)
+                    const float2 tv = shared ? centre_value(vc, delta, cc, d)
+                                             : load_entry(P.table, P.tdtype, off + corner_index(P.lay, l, p, cc));
+                    const float gv = gx.x * tv.x + gx.y * tv.y;
+#pragma unroll
+                    for (int dd = 0; dd < 3; ++dd) {
+                        float wd = 1.f;
+#pragma unroll
+                        for (int kk = 0; kk < 3; ++kk)
+                            if (kk != dd) wd *= (cc >> kk) & 1 ? p.f[kk] : 1.f - p.f[kk];
+                        dl[dd] += ((cc >> dd) & 1 ? wd : -wd) * gv;
+                    }
+                }
+            }
+            if (GROUP == kCurv) {
+#pragma unroll
+                for (int dd = 0; dd < 3; ++dd)
+                    if ((m >> dd) & 1) dsh[dd] += sc * dl[dd];
+            }
+        }
+    }
+    if (dt) {
+        const bool coarse = P.lay.resolutions[l] <= kAggregateRes;
+#pragma unroll
+        for (int cc = 0; cc < 8; ++cc) {
+            const uint64_t ent = off + corner_index(P.lay, l, pc, cc);
+            const bool nz = valid && (acc[cc].x != 0.f || acc[cc].y != 0.f);
+            if (coarse) aggregated_add2<1>(dt, ent, acc[cc].x, acc[cc].y, nz);
+            else if (nz) atomicAdd(dt + ent, acc[cc]);
+        }
+    }
+    if (GROUP == kCurv && valid) {
+        const float inv2r = 1.0f / __fsub_rn(r, -r);
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd)
+            if (dsh[dd] != 0.f) atomicAdd(P.bstate + s * kBState + dd, dsh[dd] * inv2r);
     }
 }
 
@@ -842,6 +1101,13 @@ extern "C" int angelo_sdf_net_layout_query(int32_t n_levels, int32_t n_hidden, i
                    n_levels);
     ANGELO_REQUIRE(n_hidden == 1 || n_hidden == 2, "sdf_net_layout: %d hidden layers", n_hidden);
     ANGELO_REQUIRE(out_dim >= 1 && out_dim <= 72, "sdf_net_layout: feature_dim %d > 72", out_dim);
+    // instantiated shapes: 8 levels / 1 hidden layer / 9..16 outputs and
+    // 16 levels / 2 hidden layers / 65..72 outputs
+    const int nt3 = (out_dim + 7) / 8;
+    ANGELO_REQUIRE((n_levels == 8 && n_hidden == 1 && nt3 == 2) || (n_levels == 16 && n_hidden == 2 && nt3 == 9),
+                   "sdf_net_layout: (%d levels, %d hidden, %d outputs) has no fused kernel "
+                   "(8/1/9..16 or 16/2/65..72)",
+                   n_levels, n_hidden, out_dim);
     angelo_sdf_net_layout L{};
     L.k_tiles1 = 1 + 2 * n_levels / 16;
     L.n_hidden = n_hidden;
@@ -881,38 +1147,126 @@ extern "C" int angelo_sdf_prep(const angelo_sdf_net_layout *lay, int32_t n_level
     return check_launch("sdf_prep");
 }
 
+
 namespace {
-template <int KH, int NH, int NT3>
-int launch_fwd(const SdfParams &P, cudaStream_t s) {
-    const int64_t fwd_bytes = P.nl.off_w1b;
-    const int64_t bias_bytes = ((P.nl.bytes - P.nl.off_b1 + 15) / 16) * 16;
-    const size_t smem = fwd_bytes + bias_bytes + kWarps * sizeof(WarpScratch);
-    auto k = sdf_fwd_kernel<KH, NH, NT3>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return check_launch("sdf_fwd(smem attribute)");
+
+constexpr int kSmallKH = 1, kSmallNH = 1, kSmallNT3 = 2;   // 8 levels, 1 hidden layer, 13 outputs
+constexpr int kFullKH = 2, kFullNH = 2, kFullNT3 = 9;      // 16 levels, 2 hidden layers, 65 outputs
+
+int sm_count() {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem);
-    const int64_t tiles = (P.S + 15) / 16;
-    const int64_t want = (tiles + kWarps - 1) / kWarps;
-    const int grid = (int)std::min<int64_t>(want, (int64_t)sms * std::max(per_sm, 1));
-    k<<<grid, kThreads, smem, s>>>(P);
-    return check_launch("sdf_fwd");
+    return std::max(sms, 1);
 }
 
-template <int KH, int NH>
-int dispatch_nt3(const SdfParams &P, cudaStream_t s) {
-    switch (P.nl.n_tiles3) {
-        case 2: return launch_fwd<KH, NH, 2>(P, s);
-        case 9: return launch_fwd<KH, NH, 9>(P, s);
-        default:
-            set_error("sdf_fwd: output width %d not instantiated (13 or 65 supported)", P.nl.out_dim);
-            return ANGELO_E_UNSUPPORTED;
-    }
+template <int GROUP>
+int launch_encode(const SdfParams &P, cudaStream_t s) {
+    if (P.active == 0) return ANGELO_OK;
+    const dim3 grid((unsigned)((P.S + kEncThreads - 1) / kEncThreads), (unsigned)P.active);
+    stencil_encode_kernel<GROUP><<<grid, kEncThreads, 0, s>>>(P);
+    return check_launch("sdf_stencil_encode");
 }
+
+template <int GROUP>
+int launch_scatter(const SdfParams &P, cudaStream_t s) {
+    if (P.active == 0 || (GROUP != kCurv && P.d_table == nullptr)) return ANGELO_OK;
+    const dim3 grid((unsigned)((P.S + kEncThreads - 1) / kEncThreads), (unsigned)P.active);
+    stencil_scatter_kernel<GROUP><<<grid, kEncThreads, 0, s>>>(P);
+    return check_launch("sdf_stencil_scatter");
+}
+
+template <typename K>
+int persistent_grid(K k, size_t smem, const SdfParams &P, const char *what, int *grid) {
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+        return check_launch(what);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem);
+    if (per_sm < 1) {
+        set_error("%s: %zu bytes of shared memory do not fit an SM", what, smem);
+        return ANGELO_E_UNSUPPORTED;
+    }
+    const int64_t tiles = (P.S + 15) / 16;
+    const int64_t want = (tiles + kWarps - 1) / kWarps;
+    *grid = (int)std::min<int64_t>(want, (int64_t)sm_count() * per_sm);
+    return ANGELO_OK;
+}
+
+template <int KH, int NH, int NT3, int GROUP>
+int launch_mlp_fwd(const SdfParams &P, cudaStream_t s) {
+    const int64_t fwd_bytes = P.nl.off_w1b;
+    const int64_t bias_bytes = ((P.nl.bytes - P.nl.off_b1 + 15) / 16) * 16;
+    const size_t smem = fwd_bytes + bias_bytes + kWarps * sizeof(FwdWarp);
+    auto k = sdf_mlp_fwd_kernel<KH, NH, NT3, GROUP>;
+    int grid = 0;
+    const int rc = persistent_grid(k, smem, P, "sdf_mlp_fwd", &grid);
+    if (rc != ANGELO_OK) return rc;
+    k<<<grid, kThreads, smem, s>>>(P);
+    return check_launch("sdf_mlp_fwd");
+}
+
+template <int KH, int NH, int NT3, int GROUP>
+int launch_mlp_bwd(const SdfParams &P, cudaStream_t s) {
+    const size_t smem = BwdShape<KH, NH, NT3>::bytes;
+    auto k = sdf_mlp_bwd_kernel<KH, NH, NT3, GROUP>;
+    int grid = 0;
+    const int rc = persistent_grid(k, smem, P, "sdf_mlp_bwd", &grid);
+    if (rc != ANGELO_OK) return rc;
+    k<<<grid, kThreads, smem, s>>>(P);
+    return check_launch("sdf_mlp_bwd");
+}
+
+template <int KH, int NH, int NT3>
+int run_fwd(const SdfParams &P, cudaStream_t s) {
+    int rc;
+    if (P.with_grad) {
+        if ((rc = launch_encode<kFD>(P, s)) != ANGELO_OK) return rc;
+        if ((rc = launch_mlp_fwd<KH, NH, NT3, kFD>(P, s)) != ANGELO_OK) return rc;
+    } else {
+        if ((rc = launch_encode<kPoint>(P, s)) != ANGELO_OK) return rc;
+        if ((rc = launch_mlp_fwd<KH, NH, NT3, kPoint>(P, s)) != ANGELO_OK) return rc;
+    }
+    if (P.with_laplace) {
+        if ((rc = launch_encode<kCurv>(P, s)) != ANGELO_OK) return rc;
+        if ((rc = launch_mlp_fwd<KH, NH, NT3, kCurv>(P, s)) != ANGELO_OK) return rc;
+    }
+    return ANGELO_OK;
+}
+
+template <int KH, int NH, int NT3>
+int run_bwd(const SdfParams &P, cudaStream_t s) {
+    int rc;
+    if (P.with_laplace) {
+        if ((rc = launch_mlp_bwd<KH, NH, NT3, kCurv>(P, s)) != ANGELO_OK) return rc;
+        if ((rc = launch_scatter<kCurv>(P, s)) != ANGELO_OK) return rc;
+    }
+    if (P.with_grad) {
+        if ((rc = launch_mlp_bwd<KH, NH, NT3, kFD>(P, s)) != ANGELO_OK) return rc;
+        return launch_scatter<kFD>(P, s);
+    }
+    if ((rc = launch_mlp_bwd<KH, NH, NT3, kPoint>(P, s)) != ANGELO_OK) return rc;
+    return launch_scatter<kPoint>(P, s);
+}
+
+// The two instantiated network shapes; the layout query accepts only these.
+bool shape_small(const angelo_sdf_net_layout &nl) {
+    return nl.k_tiles1 == kSmallKH + 1 && nl.n_hidden == kSmallNH && nl.n_tiles3 == kSmallNT3;
+}
+bool shape_full(const angelo_sdf_net_layout &nl) {
+    return nl.k_tiles1 == kFullKH + 1 && nl.n_hidden == kFullNH && nl.n_tiles3 == kFullNT3;
+}
+
+int64_t n_evals(int with_grad, int with_laplace) { return with_laplace ? 13 : (with_grad ? 7 : 1); }
+
 }  // namespace
+
+extern "C" int64_t angelo_sdf_workspace_floats(const angelo_hashgrid_layout_t *lay, int64_t n,
+                                               int32_t with_grad, int32_t with_laplace,
+                                               int32_t backward) {
+    if (lay == nullptr || n < 0 || lay->n_levels < 1 || lay->n_levels > ANGELO_MAX_LEVELS) return -1;
+    const int64_t x = 2 * n_evals(with_grad, with_laplace) * lay->n_levels * n;
+    return x + (backward ? kBState : kState) * n;
+}
 
 extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32_t active_levels,
                                       const void *table, int32_t table_dtype,
@@ -921,20 +1275,20 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
                                       float radius, float eps, int32_t with_grad,
                                       int32_t with_laplace, int32_t with_feature, float *sdf,
                                       float *grad, float *feature, int64_t feat_stride,
-                                      float *laplace, float *stash_x, float *stash_s, void *stream) {
+                                      float *laplace, float *workspace, void *stream) {
     ANGELO_REQUIRE(lay && nl && net && table, "sdf_stencil_fwd: null argument");
     ANGELO_REQUIRE(n >= 0, "sdf_stencil_fwd: negative n");
     if (n == 0) return ANGELO_OK;
     ANGELO_REQUIRE(lay->n_levels == 8 * (nl->k_tiles1 - 1), "sdf_stencil_fwd: levels vs net");
     ANGELO_REQUIRE(active_levels >= 0 && active_levels <= lay->n_levels, "sdf_stencil_fwd: active");
-    ANGELO_REQUIRE(pos && sdf, "sdf_stencil_fwd: null pos/sdf");
+    ANGELO_REQUIRE(pos && sdf && workspace, "sdf_stencil_fwd: null pos/sdf/workspace");
     ANGELO_REQUIRE(!with_laplace || with_grad, "sdf_stencil_fwd: laplace needs the gradient");
     ANGELO_REQUIRE(!with_grad || grad, "sdf_stencil_fwd: null grad");
     ANGELO_REQUIRE(!with_laplace || (laplace && rand_dirs), "sdf_stencil_fwd: null laplace/rand");
     ANGELO_REQUIRE(!with_feature || (feature && feat_stride >= nl->out_dim + 3),
                    "sdf_stencil_fwd: bad feature output");
-    ANGELO_REQUIRE((stash_x == nullptr) == (stash_s == nullptr), "sdf_stencil_fwd: stash pair");
     ANGELO_REQUIRE(eps > 0.f && radius > 0.f, "sdf_stencil_fwd: eps/radius");
+    ANGELO_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 7) == 0, "sdf_stencil_fwd: workspace alignment");
     SdfParams P{};
     P.lay = *lay;
     P.active = active_levels;
@@ -955,51 +1309,14 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
     P.feature = feature;
     P.feat_stride = feat_stride;
     P.laplace = laplace;
-    P.stash_x = stash_x;
-    P.stash_s = stash_s;
+    P.X = reinterpret_cast<float2 *>(workspace);
+    P.state = workspace + 2 * n_evals(with_grad, with_laplace) * lay->n_levels * n;
     cudaStream_t s = as_stream(stream);
-    if (nl->k_tiles1 == 3) {
-        return nl->n_hidden == 2 ? dispatch_nt3<2, 2>(P, s) : dispatch_nt3<2, 1>(P, s);
-    }
-    return nl->n_hidden == 2 ? dispatch_nt3<1, 2>(P, s) : dispatch_nt3<1, 1>(P, s);
+    if (shape_full(*nl)) return run_fwd<kFullKH, kFullNH, kFullNT3>(P, s);
+    if (shape_small(*nl)) return run_fwd<kSmallKH, kSmallNH, kSmallNT3>(P, s);
+    set_error("sdf_stencil_fwd: network shape not instantiated");
+    return ANGELO_E_UNSUPPORTED;
 }
-
-namespace {
-template <int KH, int NH, int NT3>
-int launch_bwd(const SdfParams &P, cudaStream_t s) {
-    const int k1cols = 16 * P.nl.k_tiles1, outp = 16 * P.nl.k_tiles3b;
-    const int n_acc = 64 * k1cols + 64 * 64 + outp * 64 + 64 + 64 + outp;
-    const size_t smem = P.nl.bytes + ((n_acc + 3) / 4) * 16 + kWarps * sizeof(WarpScratch);
-    auto k = sdf_bwd_kernel<KH, NH, NT3>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return check_launch("sdf_bwd(smem attribute)");
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem);
-    if (per_sm < 1) {
-        set_error("sdf_bwd: %zu bytes of shared memory do not fit an SM", smem);
-        return ANGELO_E_UNSUPPORTED;
-    }
-    const int64_t tiles = (P.S + 15) / 16;
-    const int64_t want = (tiles + kWarps - 1) / kWarps;
-    const int grid = (int)std::min<int64_t>(want, (int64_t)sms * per_sm);
-    k<<<grid, kThreads, smem, s>>>(P);
-    return check_launch("sdf_bwd");
-}
-
-template <int KH, int NH>
-int dispatch_bwd(const SdfParams &P, cudaStream_t s) {
-    switch (P.nl.n_tiles3) {
-        case 2: return launch_bwd<KH, NH, 2>(P, s);
-        case 9: return launch_bwd<KH, NH, 9>(P, s);
-        default:
-            set_error("sdf_bwd: output width %d not instantiated (13 or 65 supported)", P.nl.out_dim);
-            return ANGELO_E_UNSUPPORTED;
-    }
-}
-}  // namespace
 
 extern "C" int64_t angelo_sdf_grad_size(const angelo_sdf_net_layout *nl) {
     const int k1cols = 16 * nl->k_tiles1, outp = 16 * nl->k_tiles3b;
@@ -1011,18 +1328,23 @@ extern "C" int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32
                                       const angelo_sdf_net_layout *nl, const void *net,
                                       const float *pos, const float *rand_dirs, int64_t n,
                                       float radius, float eps, int32_t with_grad,
-                                      int32_t with_laplace, const float *stash_x,
-                                      const float *stash_s, const float *g_sdf,
+                                      int32_t with_laplace, const float *workspace,
+                                      float *bwd_workspace, const float *g_sdf,
                                       const float *g_grad, const float *g_feature,
                                       int64_t gfeat_stride, const float *g_laplace,
                                       float *d_table, float *d_net, void *stream) {
-    ANGELO_REQUIRE(lay && nl && net && table && pos && stash_x && stash_s && d_net,
+    ANGELO_REQUIRE(lay && nl && net && table && pos && workspace && bwd_workspace && d_net,
                    "sdf_stencil_bwd: null argument");
     ANGELO_REQUIRE(n >= 0, "sdf_stencil_bwd: negative n");
     if (n == 0) return ANGELO_OK;
     ANGELO_REQUIRE(lay->n_levels == 8 * (nl->k_tiles1 - 1), "sdf_stencil_bwd: levels vs net");
+    ANGELO_REQUIRE(active_levels >= 0 && active_levels <= lay->n_levels, "sdf_stencil_bwd: active");
     ANGELO_REQUIRE(!with_laplace || (with_grad && rand_dirs), "sdf_stencil_bwd: laplace inputs");
     ANGELO_REQUIRE(g_feature == nullptr || gfeat_stride >= nl->out_dim, "sdf_stencil_bwd: stride");
+    ANGELO_REQUIRE(eps > 0.f && radius > 0.f, "sdf_stencil_bwd: eps/radius");
+    ANGELO_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 7) == 0 &&
+                       (reinterpret_cast<uintptr_t>(bwd_workspace) & 7) == 0,
+                   "sdf_stencil_bwd: workspace alignment");
     SdfParams P{};
     P.lay = *lay;
     P.active = active_levels;
@@ -1037,8 +1359,11 @@ extern "C" int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32
     P.eps = eps;
     P.with_grad = with_grad;
     P.with_laplace = with_laplace;
-    P.stash_x = const_cast<float *>(stash_x);
-    P.stash_s = const_cast<float *>(stash_s);
+    const int64_t x = 2 * n_evals(with_grad, with_laplace) * lay->n_levels * n;
+    P.X = reinterpret_cast<float2 *>(const_cast<float *>(workspace));
+    P.state = const_cast<float *>(workspace) + x;
+    P.dX = reinterpret_cast<float2 *>(bwd_workspace);
+    P.bstate = bwd_workspace + x;
     P.g_sdf = g_sdf;
     P.g_grad = g_grad;
     P.g_feature = g_feature;
@@ -1047,6 +1372,8 @@ extern "C" int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32
     P.d_table = d_table;
     P.d_net = d_net;
     cudaStream_t s = as_stream(stream);
-    if (nl->k_tiles1 == 3) return nl->n_hidden == 2 ? dispatch_bwd<2, 2>(P, s) : dispatch_bwd<2, 1>(P, s);
-    return nl->n_hidden == 2 ? dispatch_bwd<1, 2>(P, s) : dispatch_bwd<1, 1>(P, s);
+    if (shape_full(*nl)) return run_bwd<kFullKH, kFullNH, kFullNT3>(P, s);
+    if (shape_small(*nl)) return run_bwd<kSmallKH, kSmallNH, kSmallNT3>(P, s);
+    set_error("sdf_stencil_bwd: network shape not instantiated");
+    return ANGELO_E_UNSUPPORTED;
 }
