@@ -256,6 +256,33 @@ int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32_t active_l
                            const float *g_grad, const float *g_feature, int64_t gfeat_stride,
                            const float *g_laplace, float *d_table, float *d_net, void *stream);
 
+/* ------------------------------------------------- tensor-core building block */
+
+/* D (128 x N, fp32, row-major) = A (128 x K) * B (N x K)^T on the 5th-
+ * generation tensor cores (tcgen05.mma, operands in shared memory, fp32
+ * accumulation in tensor memory) with both operands split into bf16 hi/lo
+ * (three products).  a_mn_major / b_mn_major stage the operand MN-major
+ * (0: K-major); variant 0 is the descriptor convention the fused kernels use,
+ * 1 exchanges the descriptor's two core-matrix strides (a layout self-check).
+ * N in 16..256 (multiple of 16), K in 16..64 (multiple of 16).  *status
+ * (zeroed by the caller) becomes 1 if the completion wait timed out.  No
+ * counterpart in the reference: it pins the layouts the fused MLP kernels
+ * rely on. */
+int angelo_tc_gemm_x3(const float *A, const float *B, float *D, int32_t N, int32_t K,
+                      int32_t a_mn_major, int32_t b_mn_major, int32_t variant, int32_t *status,
+                      void *stream);
+
+/* ------------------------------------------------------------------- AdamW */
+
+/* One AdamW step of a float32 parameter tensor of n elements, in place
+ * (replaces torch.optim.AdamW.step for the groups systems/utils.py:314-325
+ * builds): p -= lr*wd*p; m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2;
+ * p -= (lr/bc1) m / (sqrt(v)/sqrt(bc2) + eps).  bias_correction1/2 =
+ * 1 - beta^step, computed by the caller. */
+int angelo_adamw_step(float *param, const float *grad, float *exp_avg, float *exp_avg_sq, int64_t n,
+                      float lr, float beta1, float beta2, float eps, float weight_decay,
+                      float bias_correction1, float bias_correction2, void *stream);
+
 /* ----------------------------------------------------- fused radiance network */
 
 /* Bytes of the prepared radiance-MLP buffer for a feature input of feat_dim

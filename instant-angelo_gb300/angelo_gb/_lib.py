@@ -93,6 +93,9 @@ SIGNATURES = {
     "angelo_sdf_stencil_bwd": (c_i32, [_P(HashGridLayout), c_i32, c_vp, c_i32, _P(SdfNetLayout),
                                        c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_i32, c_i32, c_vp,
                                        c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_tc_gemm_x3": (c_i32, [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp]),
+    "angelo_adamw_step": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_f32, c_f32, c_f32,
+                                  c_f32, c_f32, c_vp]),
     "angelo_radiance_net_bytes": (c_i64, [c_i32]),
     "angelo_radiance_grad_size": (c_i64, [c_i32]),
     "angelo_radiance_prep": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),

@@ -9,6 +9,7 @@ import torch
 import torch.nn.functional as F
 
 from .config import scheduled_value, to_config
+from .optim import AdamW
 
 
 def loss_terms(out, rgb, eikonal_weight=0.1, curvature_weight=5e-4, rgb_mse_weight=10.0):
@@ -29,7 +30,8 @@ def loss_terms(out, rgb, eikonal_weight=0.1, curvature_weight=5e-4, rgb_mse_weig
 class NeuSTrainer:
     """One training step = update_step (band mask, FD eps, cosine anneal,
     occupancy refresh every 16 steps) -> forward -> losses -> backward ->
-    AdamW.  Ray counts follow the reference's dynamic sampling rule."""
+    AdamW (angelo_gb.optim, one native pass per parameter).  Ray counts follow
+    the reference's dynamic sampling rule."""
 
     def __init__(self, model, system_config=None, train_num_rays=256, max_train_num_rays=8192,
                  train_num_samples=1 << 18, dynamic_ray_sampling=True):
@@ -48,8 +50,7 @@ class NeuSTrainer:
             params = list(mod.parameters()) if isinstance(mod, torch.nn.Module) else [mod]
             groups.append({"params": params, "name": name, **a})
         args["betas"] = tuple(args.get("betas", (0.9, 0.99)))
-        fused = all(p.is_cuda for g in groups for p in g["params"])
-        self.optimizer = torch.optim.AdamW(groups, fused=fused, **args)
+        self.optimizer = AdamW(groups, **args)
         self.train_num_rays = int(train_num_rays)
         self.max_train_num_rays = int(max_train_num_rays)
         self.train_num_samples = int(train_num_samples)

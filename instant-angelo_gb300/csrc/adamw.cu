@@ -1,0 +1,111 @@
+// AdamW step of the reference's optimizer (systems/utils.py:314-325 builds
+// torch.optim.AdamW(lr, betas, eps) per parameter group) as one streaming
+// pass per parameter tensor: read param, grad, first and second moment, write
+// param and both moments (28 bytes per fp32 parameter, HBM-bound).
+//
+// The update is decoupled weight decay followed by the Adam step (Loshchilov
+// and Hutter, "Decoupled Weight Decay Regularization", algorithm 2):
+//   p   <- p - lr * wd * p
+//   m   <- m + (1 - beta1) (g - m)          (= beta1 m + (1 - beta1) g)
+//   v   <- beta2 v + (1 - beta2) g^2
+//   p   <- p - (lr / bc1) * m / (sqrt(v) / sqrt(bc2) + eps)
+// with bc1 = 1 - beta1^t, bc2 = 1 - beta2^t computed on the host per step.
+// The first moment uses the interpolation form of torch.optim.AdamW's
+// default CUDA path (foreach lerp); all arithmetic is fp32.
+#include <algorithm>
+
+#include "common.cuh"
+
+using namespace angelo;
+
+namespace {
+
+struct AdamArgs {
+    float lr, beta1, beta2, eps, wd;
+    float step_size;       // lr / bc1
+    float bc2_sqrt;        // sqrt(bc2)
+};
+
+__device__ __forceinline__ void adamw_one(float &p, float g, float &m, float &v, const AdamArgs &a) {
+    p = p - a.lr * a.wd * p;
+    m = m + (1.0f - a.beta1) * (g - m);
+    v = a.beta2 * v + (1.0f - a.beta2) * g * g;
+    const float denom = sqrtf(v) / a.bc2_sqrt + a.eps;
+    p = p - a.step_size * m / denom;
+}
+
+__global__ void adamw_vec4_kernel(float4 *__restrict__ p, const float4 *__restrict__ g,
+                                  float4 *__restrict__ m, float4 *__restrict__ v, int64_t n4,
+                                  AdamArgs a) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float4 pp = p[i], mm = m[i], vv = v[i];
+        const float4 gg = __ldcs(g + i);
+        adamw_one(pp.x, gg.x, mm.x, vv.x, a);
+        adamw_one(pp.y, gg.y, mm.y, vv.y, a);
+        adamw_one(pp.z, gg.z, mm.z, vv.z, a);
+        adamw_one(pp.w, gg.w, mm.w, vv.w, a);
+        p[i] = pp;
+        m[i] = mm;
+        v[i] = vv;
+    }
+}
+
+__global__ void adamw_scalar_kernel(float *__restrict__ p, const float *__restrict__ g,
+                                    float *__restrict__ m, float *__restrict__ v, int64_t n,
+                                    AdamArgs a) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        float pp = p[i], mm = m[i], vv = v[i];
+        adamw_one(pp, g[i], mm, vv, a);
+        p[i] = pp;
+        m[i] = mm;
+        v[i] = vv;
+    }
+}
+
+bool aligned16(const void *x) { return (reinterpret_cast<uintptr_t>(x) & 15) == 0; }
+
+}  // namespace
+
+extern "C" int angelo_adamw_step(float *param, const float *grad, float *exp_avg, float *exp_avg_sq,
+                                 int64_t n, float lr, float beta1, float beta2, float eps,
+                                 float weight_decay, float bias_correction1,
+                                 float bias_correction2, void *stream) {
+    ANGELO_REQUIRE(n >= 0, "adamw_step: negative n");
+    if (n == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(param && grad && exp_avg && exp_avg_sq, "adamw_step: null pointer");
+    ANGELO_REQUIRE(bias_correction1 > 0.f && bias_correction2 > 0.f, "adamw_step: bias corrections");
+    AdamArgs a;
+    a.lr = lr;
+    a.beta1 = beta1;
+    a.beta2 = beta2;
+    a.eps = eps;
+    a.wd = weight_decay;
+    a.step_size = lr / bias_correction1;
+    a.bc2_sqrt = sqrtf(bias_correction2);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaStream_t s = as_stream(stream);
+    const int threads = 256;
+    const int64_t cap = (int64_t)std::max(sms, 1) * 8;   // 8 CTAs of 256 per SM, grid-stride
+    int64_t head = 0;
+    if (aligned16(param) && aligned16(grad) && aligned16(exp_avg) && aligned16(exp_avg_sq)) {
+        const int64_t n4 = n / 4;
+        if (n4 > 0) {
+            const int64_t blocks = std::min<int64_t>((n4 + threads - 1) / threads, cap);
+            adamw_vec4_kernel<<<(unsigned)blocks, threads, 0, s>>>(
+                reinterpret_cast<float4 *>(param), reinterpret_cast<const float4 *>(grad),
+                reinterpret_cast<float4 *>(exp_avg), reinterpret_cast<float4 *>(exp_avg_sq), n4, a);
+        }
+        head = n4 * 4;
+    }
+    if (head < n) {
+        const int64_t rest = n - head;
+        const int64_t blocks = std::min<int64_t>((rest + threads - 1) / threads, cap);
+        adamw_scalar_kernel<<<(unsigned)blocks, threads, 0, s>>>(param + head, grad + head, exp_avg + head,
+                                                                exp_avg_sq + head, rest, a);
+    }
+    return check_launch("adamw_step");
+}

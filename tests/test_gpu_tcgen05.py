@@ -1,0 +1,69 @@
+"""The tcgen05 building block of the fused MLP kernels (angelo_tc_gemm_x3):
+D = A B^T with both operands split into bf16 hi/lo in shared memory, the
+three products accumulated in fp32 in tensor memory, against float64.
+K-major operands feed the per-row layer products, MN-major operands the
+weight-gradient products over samples; the layout convention the library
+uses is variant 0 (descriptor LBO = core-matrix stride along K, SBO = along
+M or N, for either major)."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    from angelo_gb import build
+    build.build()
+    return torch.device("cuda:0")
+
+
+def _gemm(dev, N, K, a_mn, b_mn, variant, seed=0):
+    from angelo_gb._lib import call
+    from angelo_gb.ops import _p, _s
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    A = torch.randn(128, K, generator=g).to(dev)
+    B = torch.randn(N, K, generator=g).to(dev)
+    D = torch.full((128, N), float("nan"), device=dev)
+    st = torch.zeros(1, dtype=torch.int32, device=dev)
+    call("angelo_tc_gemm_x3", _p(A), _p(B), _p(D), N, K, a_mn, b_mn, variant, _p(st), _s(dev))
+    torch.cuda.synchronize()
+    ref = A.double() @ B.double().T
+    err = ((D.double() - ref).abs().max() / ref.abs().max()).item()
+    return int(st.item()), err
+
+
+@pytest.mark.parametrize("N,K", [(16, 16), (64, 48), (80, 64), (128, 32), (256, 64)])
+def test_tc_gemm_x3_kmajor(dev, N, K):
+    st, err = _gemm(dev, N, K, 0, 0, 0)
+    assert st == 0, "tensor-core completion wait timed out"
+    # bf16x3 keeps ~2^-16 of each operand; K <= 64 terms
+    assert err < 2e-5, err
+
+
+@pytest.mark.parametrize("N,K", [(16, 16), (64, 32), (112, 16)])
+@pytest.mark.parametrize("a_mn,b_mn", [(1, 1), (1, 0), (0, 1)])
+def test_tc_gemm_x3_mnmajor(dev, N, K, a_mn, b_mn):
+    st, err = _gemm(dev, N, K, a_mn, b_mn, 0)
+    assert st == 0, "tensor-core completion wait timed out"
+    assert err < 2e-5, err
+
+
+def test_tc_layout_variant_report(dev):
+    """Variant 1 exchanges the descriptor's two core-matrix strides; it must
+    not agree with float64 when variant 0 does (the convention is pinned)."""
+    rows = []
+    for a_mn, b_mn in [(0, 0), (1, 1)]:
+        for v in (0, 1):
+            st, err = _gemm(dev, 64, 16, a_mn, b_mn, v, seed=1)
+            rows.append((a_mn, b_mn, v, st, err))
+    print("\n(a_mn, b_mn, variant, status, rel err):", rows)
+    for a_mn, b_mn, v, st, err in rows:
+        assert st == 0
+        if v == 0:
+            assert err < 2e-5
