@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--forms", default="auto", help="comma list of plain,fused (auto: all built)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--sdf-case", type=int, default=0, metavar="N",
                     help="profiling case: 3 fused VolumeSDF training passes (16 levels x 2^22, "
                          "FD + curvature) on N points of the full model, then exit")
@@ -426,6 +427,8 @@ def run_ours(args):
     }
     if "fused" in results and "plain" in results:
         line["fused_vs_plain"] = round(results["fused"]["value"] / results["plain"]["value"], 3)
+    if rank == 0 and not args.no_serving and "fused" in forms:
+        line["serving"] = run_serving(dev, seed=1000 + rank)
     if rank == 0 and not args.no_cpu_baseline:
         model, tr = make_trainer("plain", dev)
         model.update_step(0, GLOBAL_STEP)
@@ -434,6 +437,106 @@ def run_ours(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+# ------------------------------------------------------------------ serving
+
+SERVE_RES = ((256, 256), (512, 512), (800, 600), (1920, 1080))
+SERVE_GRIDS = (64, 128, 256, 512)
+
+
+def serving_requests(n_render, n_grid, rate, seed):
+    """Poisson arrivals (rate per second) of renders with resolutions drawn
+    uniformly from SERVE_RES and random poses on a radius-2.5 sphere,
+    interleaved with SDF grids of SERVE_GRIDS points per axis."""
+    from angelo_gb.scenes import look_at_c2w
+    from angelo_gb.serve import RenderRequest, SdfGridRequest
+    g = np.random.default_rng(seed)
+    reqs = []
+    t = 0.0
+    kinds = ["r"] * n_render + ["g"] * n_grid
+    g.shuffle(kinds)
+    gi = 0
+    for i, k in enumerate(kinds):
+        t += g.exponential(1.0 / rate)
+        if k == "r":
+            v = g.normal(size=3)
+            eye = tuple(2.5 * v / np.linalg.norm(v))
+            W, H = SERVE_RES[g.integers(len(SERVE_RES))]
+            reqs.append(RenderRequest(i, look_at_c2w(eye), int(W), int(H), arrival=t))
+        else:
+            reqs.append(SdfGridRequest(i, SERVE_GRIDS[gi % len(SERVE_GRIDS)], arrival=t))
+            gi += 1
+    return reqs
+
+
+def serving_model(dev, fused):
+    """The small model's architecture (8 levels x 2^16, 1 hidden layer,
+    radiance MLP, near/far 0.5-4.5, 128 samples per ray) with seeded weights:
+    sphere-initialised geometry and a U(-0.05, 0.05) table."""
+    from angelo_gb import models, workloads
+    torch.manual_seed(0)
+    m = models.make("neus", workloads.model_config("small", fused=fused)).to(dev)
+    m.update_step(0, 5000)
+    with torch.no_grad():
+        gen = torch.Generator(device="cpu").manual_seed(7)
+        p = m.geometry.hashgrid.encoding.params
+        p.copy_((torch.rand(p.shape, generator=gen) * 0.1 - 0.05).to(dev))
+    return m.eval()
+
+
+def run_serving(dev, seed, n_render=16, n_grid=4, rate=50.0):
+    """Served Mrays/s and p50/p99 latency of the persistent loop on a Poisson
+    request stream, beside the reference's sequential eval path (plain
+    kernels, one request at a time, 2048-ray chunks moved to the host) timed
+    on the smallest requests of the same stream."""
+    from angelo_gb import serve
+    m = serving_model(dev, fused=True)
+    srv = serve.Server(m, ray_bucket=1 << 14, max_samples_per_ray=128, point_bucket=1 << 21,
+                       hbm_reserve=8 << 30)
+    warm = serving_requests(2, 1, rate, seed + 1)
+    srv.run(warm, realtime=False)
+    reqs = serving_requests(n_render, n_grid, rate, seed)
+    t0 = time.perf_counter()
+    srv.run(reqs, realtime=True)
+    wall = time.perf_counter() - t0
+    renders = [q for q in reqs if isinstance(q, serve.RenderRequest)]
+    grids = [q for q in reqs if isinstance(q, serve.SdfGridRequest)]
+    rays = sum(q.n for q in renders)
+    pts = sum(q.n for q in grids)
+    makespan = max(q.done for q in reqs) - min(q.arrival for q in reqs)
+    p50, p99 = serve.latency_stats(reqs)
+    r50, r99 = serve.latency_stats(renders)
+    out = {"workload": f"small-model field, {n_render} renders {SERVE_RES} + {n_grid} SDF grids "
+                       f"{SERVE_GRIDS[:n_grid]}^3, Poisson {rate}/s, 128 samples/ray",
+           "served_mrays_per_s": round(rays / makespan / 1e6, 3),
+           "served_mpts_per_s_sdf": round(pts / makespan / 1e6, 3),
+           "p50_ms": round(p50, 2), "p99_ms": round(p99, 2),
+           "render_p50_ms": round(r50, 2), "render_p99_ms": round(r99, 2),
+           "rays": rays, "sdf_points": pts, "makespan_s": round(makespan, 3),
+           "wall_s": round(wall, 3), "buckets": srv.buckets, "overflows": srv.overflows}
+    del srv
+    torch.cuda.empty_cache()
+    # the reference's serving path on the two smallest renders and the
+    # smallest grid of the stream
+    plain = serving_model(dev, fused=False)
+    sample = sorted(renders, key=lambda q: q.n)[:2] + sorted(grids, key=lambda q: q.n)[:1]
+    seq = [type(q)(**{k: getattr(q, k) for k in (("rid", "c2w", "W", "H") if isinstance(
+        q, serve.RenderRequest) else ("rid", "res"))}) for q in sample]
+    t0 = time.perf_counter()
+    serve.sequential_plain(plain, seq)
+    t_seq = time.perf_counter() - t0
+    s_rays = sum(q.n for q in seq if isinstance(q, serve.RenderRequest))
+    s_ray_time = sum(q.done - (seq[i - 1].done if i else 0.0) for i, q in enumerate(seq)
+                     if isinstance(q, serve.RenderRequest))
+    out["plain_sequential"] = {
+        "mrays_per_s": round(s_rays / s_ray_time / 1e6, 4),
+        "sample": f"{len(seq)} requests of the stream ({s_rays} rays), back to back",
+        "wall_s": round(t_seq, 3)}
+    out["served_vs_plain"] = round(out["served_mrays_per_s"] / out["plain_sequential"]["mrays_per_s"], 2)
+    del plain
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_reference(args):
