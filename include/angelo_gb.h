@@ -196,6 +196,9 @@ typedef struct {
     int32_t k_tiles1, n_hidden, n_tiles3, k_tiles3b, out_dim;
     int64_t off_w1f, off_w2f, off_w3f, off_w1b, off_w2b, off_w3b;
     int64_t off_b1, off_b2, off_b3, off_w3row0;
+    /* tensor-core (tcgen05) operands: W1 (64 x 16*k_tiles1), W2 (64 x 64),
+     * W3 (16*k_tiles3b x 64) in the K-major core-matrix layout, bf16 hi then lo */
+    int64_t off_tcw1, off_tcw2, off_tcw3;
     int64_t bytes;
 } angelo_sdf_net_layout;
 
@@ -268,6 +271,12 @@ int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32_t active_l
  * (zeroed by the caller) becomes 1 if the completion wait timed out.  No
  * counterpart in the reference: it pins the layouts the fused MLP kernels
  * rely on. */
+/* Number of CTAs of the tensor-core kernels that stopped waiting for an MMA
+ * completion (bounded mbarrier waits) since the last reset; synchronous, -1
+ * on a CUDA error.  A diagnostic counter: the one piece of mutable device
+ * state of the library besides the allocation-free scan's workspace. */
+int64_t angelo_tc_timeouts(int32_t reset);
+
 int angelo_tc_gemm_x3(const float *A, const float *B, float *D, int32_t N, int32_t K,
                       int32_t a_mn_major, int32_t b_mn_major, int32_t variant, int32_t *status,
                       void *stream);

@@ -45,7 +45,8 @@ class SdfNetLayout(ctypes.Structure):
                 ("off_w1f", c_i64), ("off_w2f", c_i64), ("off_w3f", c_i64),
                 ("off_w1b", c_i64), ("off_w2b", c_i64), ("off_w3b", c_i64),
                 ("off_b1", c_i64), ("off_b2", c_i64), ("off_b3", c_i64),
-                ("off_w3row0", c_i64), ("bytes", c_i64)]
+                ("off_w3row0", c_i64), ("off_tcw1", c_i64), ("off_tcw2", c_i64),
+                ("off_tcw3", c_i64), ("bytes", c_i64)]
 
 
 class AngeloError(RuntimeError):
@@ -93,6 +94,7 @@ SIGNATURES = {
     "angelo_sdf_stencil_bwd": (c_i32, [_P(HashGridLayout), c_i32, c_vp, c_i32, _P(SdfNetLayout),
                                        c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_i32, c_i32, c_vp,
                                        c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_tc_timeouts": (c_i64, [c_i32]),
     "angelo_tc_gemm_x3": (c_i32, [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp]),
     "angelo_adamw_step": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_f32, c_f32, c_f32,
                                   c_f32, c_f32, c_vp]),

@@ -35,6 +35,7 @@
 
 #include "common.cuh"
 #include "mlp.cuh"
+#include "tc.cuh"
 
 using namespace angelo;
 
@@ -145,6 +146,33 @@ __global__ void sdf_prep_kernel(const float *__restrict__ W1, const float *__res
     const int64_t idx = (int64_t)(kt * NT + nt) * 32 + lane;
     dst[idx] = make_uint2(s0.hi, s1.hi);
     dst[n_frag + idx] = make_uint2(s0.lo, s1.lo);
+}
+
+// tcgen05 operands of the three layers (Y = X W^T, kernel column order):
+// element (n, k) at kmajor_offset(n, k, K) of the region's hi half, its lo
+// part at the same offset of the lo half.
+__global__ void sdf_prep_tc_kernel(const float *__restrict__ W1, const float *__restrict__ W2,
+                                   const float *__restrict__ W3, int in_dim, int n_hash,
+                                   angelo_sdf_net_layout lay, char *__restrict__ net) {
+    const int K1 = 16 * lay.k_tiles1, N3 = 16 * lay.k_tiles3b;
+    const int n1 = 64 * K1, n2 = lay.n_hidden == 2 ? 64 * 64 : 0, n3 = N3 * 64;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int layer, n, k, K;
+    int64_t off, half;
+    if (i < n1) {
+        layer = 1, K = K1, n = i / K, k = i % K, off = lay.off_tcw1, half = (int64_t)n1 * 2;
+    } else if ((i -= n1) < n2) {
+        layer = 2, K = 64, n = i / 64, k = i % 64, off = lay.off_tcw2, half = (int64_t)n2 * 2;
+    } else if ((i -= n2) < n3) {
+        layer = 3, K = 64, n = i / 64, k = i % 64, off = lay.off_tcw3, half = (int64_t)n3 * 2;
+    } else {
+        return;
+    }
+    const float v = layer_w(layer, n, k, W1, W2, W3, in_dim, n_hash, lay.out_dim);
+    const Split sp = split2(v, 0.0f);
+    const uint32_t o = tc::kmajor_offset(n, k, K);
+    *reinterpret_cast<uint16_t *>(net + off + o) = (uint16_t)(sp.hi & 0xFFFFu);
+    *reinterpret_cast<uint16_t *>(net + off + half + o) = (uint16_t)(sp.lo & 0xFFFFu);
 }
 
 // ----------------------------------------------------------- kernel params
@@ -381,123 +409,260 @@ __device__ __forceinline__ float fd_grad(const float *s6, float eps, float g[3])
 }
 
 // --------------------------------------------------------------- MLP forward
+// tcgen05: a CTA of 16 warps owns 128 consecutive samples through every
+// evaluation of the group.  Row r (sample s0 + r, tensor-memory lane r) is
+// shared by four threads: warp w serves lanes 32 (w % 4) .. + 31 and the
+// 16-column slice w / 4 of every 64-wide layer.  Per evaluation and layer the
+// layer input is staged as a bf16 hi/lo K-major operand (128 rows), one
+// thread issues the three products of each 16-wide K step (lo*hi, hi*lo,
+// hi*hi) into fp32 tensor memory and commits them to an mbarrier, and every
+// thread reads its slice back (bias, softplus, the next layer's operand).
+// Two CTAs per SM overlap one's tensor work with the other's epilogue.
 
-struct FwdWarp {
-    float base[16][3];
-    float s13[16][13];
+__device__ unsigned int g_tc_timeouts;   // CTAs that stopped waiting for the tensor cores
+
+constexpr uint32_t kTcWaitPolls = 1u << 24;
+constexpr int kTcThreads = 512;
+
+template <int KH, int NH, int NT3>
+struct TcFwdShape {
+    static constexpr int K1 = 16 * (KH + 1);
+    static constexpr int N3 = 16 * ((NT3 + 1) / 2);
+    // bytes of one (hi or lo) half of each operand
+    static constexpr uint32_t w1 = 64 * K1 * 2, w2 = NH == 2 ? 64 * 64 * 2 : 0, w3 = N3 * 64 * 2;
+    static constexpr uint32_t a1 = 128 * K1 * 2, a2 = 128 * 64 * 2;
+    static constexpr uint32_t off_w1 = 0, off_w2 = off_w1 + 2 * w1, off_w3 = off_w2 + 2 * w2,
+                              off_a1 = off_w3 + 2 * w3, off_a2 = off_a1 + 2 * a1, off_bias = off_a2 + 2 * a2,
+                              off_s13 = off_bias + (128 + N3) * 4, off_bar = off_s13 + 13 * 128 * 4,
+                              bytes = off_bar + 16;
+    static constexpr uint32_t tmem_cols = 256;   // Z1 [0, 64), Z2 [64, 128), output [128, 128 + N3)
 };
 
-template <int KH, int NH, int NT3, int GROUP>
-__global__ void __launch_bounds__(kThreads) sdf_mlp_fwd_kernel(const __grid_constant__ SdfParams P) {
-    extern __shared__ __align__(16) char smem[];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const angelo_sdf_net_layout &nl = P.nl;
-    const int64_t fwd_bytes = nl.off_w1b;  // forward fragments come first
-    const int64_t bias_bytes = nl.bytes - nl.off_b1;
-    for (int64_t i = tid * 16; i < fwd_bytes; i += kThreads * 16)
-        *reinterpret_cast<uint4 *>(smem + i) = *reinterpret_cast<const uint4 *>(P.net + i);
-    for (int64_t i = tid * 4; i < bias_bytes; i += kThreads * 4)
-        *reinterpret_cast<float *>(smem + fwd_bytes + i) = *reinterpret_cast<const float *>(P.net + nl.off_b1 + i);
-    FwdWarp *wsa = reinterpret_cast<FwdWarp *>(smem + fwd_bytes + ((bias_bytes + 15) / 16) * 16);
-    FwdWarp &ws = wsa[warp];
+// D (128 x N) = A (128 x 16 KSTEPS) * B (N x 16 KSTEPS)^T in bf16x3, one thread
+template <int KSTEPS>
+__device__ __forceinline__ void tc_layer(uint32_t d_tmem, uint32_t a_hi, uint32_t a_lo, uint32_t a_sbo,
+                                         uint32_t b_hi, uint32_t b_lo, uint32_t b_sbo, uint32_t idesc) {
+#pragma unroll
+    for (int ks = 0; ks < KSTEPS; ++ks) {
+        const uint32_t o = ks * 256;
+        const uint64_t ah = tc::smem_desc(a_hi + o, 128, a_sbo), al = tc::smem_desc(a_lo + o, 128, a_sbo);
+        const uint64_t bh = tc::smem_desc(b_hi + o, 128, b_sbo), bl = tc::smem_desc(b_lo + o, 128, b_sbo);
+        tc::mma_bf16(d_tmem, al, bh, idesc, ks > 0 ? 1u : 0u);
+        tc::mma_bf16(d_tmem, ah, bl, idesc, 1u);
+        tc::mma_bf16(d_tmem, ah, bh, idesc, 1u);
+    }
+}
+
+// Every thread waits for the mbarrier phase; false (the same in every thread)
+// when some thread gave up.
+__device__ __forceinline__ bool tc_wait_all(uint64_t *bar, uint32_t phase) {
+    const bool ok = tc::mbar_wait(bar, phase, kTcWaitPolls);
+    const int failed = __syncthreads_or(!ok);
+    tc::fence_after_sync();
+    return failed == 0;
+}
+
+// Operand writes of every thread visible to the tensor cores, then thread 0
+// may issue (after this, all threads have also finished their tensor-memory
+// reads of the previous phase).
+__device__ __forceinline__ void tc_publish() {
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
     __syncthreads();
-    NetSmem net;
-    net.w1f = reinterpret_cast<const uint2 *>(smem + nl.off_w1f);
-    net.w2f = reinterpret_cast<const uint2 *>(smem + nl.off_w2f);
-    net.w3f = reinterpret_cast<const uint2 *>(smem + nl.off_w3f);
-    net.b1 = reinterpret_cast<const float *>(smem + fwd_bytes);
-    net.b2 = reinterpret_cast<const float *>(smem + fwd_bytes + (nl.off_b2 - nl.off_b1));
-    net.b3 = reinterpret_cast<const float *>(smem + fwd_bytes + (nl.off_b3 - nl.off_b1));
+    tc::fence_after_sync();
+}
+
+// 16 consecutive columns c0 .. c0 + 15 (c0 % 16 == 0) of row r of a K-major
+// operand with K columns, split into bf16 hi and lo
+__device__ __forceinline__ void stage16(char *hi, char *lo, int r, int c0, int K, const float (&v)[16]) {
+    uint32_t h[8], l[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const Split sp = split2(v[2 * i], v[2 * i + 1]);
+        h[i] = sp.hi;
+        l[i] = sp.lo;
+    }
+    const uint32_t o0 = tc::kmajor_offset(r, c0, K), o1 = tc::kmajor_offset(r, c0 + 8, K);
+    *reinterpret_cast<uint4 *>(hi + o0) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(hi + o1) = make_uint4(h[4], h[5], h[6], h[7]);
+    *reinterpret_cast<uint4 *>(lo + o0) = make_uint4(l[0], l[1], l[2], l[3]);
+    *reinterpret_cast<uint4 *>(lo + o1) = make_uint4(l[4], l[5], l[6], l[7]);
+}
+
+template <int KH, int NH, int NT3, int GROUP>
+__global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid_constant__ SdfParams P) {
+    using Sh = TcFwdShape<KH, NH, NT3>;
+    constexpr int K1 = Sh::K1, N3 = Sh::N3;
+    extern __shared__ __align__(1024) char smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int row = (warp & 3) * 32 + lane, slice = warp >> 2;   // row of the tile, 16-column slice
+    const angelo_sdf_net_layout &nl = P.nl;
+    auto copy16 = [&](uint32_t dst, int64_t src, uint32_t bytes) {
+        for (uint32_t i = tid * 16; i < bytes; i += kTcThreads * 16)
+            *reinterpret_cast<uint4 *>(smem + dst + i) = *reinterpret_cast<const uint4 *>(P.net + src + i);
+    };
+    copy16(Sh::off_w1, nl.off_tcw1, 2 * Sh::w1);
+    if (NH == 2) copy16(Sh::off_w2, nl.off_tcw2, 2 * Sh::w2);
+    copy16(Sh::off_w3, nl.off_tcw3, 2 * Sh::w3);
+    float *bias = reinterpret_cast<float *>(smem + Sh::off_bias);   // b1 [64], b2 [64], b3 [N3]
+    for (int i = tid; i < 128 + N3; i += kTcThreads) {
+        float v = 0.f;
+        if (i < 64) v = reinterpret_cast<const float *>(P.net + nl.off_b1)[i];
+        else if (i < 128) v = NH == 2 ? reinterpret_cast<const float *>(P.net + nl.off_b2)[i - 64] : 0.f;
+        else if (i - 128 < 8 * NT3) v = reinterpret_cast<const float *>(P.net + nl.off_b3)[i - 128];
+        bias[i] = v;
+    }
+    float *s13 = reinterpret_cast<float *>(smem + Sh::off_s13);      // [13][128]
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + Sh::off_bar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
+    char *a1h = smem + Sh::off_a1, *a1l = a1h + Sh::a1, *a2h = smem + Sh::off_a2, *a2l = a2h + Sh::a2;
+    if (warp == 0) {
+        tc::tmem_alloc(slot, Sh::tmem_cols);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) tc::mbar_init(bar, 1);
+    tc_publish();
+    const uint32_t tmem = *slot;
+    const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+    const uint32_t sA1h = tc::smem_addr(a1h), sA1l = tc::smem_addr(a1l);
+    const uint32_t sA2h = tc::smem_addr(a2h), sA2l = tc::smem_addr(a2l);
+    const uint32_t sW1h = tc::smem_addr(smem + Sh::off_w1), sW1l = sW1h + Sh::w1;
+    const uint32_t sW2h = tc::smem_addr(smem + Sh::off_w2), sW2l = sW2h + Sh::w2;
+    const uint32_t sW3h = tc::smem_addr(smem + Sh::off_w3), sW3l = sW3h + Sh::w3;
+    constexpr uint32_t id_hidden = tc::idesc_bf16_f32(128, 64);
+    constexpr uint32_t id_out_main = tc::idesc_bf16_f32(128, N3), id_out_tap = tc::idesc_bf16_f32(128, 16);
 
     constexpr int e0 = GROUP == kCurv ? 7 : 0;
     constexpr int ne = GROUP == kPoint ? 1 : (GROUP == kFD ? 7 : 6);
-    const int g = lane >> 2, q = lane & 3;
     const float r_ = P.radius, eps = P.eps;
-    const int64_t n_tiles = (P.S + 15) / 16;
-    for (int64_t t = (int64_t)blockIdx.x * kWarps + warp; t < n_tiles; t += (int64_t)gridDim.x * kWarps) {
-        const int64_t s0 = t * 16;
-        if (lane < 16) {
-            const int64_t s = s0 + lane;
-            const bool v = s < P.S;
-            const float *src = GROUP == kCurv ? P.state + s * kState + 13 : P.pos + s * 3;
+    const int od = nl.out_dim;
+    uint32_t phase = 0;
+    bool alive = true;
+    // work items k = (tile blockIdx.x + (k / ne) gridDim.x, evaluation e0 + k % ne)
+    const int64_t n_tiles = (P.S + 127) / 128;
+    const int64_t my_tiles = (int64_t)blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t n_items = my_tiles * ne;
+    auto item_sample = [&](int64_t k) { return (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row; };
+    auto item_base = [&](int64_t sk, float b[3]) {
+        const bool vk = sk < P.S;
+        const float *src = GROUP == kCurv ? P.state + sk * kState + 13 : P.pos + sk * 3;
+        for (int d = 0; d < 3; ++d) b[d] = vk ? src[d] : 0.f;
+    };
+    // layer-1 operand of item k: slice q < KH holds hash levels 8q .. 8q + 7,
+    // slice KH the xyz columns
+    auto stage_x = [&](int64_t k) {
+        const int64_t sk = item_sample(k);
+        const int ek = e0 + (int)(k % ne);
+        const bool vk = sk < P.S;
+        if (slice < KH) {
+            float x[16];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) ws.base[lane][d] = v ? src[d] : 0.f;
-            if (GROUP == kCurv)
-                for (int e = 1; e < 7; ++e) ws.s13[lane][e] = v ? P.state[s * kState + e] : 0.f;
-        }
-        __syncwarp();
-        const bool v0 = s0 + g < P.S, v1 = s0 + g + 8 < P.S;
-#pragma unroll 1
-        for (int i = 0; i < ne; ++i) {
-            const int e = e0 + i;
-            float xc0[3], xc1[3];
-            int m0, m1;
-            tap_point(r_, eps, ws.base[g], e, xc0, &m0);
-            tap_point(r_, eps, ws.base[g + 8], e, xc1, &m1);
-            AFrag<KH> A;
-            load_x<KH>(P, e, s0, v0, v1, lane, xc0, xc1, A);
-            uint32_t hh[4][4], hl[4][4];
-            {
-                float Z[8][4];
-                hidden_layer<KH + 1>(A.hi, A.lo, net.w1f, net.b1, lane, Z);
-                activate(Z, hh, hl);
-                if (NH == 2) {
-                    hidden_layer<4>(hh, hl, net.w2f, net.b2, lane, Z);
-                    activate(Z, hh, hl);
-                }
+            for (int j = 0; j < 8; ++j) {
+                const int l = 8 * slice + j;
+                const float2 f = (vk && l < P.active) ? __ldg(P.X + xidx(P, ek, l, sk)) : make_float2(0.f, 0.f);
+                x[2 * j] = f.x;
+                x[2 * j + 1] = f.y;
             }
+            stage16(a1h, a1l, row, 16 * slice, K1, x);
+        } else if (slice == KH) {
+            float b[3], xc[3], x[16];
+            int m;
+            item_base(sk, b);
+            tap_point(r_, eps, b, ek, xc, &m);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) x[j] = 0.f;
+            x[0] = x2m1(xc[0]);
+            x[1] = x2m1(xc[1]);
+            x[2] = x2m1(xc[2]);
+            stage16(a1h, a1l, row, 16 * KH, K1, x);
+        }
+    };
+    if (n_items > 0) stage_x(0);
+    for (int64_t k = 0; k < n_items && alive; ++k) {
+        const int64_t s = item_sample(k);
+        const bool v = s < P.S;
+        const int i = (int)(k % ne), e = e0 + i;
+        float base[3], xc[3];
+        int m;
+        item_base(s, base);
+        tap_point(r_, eps, base, e, xc, &m);
+        {
+            tc_publish();
+            if (tid == 0) {
+                tc_layer<K1 / 16>(tmem, sA1h, sA1l, 16 * K1, sW1h, sW1l, 16 * K1, id_hidden);
+                tc::commit(bar);
+            }
+            if (!(alive = tc_wait_all(bar, phase))) break;
+            phase ^= 1;
+            // the layer-1 operand is free: stage the next item's, whose loads
+            // overlap this item's remaining layers
+            if (k + 1 < n_items) stage_x(k + 1);
+            // hidden layers: bias, softplus, next operand
+#pragma unroll
+            for (int layer = 0; layer < NH; ++layer) {
+                const uint32_t zcol = 64 * layer;
+                {
+                    float z[16];
+                    tc::ld16(tmem + lane_off + zcol + 16 * slice, z);
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) z[j] = softplus100(z[j] + bias[64 * layer + 16 * slice + j]);
+                    stage16(a2h, a2l, row, 16 * slice, 64, z);
+                }
+                tc_publish();
+                if (tid == 0) {
+                    if (layer + 1 < NH)
+                        tc_layer<4>(tmem + 64, sA2h, sA2l, 1024, sW2h, sW2l, 1024, id_hidden);
+                    else if (GROUP != kCurv && e == 0 && P.with_feature)
+                        tc_layer<4>(tmem + 128, sA2h, sA2l, 1024, sW3h, sW3l, 1024, id_out_main);
+                    else
+                        tc_layer<4>(tmem + 128, sA2h, sA2l, 1024, sW3h, sW3l, 1024, id_out_tap);
+                    tc::commit(bar);
+                }
+                if (!(alive = tc_wait_all(bar, phase))) break;
+                phase ^= 1;
+            }
+            if (!alive) break;
             if (GROUP != kCurv && e == 0 && P.with_feature) {
-                float D[NT3][4];
-                out_layer<NT3>(hh, hl, net.w3f, NT3, net.b3, lane, D);
-                const int od = nl.out_dim;
+                for (int q = slice; q < N3 / 16; q += 4) {
+                    float y[16];
+                    tc::ld16(tmem + lane_off + 128 + 16 * q, y);
 #pragma unroll
-                for (int nt = 0; nt < NT3; ++nt) {
-                    const int col = nt * 8 + q * 2;
-                    if (v0) {
-                        float *o = P.feature + (s0 + g) * P.feat_stride;
-                        if (col < od) o[col] = D[nt][0];
-                        if (col + 1 < od) o[col + 1] = D[nt][1];
-                    }
-                    if (v1) {
-                        float *o = P.feature + (s0 + g + 8) * P.feat_stride;
-                        if (col < od) o[col] = D[nt][2];
-                        if (col + 1 < od) o[col + 1] = D[nt][3];
+                    for (int j = 0; j < 16; ++j) {
+                        const int col = 16 * q + j;
+                        const float val = y[j] + bias[128 + col];
+                        if (col == 0) s13[row] = val;
+                        if (v && col < od) P.feature[s * P.feat_stride + col] = val;
                     }
                 }
-                if (q == 0) {
-                    ws.s13[g][0] = D[0][0];
-                    ws.s13[g + 8][0] = D[0][2];
+                if (v && slice == 0) {
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        if (v0) P.feature[(s0 + g) * P.feat_stride + od + d] = x2m1(xc0[d]);
-                        if (v1) P.feature[(s0 + g + 8) * P.feat_stride + od + d] = x2m1(xc1[d]);
-                    }
+                    for (int d = 0; d < 3; ++d) P.feature[s * P.feat_stride + od + d] = x2m1(xc[d]);
                 }
-            } else {
-                float D[1][4];
-                out_layer<1>(hh, hl, net.w3f, NT3, net.b3, lane, D);
-                if (q == 0) {
-                    ws.s13[g][e] = D[0][0];
-                    ws.s13[g + 8][e] = D[0][2];
-                }
+            } else if (slice == 0) {
+                float y[16];
+                tc::ld16(tmem + lane_off + 128, y);
+                s13[e * 128 + row] = y[0] + bias[128];
             }
         }
-        __syncwarp();
-        if (lane < 16 && s0 + lane < P.S) {
-            const int64_t s = s0 + lane;
+        if (!alive) break;
+        // after the tile's last evaluation: the sample's stencil arithmetic
+        // (s13 of row r is written and read by the same slice-0 thread)
+        if (i == ne - 1 && v && slice == 0) {
             float *st = P.state + s * kState;
+            float sv[13];
+            for (int e = e0; e < e0 + ne; ++e) sv[e] = s13[e * 128 + row];
             if (GROUP != kCurv) {
-                P.sdf[s] = ws.s13[lane][0];
-                st[0] = ws.s13[lane][0];
+                P.sdf[s] = sv[0];
+                st[0] = sv[0];
             }
             if (GROUP == kFD) {
                 float gr[3];
-                const float gn = fmaxf(fd_grad(&ws.s13[lane][1], eps, gr), 1e-12f);
+                const float gn = fmaxf(fd_grad(&sv[1], eps, gr), 1e-12f);
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
                     P.grad[s * 3 + d] = gr[d];
-                    st[1 + 2 * d] = ws.s13[lane][1 + 2 * d];
-                    st[2 + 2 * d] = ws.s13[lane][2 + 2 * d];
+                    st[1 + 2 * d] = sv[1 + 2 * d];
+                    st[2 + 2 * d] = sv[2 + 2 * d];
                 }
                 if (P.with_laplace) {
                     // tangent-shifted point (models/geometry.py:236-246): the
@@ -515,25 +680,29 @@ __global__ void __launch_bounds__(kThreads) sdf_mlp_fwd_kernel(const __grid_cons
                                          nrm[0] * rdn[1] - nrm[1] * rdn[0]};
 #pragma unroll
                     for (int d = 0; d < 3; ++d) {
-                        const float xc = __fdiv_rn(__fsub_rn(ws.base[lane][d], -r_), __fsub_rn(r_, -r_));
+                        const float xc = __fdiv_rn(__fsub_rn(base[d], -r_), __fsub_rn(r_, -r_));
                         st[13 + d] = __fadd_rn(xc, __fmul_rn(tg[d], eps));
                     }
                 }
             }
             if (GROUP == kCurv) {
-                float gr[3], gs[3];
-                const float gn = fmaxf(fd_grad(&ws.s13[lane][1], eps, gr), 1e-12f);
-                const float gsn = fmaxf(fd_grad(&ws.s13[lane][7], eps, gs), 1e-12f);
+                float gr[3], gs[3], fd[6];
+                for (int kk = 0; kk < 6; ++kk) fd[kk] = st[1 + kk];
+                const float gn = fmaxf(fd_grad(fd, eps, gr), 1e-12f);
+                const float gsn = fmaxf(fd_grad(&sv[7], eps, gs), 1e-12f);
                 float dot = 0.f;
 #pragma unroll
                 for (int d = 0; d < 3; ++d) dot += (gr[d] / gn) * (gs[d] / gsn);
                 dot = fminf(fmaxf(dot, -1.0f + 1e-6f), 1.0f - 1e-6f);
                 P.laplace[s] = acosf(dot) / 3.14159265358979f;
-                for (int e = 7; e < 13; ++e) st[e] = ws.s13[lane][e];
+                for (int e = 7; e < 13; ++e) st[e] = sv[e];
             }
         }
-        __syncwarp();
     }
+    if (!alive && tid == 0) atomicAdd(&g_tc_timeouts, 1u);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, Sh::tmem_cols);
 }
 
 // -------------------------------------------------------------- MLP backward
@@ -634,7 +803,7 @@ template <int KH, int NH, int NT3, int GROUP>
 __global__ void __launch_bounds__(kThreads, 1) sdf_mlp_bwd_kernel(const __grid_constant__ SdfParams P) {
     using Sh = BwdShape<KH, NH, NT3>;
     constexpr int KT3 = Sh::KT3;
-    extern __shared__ __align__(16) char smem[];
+    extern __shared__ __align__(1024) char smem[];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const angelo_sdf_net_layout &nl = P.nl;
     auto copy16 = [&](int64_t dst, int64_t src, int64_t bytes) {
@@ -1126,6 +1295,9 @@ extern "C" int angelo_sdf_net_layout_query(int32_t n_levels, int32_t n_hidden, i
     L.off_b2 = take(64 * 4);
     L.off_b3 = take(8 * L.n_tiles3 * 4);
     L.off_w3row0 = take(64 * 4);
+    L.off_tcw1 = take(2 * 64 * (16 * L.k_tiles1) * 2);
+    L.off_tcw2 = take(n_hidden == 2 ? 2 * 64 * 64 * 2 : 0);
+    L.off_tcw3 = take(2 * (16 * L.k_tiles3b) * 64 * 2);
     L.bytes = o;
     *out = L;
     return ANGELO_OK;
@@ -1144,6 +1316,9 @@ extern "C" int angelo_sdf_prep(const angelo_sdf_net_layout *lay, int32_t n_level
     const int threads = (frags + extra) * 32;
     sdf_prep_kernel<<<blocks_for(threads, 256), 256, 0, as_stream(stream)>>>(
         W1, b1, W2, b2, W3, b3, in_dim, 2 * n_levels, *lay, reinterpret_cast<char *>(net));
+    const int tc_elems = 64 * 16 * K1 + (nh == 2 ? 64 * 64 : 0) + 16 * lay->k_tiles3b * 64;
+    sdf_prep_tc_kernel<<<blocks_for(tc_elems, 256), 256, 0, as_stream(stream)>>>(
+        W1, W2, W3, in_dim, 2 * n_levels, *lay, reinterpret_cast<char *>(net));
     return check_launch("sdf_prep");
 }
 
@@ -1194,14 +1369,25 @@ int persistent_grid(K k, size_t smem, const SdfParams &P, const char *what, int 
 
 template <int KH, int NH, int NT3, int GROUP>
 int launch_mlp_fwd(const SdfParams &P, cudaStream_t s) {
-    const int64_t fwd_bytes = P.nl.off_w1b;
-    const int64_t bias_bytes = ((P.nl.bytes - P.nl.off_b1 + 15) / 16) * 16;
-    const size_t smem = fwd_bytes + bias_bytes + kWarps * sizeof(FwdWarp);
+    const size_t smem = TcFwdShape<KH, NH, NT3>::bytes;
     auto k = sdf_mlp_fwd_kernel<KH, NH, NT3, GROUP>;
-    int grid = 0;
-    const int rc = persistent_grid(k, smem, P, "sdf_mlp_fwd", &grid);
-    if (rc != ANGELO_OK) return rc;
-    k<<<grid, kThreads, smem, s>>>(P);
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+        return check_launch("sdf_mlp_fwd(smem attribute)");
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kTcThreads, smem);
+    if (per_sm < 1) {
+        set_error("sdf_mlp_fwd: %zu bytes of shared memory do not fit an SM", smem);
+        return ANGELO_E_UNSUPPORTED;
+    }
+    // two CTAs per SM: their registers (2 x 512 x 64) and shared memory
+    // (2 x 115 KB) fit, and each holds 256 of the SM's 512 tensor-memory
+    // columns (the occupancy query answers 1 here); CTAs beyond what the SMs
+    // hold run as a later wave of the persistent loop
+    per_sm = 2;
+    const int64_t tiles = (P.S + 127) / 128;
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm);
+    k<<<grid, kTcThreads, smem, s>>>(P);
     return check_launch("sdf_mlp_fwd");
 }
 
@@ -1316,6 +1502,16 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
     if (shape_small(*nl)) return run_fwd<kSmallKH, kSmallNH, kSmallNT3>(P, s);
     set_error("sdf_stencil_fwd: network shape not instantiated");
     return ANGELO_E_UNSUPPORTED;
+}
+
+extern "C" int64_t angelo_tc_timeouts(int32_t reset) {
+    unsigned int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_tc_timeouts, sizeof(v)) != cudaSuccess) return -1;
+    if (reset) {
+        const unsigned int z = 0;
+        if (cudaMemcpyToSymbol(g_tc_timeouts, &z, sizeof(z)) != cudaSuccess) return -1;
+    }
+    return (int64_t)v;
 }
 
 extern "C" int64_t angelo_sdf_grad_size(const angelo_sdf_net_layout *nl) {
