@@ -309,8 +309,8 @@ class _FusedComposite(torch.autograd.Function):
         call("angelo_composite_fwd", _p(offsets), n_rays, _p(sdf), _p(grad), _p(t0), _p(t1),
              _p(rays_d), _p(rgb), _p(variance), float(meta["cos_ratio"]), _p(bg),
              float(meta["eps"]), float(meta["gate"]), _p(opacity), _p(depth), _p(comp_rgb),
-             _p(comp_normal), _p(comp_full), _p(acc_n), _p(weights), _p(trans), _p(None),
-             _s(dev), units=dict(n=S, rays=n_rays, bwd=False))
+             _p(comp_normal), _p(comp_full), _p(acc_n), _p(weights), _p(trans),
+             _p(meta.get("alpha_out")), _s(dev), units=dict(n=S, rays=n_rays, bwd=False))
         ctx.save_for_backward(sdf, grad, rgb, variance, t0, t1, offsets, rays_d, bg, opacity,
                               acc_n, weights, trans)
         ctx.meta = meta

@@ -151,6 +151,18 @@ class WNLinear(nn.Module):
         return F.linear(x, self.weight, self.bias)
 
 
+def output_activation(name):
+    """VanillaMLP's output activation (models/network_utils.py:107,112 through
+    models/utils.py get_activation): none, sigmoid, tanh, relu, exp."""
+    if name in (None, "none", "None"):
+        return lambda x: x
+    fns = {"sigmoid": torch.sigmoid, "tanh": torch.tanh, "relu": torch.relu, "exp": torch.exp}
+    key = str(name).lower()
+    if key not in fns:
+        raise NotImplementedError(f"output activation {name!r}")
+    return fns[key]
+
+
 class VanillaMLP(nn.Module):
     """models/network_utils.py:96-140: Linear(+bias) chain, Softplus(beta=100)
     between layers when sphere_init (ReLU otherwise), FP32."""
@@ -173,9 +185,7 @@ class VanillaMLP(nn.Module):
 
     def forward(self, x):
         x = self.layers(x.float())
-        if self.output_activation not in (None, "none"):
-            raise NotImplementedError("output activations other than none are not on the path")
-        return x
+        return output_activation(self.output_activation)(x)
 
     def linears(self):
         return [m for m in self.layers if isinstance(m, (nn.Linear, WNLinear))]

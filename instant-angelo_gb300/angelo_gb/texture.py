@@ -72,7 +72,11 @@ class VolumeDualColor(VolumeRadiance):
 @models.register("volume-dual-colorV3")
 class VolumeDualColorV3(nn.Module):
     """Camera-direction and reflected-direction branches blended by a weight
-    MLP (models/texture.py:113-146)."""
+    MLP (models/texture.py:113-146).  With ``use_ide`` the reflected branch
+    encodes (r + 1) / 2 of the reflected direction r with the integrated
+    directional encoding of degree ``ide_degree`` and roughness
+    sigmoid(feature 5), the reference's use_ide form (models/texture.py:73-99,
+    models/utils.py:209-273)."""
 
     def __init__(self, config):
         super().__init__()
@@ -81,8 +85,15 @@ class VolumeDualColorV3(nn.Module):
         self.n_output_dims = 3
         self.encoding = get_encoding(self.n_dir_dims, config.dir_encoding_config)
         self.n_input_dims = config.input_feature_dim + self.encoding.n_output_dims
+        self.use_ide = bool(config.get("use_ide", False))
+        if self.use_ide:
+            from .ide import IntegratedDirEncoding
+            self.ide = IntegratedDirEncoding(int(config.get("ide_degree", 4)))
+            n_ref = config.input_feature_dim + self.ide.n_output_dims
+        else:
+            n_ref = self.n_input_dims
         self.cam_network = get_mlp(self.n_input_dims, 3, config.mlp_network_config)
-        self.ref_network = get_mlp(self.n_input_dims, 3, config.mlp_network_config)
+        self.ref_network = get_mlp(n_ref, 3, config.mlp_network_config)
         # the reference spells this key 'weitht_network_config' (models/texture.py:125)
         wcfg = config.get("weitht_network_config", config.get("weight_network_config"))
         self.weight_network = get_mlp(config.input_feature_dim, 1, wcfg)
@@ -93,7 +104,11 @@ class VolumeDualColorV3(nn.Module):
         vdotn = (-viewdirs * normals).sum(-1, keepdim=True)
         ref = 2 * vdotn * normals + viewdirs
         ref = (ref + 1.0) / 2.0
-        remb = self.encoding(ref.reshape(-1, self.n_dir_dims))
+        if self.use_ide:
+            rough = torch.sigmoid(features[..., 5:6]).reshape(-1, 1)
+            remb = self.ide(ref.reshape(-1, self.n_dir_dims), rough)
+        else:
+            remb = self.encoding(ref.reshape(-1, self.n_dir_dims))
         inp = torch.cat([features.reshape(-1, features.shape[-1]),
                          normals.reshape(-1, normals.shape[-1])], dim=-1)
         w = self.weight_network(inp)

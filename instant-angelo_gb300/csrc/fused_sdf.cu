@@ -238,6 +238,17 @@ __device__ __forceinline__ void tap_point(float r, float eps, const float base[3
     *mask = e == 0 ? 7 : m;
 }
 
+// Whether the +eps and -eps taps of axis d around base coordinate b are the
+// same point after the clamp to [-r, r] (b beyond the box by more than eps).
+// Their evaluations are then identical, the two contributions +h and -h of
+// the FD backward cancel exactly, and the backward gives them weight 0: the
+// reference's formulation reaches them through normalize() of a zero FD
+// gradient, whose derivative is scaled by 1e12, and fp32 accumulation of
+// those cancelling terms would otherwise leave rounding noise of that size.
+__device__ __forceinline__ bool coincident_taps(float b, float r, float eps) {
+    return fminf(fmaxf(__fadd_rn(b, eps), -r), r) == fminf(fmaxf(__fadd_rn(b, -eps), -r), r);
+}
+
 // The stencil centre whose corners the taps share: the base clamped to the
 // box, so that the coordinates a tap does not move are bit-identical to it.
 __device__ __forceinline__ void clamped_centre(float r, const float base[3], float xc[3]) {
@@ -900,7 +911,7 @@ __global__ void __launch_bounds__(kThreads, 1) sdf_mlp_bwd_kernel(const __grid_c
                 normalize_bwd(gs, gsn, ns, dns, dgs);
 #pragma unroll
                 for (int d = 0; d < 3; ++d) {
-                    const float h = __fdiv_rn(0.5f * dgs[d], eps);
+                    const float h = coincident_taps(st[13 + d], r_, eps) ? 0.f : __fdiv_rn(0.5f * dgs[d], eps);
                     ws.ds[lane][7 + 2 * d] = h;
                     ws.ds[lane][8 + 2 * d] = -h;
                 }
@@ -934,7 +945,9 @@ __global__ void __launch_bounds__(kThreads, 1) sdf_mlp_bwd_kernel(const __grid_c
 #pragma unroll
                     for (int d = 0; d < 3; ++d) {
                         const float gin = P.g_grad ? P.g_grad[s * 3 + d] : 0.f;
-                        const float h = __fdiv_rn(0.5f * (dg[d] + gin), eps);
+                        const float h = coincident_taps(P.pos[s * 3 + d], r_, eps)
+                                            ? 0.f
+                                            : __fdiv_rn(0.5f * (dg[d] + gin), eps);
                         ws.ds[lane][1 + 2 * d] = h;
                         ws.ds[lane][2 + 2 * d] = -h;
                     }
@@ -1027,9 +1040,6 @@ __global__ void __launch_bounds__(kThreads, 1) sdf_mlp_bwd_kernel(const __grid_c
                         part[nt][1] += __shfl_xor_sync(0xffffffffu, part[nt][1], o);
                     }
                 }
-                float sdy = dy0 + dy1;
-#pragma unroll
-                for (int o = 4; o < 32; o <<= 1) sdy += __shfl_xor_sync(0xffffffffu, sdy, o);
                 if (lane < 4) {
 #pragma unroll
                     for (int nt = 0; nt < 8; ++nt) {
@@ -1037,7 +1047,9 @@ __global__ void __launch_bounds__(kThreads, 1) sdf_mlp_bwd_kernel(const __grid_c
                         red_add(S.dW3 + nt * 8 + lane * 2 + 1, part[nt][1]);
                     }
                 }
-                if (lane == 0) red_add(S.db3, sdy);
+                // the taps' SDF-bias gradient, sum_e ds_e, is exactly zero (each
+                // axis contributes +h and -h): it is not accumulated, so that
+                // large cancelling terms do not round into the bias
             }
 #pragma unroll
             for (int nt = 0; nt < 8; ++nt)

@@ -13,7 +13,9 @@ feeds the reference's own modules (through the stub harness in
 Hash-grid cells and corner indices come from the C restatement (float32
 arithmetic exactly as tcnn's kernel performs it, see ``oracle.c``); trilinear
 weights and everything downstream are float64 and differentiable, so
-``torch.autograd`` on this module is the gradient reference.
+``torch.autograd`` on this module is the gradient reference.  The float64
+arithmetic runs on the device of its inputs (the precision study runs it on
+the GPU); the cells are always computed on the host.
 """
 from __future__ import annotations
 
@@ -57,13 +59,13 @@ def hash_encode(x, table, lay: HashGridLayout, active_levels=None):
     act = L if active_levels is None else int(active_levels)
     x32 = x.detach().to(torch.float32).cpu().numpy()
     idx, _, cells = cref.hashgrid_index(x32, lay.cref_layout, with_cells=True)
-    idx = torch.from_numpy(idx.astype(np.int64))
-    cells = torch.from_numpy(cells.astype(np.float64)).to(x.dtype)
+    idx = torch.from_numpy(idx.astype(np.int64)).to(x.device)
+    cells = torch.from_numpy(cells.astype(np.float64)).to(device=x.device, dtype=x.dtype)
     tab = table.view(-1, Fd)
     outs = []
     for l in range(L):
         if l >= act:
-            outs.append(torch.zeros(x.shape[0], Fd, dtype=x.dtype))
+            outs.append(torch.zeros(x.shape[0], Fd, dtype=x.dtype, device=x.device))
             continue
         s = float(lay.scales[l])
         frac = x * s + 0.5 - cells[:, l, :]              # (N,3), float64, d/dx = scale
@@ -170,7 +172,7 @@ def volume_sdf(points, P, G, rand_dirs=None, with_grad=True, with_feature=True,
     rv = [sdf]
     grad = None
     if with_grad:
-        off = torch.tensor(_FD_OFFSETS, dtype=points.dtype) * eps
+        off = torch.tensor(_FD_OFFSETS, dtype=points.dtype, device=points.device) * eps
         pd = (points[:, None, :] + off).clamp(-r, r)
         sd = field(contract(pd, r).reshape(-1, 3))[:, 0].reshape(-1, 6)
         grad = 0.5 * (sd[:, 0::2] - sd[:, 1::2]) / eps
@@ -182,7 +184,7 @@ def volume_sdf(points, P, G, rand_dirs=None, with_grad=True, with_feature=True,
         normals = F.normalize(grad, dim=-1)
         tangent = torch.cross(normals, rd, dim=-1)
         shifted = pts_c + tangent * eps                 # contracted points (reference quirk)
-        off = torch.tensor(_FD_OFFSETS, dtype=points.dtype) * eps
+        off = torch.tensor(_FD_OFFSETS, dtype=points.dtype, device=points.device) * eps
         psd = (shifted[:, None, :] + off).clamp(-r, r)  # clamped as if world coordinates
         ssd = field(contract(psd, r).reshape(-1, 3))[:, 0].reshape(-1, 6)
         gs = 0.5 * (ssd[:, 0::2] - ssd[:, 1::2]) / eps
@@ -224,13 +226,42 @@ def texture(features, dirs, normal, P, T):
     return torch.sigmoid(color)
 
 
+def ide(xyz, kappa_inv, deg):
+    """Integrated directional encoding (models/utils.py:209-273; Ref-NeRF eq.
+    6-8): for l = 2^i (i < deg), m = 0..l, (x + i y)^m N_lm Q_l^m(z)
+    exp(-l(l+1)/2 kappa_inv), real parts then imaginary parts.  Q_l^m =
+    P_l^m / (1 - z^2)^(m/2) (Condon-Shortley phase) by the recurrence in l:
+    Q_m^m = (-1)^m (2m-1)!!, Q_{m+1}^m = (2m+1) z Q_m^m,
+    (l - m) Q_l^m = (2l - 1) z Q_{l-1}^m - (l + m - 1) Q_{l-2}^m."""
+    x, y, z = xyz[..., 0:1], xyz[..., 1:2], xyz[..., 2:3]
+    w = torch.complex(x, y)
+    re, im = [], []
+    for i in range(deg):
+        l = 2 ** i
+        for m in range(l + 1):
+            q_prev, q = None, torch.full_like(z, (-1.0) ** m * float(np.prod(np.arange(2 * m - 1, 0, -2))))
+            for ll in range(m + 1, l + 1):
+                nxt = ((2 * ll - 1) * z * q - ((ll + m - 1) * q_prev if q_prev is not None else 0.0)) / (ll - m)
+                q_prev, q = q, nxt
+            norm = math.sqrt((2 * l + 1) / (4 * math.pi) * math.factorial(l - m) / math.factorial(l + m))
+            val = w ** m * (norm * q * torch.exp(-0.5 * l * (l + 1) * kappa_inv))
+            re.append(val.real)
+            im.append(val.imag)
+    return torch.cat(re + im, dim=-1)
+
+
 def texture_v3(features, viewdirs, normals, P, T):
     """VolumeDualColorV3 (models/texture.py:127-146): camera and reflected
     branches blended by a weight MLP."""
     emb = sh4((viewdirs + 1.0) / 2.0)
     vdotn = (-viewdirs * normals).sum(-1, keepdim=True)
     ref = 2 * vdotn * normals + viewdirs
-    remb = sh4((ref + 1.0) / 2.0)
+    if T.get("ide_degree"):
+        # reflection branch on the IDE of (r + 1) / 2 with roughness
+        # sigmoid(feature 5), the reference's use_ide form (models/texture.py:91-95)
+        remb = ide((ref + 1.0) / 2.0, torch.sigmoid(features[..., 5:6]), T["ide_degree"])
+    else:
+        remb = sh4((ref + 1.0) / 2.0)
     inp = torch.cat([features, normals], dim=-1)
     wl = mlp_layers(P, "texture.weight_network", T["n_weight_layers"], False)
     wgt = mlp(inp, wl, False)
@@ -269,13 +300,13 @@ def render_weights(alpha, offsets, early_stop_eps=1e-4):
     w_j = alpha_j * prod_{k<j}(1 - alpha_k), zero once the transmittance has
     dropped below early_stop_eps.  Differentiable float64."""
     n = alpha.shape[0]
-    out = torch.zeros(n, dtype=alpha.dtype)
+    out = torch.zeros(n, dtype=alpha.dtype, device=alpha.device)
     ws = []
     for r in range(len(offsets) - 1):
         a = alpha[offsets[r]:offsets[r + 1]]
         if a.numel() == 0:
             continue
-        T = torch.cumprod(torch.cat([torch.ones(1, dtype=a.dtype), 1 - a[:-1]]), 0)
+        T = torch.cumprod(torch.cat([torch.ones(1, dtype=a.dtype, device=a.device), 1 - a[:-1]]), 0)
         ws.append(a * T * (T >= early_stop_eps).to(a.dtype))
     if ws:
         out = torch.cat(ws)
@@ -285,7 +316,7 @@ def render_weights(alpha, offsets, early_stop_eps=1e-4):
 def accumulate(w, ray_indices, values, n_rays):
     """accumulate_along_rays (nerfacc 0.3.3, models/neus.py:235-240)."""
     src = w[:, None] if values is None else w[:, None] * values
-    out = torch.zeros(n_rays, src.shape[-1], dtype=src.dtype)
+    out = torch.zeros(n_rays, src.shape[-1], dtype=src.dtype, device=src.device)
     return out.index_add(0, ray_indices, src)
 
 
@@ -296,9 +327,9 @@ def neus_render(rays, P, G, T, march, rand_dirs, cos_anneal_ratio, background_co
     nerfacc restatement (integers and float32 t); everything else float64."""
     n_rays = rays.shape[0]
     offsets, ray_idx, t0, t1 = march
-    ray_idx = torch.as_tensor(ray_idx, dtype=torch.int64)
-    t0 = torch.as_tensor(t0, dtype=rays.dtype)[:, None]
-    t1 = torch.as_tensor(t1, dtype=rays.dtype)[:, None]
+    ray_idx = torch.as_tensor(ray_idx, dtype=torch.int64, device=rays.device)
+    t0 = torch.as_tensor(t0, dtype=rays.dtype, device=rays.device)[:, None]
+    t1 = torch.as_tensor(t1, dtype=rays.dtype, device=rays.device)[:, None]
     o, d = rays[:, 0:3], rays[:, 3:6]
     t_o, t_d = o[ray_idx], d[ray_idx]
     mid = (t0 + t1) / 2.0

@@ -1,0 +1,189 @@
+"""Precision study (the precision form of the small configuration): the fused
+path with an FP16 or FP32 hash table, the geometry and radiance MLPs on
+tensor cores (bf16 hi/lo operands, fp32 accumulation), fp32 alpha with the
+FP64-gated sigmoid difference above inv_s = 2048 and the log-space
+transmittance scan; the plain FP32 path beside it.  Every error is against
+the FP64 oracle run on the GPU (oracle/neus_fp64.py):
+
+* SDF and unit normals (finite-difference gradient, eps 1e-2) on 2^20 uniform
+  points in [-1, 1]^3;
+* per-ray colour and per-sample weights on 8192 rays;
+* alpha at inv_s in {20, 2048, 1e4, 1e5} from the same fp32 inputs (the FP64
+  sigmoid difference of those inputs is the reference, so the comparison
+  isolates the alpha arithmetic from the conditioning of alpha in the SDF).
+
+The report (max / mean absolute errors) goes to $ANGELO_PRECISION_REPORT when
+that is set.  Bounds: 1e-3 for every fused output with the FP32 table and for
+the gated alpha at every inv_s."""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+N_POINTS = 1 << 20
+N_RAYS = 8192
+REPORT = {}
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    from angelo_gb import build
+    build.build()
+    return torch.device("cuda:0")
+
+
+def _model(dev, fused, fp16_table=False):
+    from angelo_gb import models, workloads
+    torch.manual_seed(0)
+    m = models.make("neus", workloads.model_config("small", fused=fused)).to(dev)
+    m.update_step(0, 5000)
+    with torch.no_grad():
+        g = torch.Generator(device="cpu").manual_seed(7)
+        p = m.geometry.hashgrid.encoding.params
+        p.copy_((torch.rand(p.shape, generator=g) * 0.1 - 0.05).to(dev))
+        # the sphere initialisation leaves the hash-feature columns of the
+        # first layer at zero: give them weight so that the table matters
+        wv = m.geometry.network.layers[0].weight_v
+        wv[:, 3:].copy_((torch.randn(wv[:, 3:].shape, generator=g) * 0.05).to(dev))
+        if fp16_table:
+            m.geometry.hashgrid.encoding.params.data = p.data.half()
+    return m.train()
+
+
+def _oracle_cfg(m):
+    from oracle import neus_fp64 as O
+    c = m.config
+    h = c.geometry.xyz_encoding_config
+    lay = O.HashGridLayout(h.n_levels, h.n_features_per_level, h.log2_hashmap_size,
+                           h.base_resolution, h.per_level_scale)
+    G = dict(radius=float(c.radius), eps=float(m.geometry._finite_difference_eps), lay=lay,
+             active_levels=int(m.geometry.hashgrid.mask_levels),
+             n_layers=c.geometry.mlp_network_config.n_hidden_layers + 1,
+             feature_dim=c.geometry.feature_dim)
+    T = dict(kind="radiance", n_layers=c.texture.mlp_network_config.n_hidden_layers + 1)
+    P = {k: v.detach().double() for k, v in m.state_dict().items()}
+    return P, G, T
+
+
+def _err(a, b):
+    d = (a.double() - b.double()).abs()
+    return {"max": float(d.max()), "mean": float(d.mean())}
+
+
+def _unit(v):
+    return torch.nn.functional.normalize(v.double(), p=2, dim=-1)
+
+
+def _write():
+    path = os.environ.get("ANGELO_PRECISION_REPORT")
+    if path:
+        with open(path, "w") as f:
+            json.dump(REPORT, f, indent=1, sort_keys=True)
+
+
+def test_precision_sdf_and_normals(dev):
+    from oracle import neus_fp64 as O
+    forms = {"plain_fp32": _model(dev, False), "fused_fp32_table": _model(dev, True),
+             "fused_fp16_table": _model(dev, True, fp16_table=True)}
+    P, G, _ = _oracle_cfg(forms["plain_fp32"])
+    g = torch.Generator(device="cpu").manual_seed(11)
+    pts = (torch.rand(N_POINTS, 3, generator=g) * 2.0 - 1.0).to(dev)
+    ref_s, ref_n = [], []
+    with torch.no_grad():
+        for c in range(0, N_POINTS, 1 << 16):
+            s64, g64 = O.volume_sdf(pts[c:c + (1 << 16)].double(), P, G, None, True, False, False)
+            ref_s.append(s64)
+            ref_n.append(_unit(g64))
+    ref_s, ref_n = torch.cat(ref_s), torch.cat(ref_n)
+    out = {}
+    for name, m in forms.items():
+        with torch.no_grad():
+            sdf, grad = m.geometry(pts, with_grad=True, with_feature=False)
+        out[name] = {"sdf": _err(sdf, ref_s), "normal": _err(_unit(grad), ref_n)}
+    REPORT["points_2^20"] = out
+    _write()
+    for name in ("plain_fp32", "fused_fp32_table"):
+        assert out[name]["sdf"]["max"] < 1e-3, (name, out[name])
+        assert out[name]["normal"]["mean"] < 1e-3, (name, out[name])
+    assert out["fused_fp16_table"]["sdf"]["max"] < 1e-2, out["fused_fp16_table"]
+
+
+def _rays(dev):
+    from angelo_gb.scenes import look_at_c2w, pixel_directions, rays_from
+    g = np.random.default_rng(5)
+    dirs = pixel_directions(256, 256, 64.0, device=dev).reshape(-1, 3)
+    out = []
+    for k in range(N_RAYS // 1024):
+        v = g.normal(size=3)
+        c2w = torch.as_tensor(look_at_c2w(tuple(2.5 * v / np.linalg.norm(v))), dtype=torch.float32,
+                              device=dev)
+        pix = torch.from_numpy(g.integers(0, dirs.shape[0], 1024)).to(dev)
+        out.append(rays_from(dirs[pix], c2w[None].expand(1024, 3, 4)))
+    return torch.cat(out).float().contiguous()
+
+
+def test_precision_render(dev):
+    from angelo_gb import fused
+    from oracle import neus_fp64 as O
+    rays = _rays(dev)
+    o, d = rays[:, :3].contiguous(), rays[:, 3:].contiguous()
+    plain = _model(dev, False)
+    bg = torch.ones(3, device=dev)
+    plain.background_color = bg
+    plain.randomized = False
+    ri, t0, t1, off = plain.march_rays(o, d)
+    P, G, T = _oracle_cfg(plain)
+    rd = torch.randn(ri.numel(), 3, generator=torch.Generator(device="cpu").manual_seed(3)).to(dev)
+    with torch.no_grad():
+        ref = O.neus_render(rays.double(), P, G, T, (off.cpu().numpy(), ri.long(), t0, t1), rd.double(),
+                            1.0, bg.double(), training=True)
+    out = {}
+    for name, m in (("plain_fp32", plain), ("fused_fp32_table", _model(dev, True)),
+                    ("fused_fp16_table", _model(dev, True, fp16_table=True))):
+        m.background_color = bg
+        m.geometry.curvature_dirs_fn = lambda t: rd
+        m.train()
+        m.randomized = False
+        with torch.no_grad():
+            r = m.forward_(rays)
+        out[name] = {"colour": _err(r["comp_rgb_full"], ref["comp_rgb_full"]),
+                     "weights": _err(r["weights"].view(-1), ref["weights"])}
+    REPORT["rays_8192"] = out
+    _write()
+    for name in ("plain_fp32", "fused_fp32_table"):
+        assert out[name]["colour"]["max"] < 1e-3, (name, out[name])
+        assert out[name]["weights"]["max"] < 1e-3, (name, out[name])
+
+    # alpha at increasing sharpness, from the same fp32 inputs
+    sdf32 = ref["sdf_samples"].float()
+    n32 = _unit(ref["sdf_grad_samples"]).float()
+    d32 = d[ri.long()]
+    dist32 = (t1 - t0).float()
+    alpha_rows = {}
+    for inv_s in (20.0, 2048.0, 1e4, 1e5):
+        var = torch.tensor([math.log(inv_s) / 10.0], device=dev)
+        s64 = torch.exp(var.double() * 10.0)
+        a64 = O.get_alpha(sdf32.double(), n32.double(), d32.double(), dist32.double(), s64, 1.0)
+        with torch.no_grad():
+            plain.variance.variance.fill_(float(var))
+            a_plain = plain.get_alpha(sdf32, n32, d32, dist32[:, None]).view(-1)
+        row = {"plain_fp32": _err(a_plain, a64)}
+        for label, gate in (("fused_gated", fused.FP64_ALPHA_GATE), ("fused_fp32_only", float("inf"))):
+            alpha = torch.empty(sdf32.numel(), device=dev)
+            meta = dict(cos_ratio=1.0, eps=1e-4, gate=gate, alpha_out=alpha)
+            rgb = torch.zeros(sdf32.numel(), 3, device=dev)
+            with torch.no_grad():
+                fused._FusedComposite.apply(sdf32, n32, rgb, var, t0, t1, off, d, bg, meta)
+            row[label] = _err(alpha, a64)
+        alpha_rows[f"inv_s={inv_s:g}"] = row
+    REPORT["alpha"] = alpha_rows
+    _write()
+    for k, row in alpha_rows.items():
+        assert row["fused_gated"]["max"] < 1e-3, (k, row)

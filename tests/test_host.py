@@ -96,3 +96,18 @@ def test_unbound_entry_point_is_refused(lib):
     from angelo_gb import _lib
     with pytest.raises(_lib.AngeloError):
         _lib.call("angelo_not_declared", 1, 2)
+
+
+def test_ide_matches_reference_golden():
+    """angelo_gb.ide (Legendre-derivative polynomials) against the reference's
+    generate_ide_fn(4) golden vectors."""
+    import os
+    import torch
+    from angelo_gb.ide import IntegratedDirEncoding
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ide_deg4.npz"))
+    enc = IntegratedDirEncoding(4).double()
+    out = enc(torch.from_numpy(g["xyz"]).double(), torch.from_numpy(g["kappa_inv"]).double())
+    assert enc.n_output_dims == 38
+    np.testing.assert_allclose(out.numpy(), g["ide"], rtol=1e-5, atol=1e-5)
+    out32 = IntegratedDirEncoding(4)(torch.from_numpy(g["xyz"]), torch.from_numpy(g["kappa_inv"]))
+    np.testing.assert_allclose(out32.numpy(), g["ide"], rtol=1e-4, atol=1e-4)

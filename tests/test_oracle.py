@@ -205,3 +205,14 @@ def test_missing_ray_gets_far_sentinel():
     tmin, tmax = cref.ray_aabb(np.array([[5, 5, 5]], np.float32), np.array([[1, 0, 0]], np.float32),
                                np.array([-1, -1, -1, 1, 1, 1], np.float32))
     assert tmin[0] == np.float32(1e10) and tmax[0] == np.float32(1e10)
+
+
+def test_ide_matches_reference_golden():
+    """The oracle's integrated directional encoding (associated-Legendre
+    recurrence) against the reference's generate_ide_fn(4) (golden vectors
+    from tests/golden/make_ide_golden.py, float32 as the reference computes)."""
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "ide_deg4.npz"))
+    out = O.ide(torch.from_numpy(g["xyz"]).double(), torch.from_numpy(g["kappa_inv"]).double(), 4)
+    assert out.shape == (96, 38)
+    np.testing.assert_allclose(out.numpy(), g["ide"], rtol=1e-5, atol=1e-5)
