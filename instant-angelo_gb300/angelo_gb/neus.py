@@ -236,6 +236,7 @@ class NeuSModel(nn.Module):
                                                cone_angle=0.0, max_steps=self.max_march_steps,
                                                **grid)
         self._last_march = (t_min, t_max)
+        self.last_num_samples = int(t0.shape[0])   # host-side, no device read
         return ri, t0, t1, offsets
 
     def forward_(self, rays):

@@ -201,8 +201,10 @@ UNBOUNDED_ROI = (-1e10, -1e10, -1e10, 1e10, 1e10, 1e10)
 def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), bits=None,
           cone_angle=0.0, max_steps=1 << 20):
     """Occupancy-grid ray marching.  Returns (ray_indices int32 (S,),
-    t_starts (S,), t_ends (S,), offsets int64 (R+1,)).  Reads the sample count
-    back to the host to size the outputs, as the reference does."""
+    t_starts (S,), t_ends (S,), offsets int64 (R+1,), status): the sample
+    count is read back to the host to size the outputs, as the reference
+    does; status is a device int32 tensor (bit 0: a ray reached max_steps)
+    that is not read here, so the caller's stream keeps running."""
     rays_o = _cuda(rays_o, "rays_o", dims=2)
     rays_d = _cuda(rays_d, "rays_d", dims=2)
     t_min = _cuda(t_min, "t_min").reshape(-1)
@@ -227,11 +229,8 @@ def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), 
     call("angelo_march_fill", _p(rays_o), _p(rays_d), _p(t_min), _p(t_max), n, ctypes.byref(g),
          float(step), float(cone_angle), int(max_steps), _p(offsets), total, _p(ri), _p(t0),
          _p(t1), _p(status), s)
-    st = int(status.item())
-    if st & 2:
-        raise _lib.AngeloError("angelo_march_fill", _lib.ANGELO_E_CAPACITY,
-                               "sample capacity exceeded")
-    return ri, t0, t1, offsets, st
+    # the outputs are sized by the count pass, so the fill cannot exceed them
+    return ri, t0, t1, offsets, status[0]
 
 
 def scan(counts):

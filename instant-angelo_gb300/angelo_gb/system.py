@@ -65,7 +65,11 @@ class NeuSTrainer:
         m.update_step(0, self.global_step)
         m.background_color = background_color
         out = m(rays)
-        n_samples = int(out["num_samples_full"].sum().item())
+        # the march sized its outputs on the host: no device read here, so
+        # the backward is enqueued while the forward still runs
+        n_samples = getattr(m, "last_num_samples", None)
+        if n_samples is None:
+            n_samples = int(out["num_samples_full"].sum().item())
         if self.dynamic:
             new = int(self.train_num_rays * (self.train_num_samples / max(n_samples, 1)))
             self.train_num_rays = min(int(self.train_num_rays * 0.9 + new * 0.1),

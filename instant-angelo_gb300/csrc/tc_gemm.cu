@@ -1,5 +1,5 @@
 // The tcgen05 building block of the fused MLP kernels as a callable GEMM:
-// D (128 x N, fp32) = A (128 x K) * B (N x K)^T with both operands split into
+// D (M x N, fp32) = A (M x K) * B (N x K)^T, M = 64 or 128, with both operands split into
 // bf16 hi/lo parts in shared memory (no swizzle) and the three products
 // lo*hi + hi*lo + hi*hi accumulated in tensor memory (bf16x3), one CTA of 4
 // warps.  Each operand is staged K-major (8 x 8 core matrices, K contiguous)
@@ -28,8 +28,8 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16 *hi, __nv_bflo
 
 __global__ void __launch_bounds__(128, 1)
     tc_gemm_x3_kernel(const float *__restrict__ A, const float *__restrict__ B, float *__restrict__ D, int N,
-                      int K, int a_mn, int b_mn, int variant, uint32_t ncols, int a_region, int b_region,
-                      int *status) {
+                      int K, int M, int a_mn, int b_mn, int variant, uint32_t ncols, int a_region,
+                      int b_region, int *status) {
     extern __shared__ __align__(1024) char smem[];
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     char *a_hi = smem, *a_lo = a_hi + a_region, *b_hi = a_lo + a_region, *b_lo = b_hi + b_region;
@@ -37,9 +37,9 @@ __global__ void __launch_bounds__(128, 1)
     uint32_t *slot = reinterpret_cast<uint32_t *>(mbar + 1);
     // K-major: element (r, k) at kmajor_offset(r, k, K); MN-major: the
     // transposed storage, kmajor_offset(k, r, rows)
-    for (int i = tid; i < 128 * K; i += 128) {
+    for (int i = tid; i < M * K; i += 128) {
         const int r = i / K, k = i % K;
-        const uint32_t o = a_mn ? tc::kmajor_offset(k, r, 128) : tc::kmajor_offset(r, k, K);
+        const uint32_t o = a_mn ? tc::kmajor_offset(k, r, M) : tc::kmajor_offset(r, k, K);
         split_bf16(A[i], reinterpret_cast<__nv_bfloat16 *>(a_hi + o), reinterpret_cast<__nv_bfloat16 *>(a_lo + o));
     }
     for (int i = tid; i < N * K; i += 128) {
@@ -58,16 +58,16 @@ __global__ void __launch_bounds__(128, 1)
     tc::fence_after_sync();
     const uint32_t tmem = *slot;
     if (tid == 0) {
-        const uint32_t id = tc::idesc_bf16_f32(128, N, a_mn, b_mn);
+        const uint32_t id = tc::idesc_bf16_f32(M, N, a_mn, b_mn);
         // core-matrix strides: LBO along K, SBO along M (or N), for either
         // operand major; variant 1 exchanges the two fields
-        const uint32_t a_k = tc::k_stride(a_mn, 128, K), a_m = tc::mn_stride(a_mn, 128, K);
+        const uint32_t a_k = tc::k_stride(a_mn, M, K), a_m = tc::mn_stride(a_mn, M, K);
         const uint32_t b_k = tc::k_stride(b_mn, N, K), b_m = tc::mn_stride(b_mn, N, K);
         const uint32_t a_lbo = variant == 0 ? a_k : a_m, a_sbo = variant == 0 ? a_m : a_k;
         const uint32_t b_lbo = variant == 0 ? b_k : b_m, b_sbo = variant == 0 ? b_m : b_k;
         for (int ks = 0; ks < K / 16; ++ks) {
             // one K step of 16: two K chunks (K-major) or two 8-row groups (MN-major)
-            const uint32_t a_off = a_mn ? ks * 2 * (16u * 128u) : ks * 256u;
+            const uint32_t a_off = a_mn ? ks * 2 * (16u * (uint32_t)M) : ks * 256u;
             const uint32_t b_off = b_mn ? ks * 2 * (16u * (uint32_t)N) : ks * 256u;
             const uint64_t ah = tc::smem_desc(tc::smem_addr(a_hi) + a_off, a_lbo, a_sbo);
             const uint64_t al = tc::smem_desc(tc::smem_addr(a_lo) + a_off, a_lbo, a_sbo);
@@ -84,13 +84,15 @@ __global__ void __launch_bounds__(128, 1)
     if (!done) {
         if (lane == 0) atomicExch(status, 1);
     } else {
+        // every tensor-memory lane (128 x N): for M = 128 lane i holds row i of D
         tc::fence_after_sync();
         const int row = warp * 32 + lane;
-        for (int c0 = 0; c0 < N; c0 += 16) {
+        const int width = M == 64 ? 2 * N : N;
+        for (int c0 = 0; c0 < width; c0 += 16) {
             float v[16];
             tc::ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) D[(int64_t)row * N + c0 + j] = v[j];
+            for (int j = 0; j < 16; ++j) D[(int64_t)row * width + c0 + j] = v[j];
         }
     }
     tc::fence_before_sync();
@@ -115,25 +117,27 @@ int operand_region(int rows, int K, int mn_major) {
 
 }  // namespace
 
-extern "C" int angelo_tc_gemm_x3(const float *A, const float *B, float *D, int32_t N, int32_t K,
-                                 int32_t a_mn_major, int32_t b_mn_major, int32_t variant, int32_t *status,
-                                 void *stream) {
+extern "C" int angelo_tc_gemm_x3(const float *A, const float *B, float *D, int32_t M, int32_t N,
+                                 int32_t K, int32_t a_mn_major, int32_t b_mn_major, int32_t variant,
+                                 int32_t *status, void *stream) {
     ANGELO_REQUIRE(A && B && D && status, "tc_gemm_x3: null pointer");
+    ANGELO_REQUIRE(M == 64 || M == 128, "tc_gemm_x3: M %d (64 or 128)", M);
+    ANGELO_REQUIRE(M == 128 || N <= 128, "tc_gemm_x3: N %d > 128 with M = 64", N);
     ANGELO_REQUIRE(N >= 16 && N <= 256 && N % 16 == 0, "tc_gemm_x3: N %d (16..256, multiple of 16)", N);
     ANGELO_REQUIRE(K >= 16 && K <= 64 && K % 16 == 0, "tc_gemm_x3: K %d (16..64, multiple of 16)", K);
     ANGELO_REQUIRE(variant == 0 || variant == 1, "tc_gemm_x3: variant %d", variant);
     ANGELO_REQUIRE((a_mn_major | b_mn_major) >= 0 && a_mn_major <= 1 && b_mn_major <= 1,
                    "tc_gemm_x3: operand majors");
     uint32_t ncols = 32;
-    while (ncols < (uint32_t)N) ncols <<= 1;
-    const int a_region = operand_region(128, K, a_mn_major);
+    while (ncols < (uint32_t)(M == 64 ? 2 * N : N)) ncols <<= 1;
+    const int a_region = operand_region(M, K, a_mn_major);
     const int b_region = operand_region(N, K, b_mn_major);
     const size_t smem = (size_t)2 * a_region + (size_t)2 * b_region + 64;
     ANGELO_REQUIRE(smem <= 227 * 1024, "tc_gemm_x3: %zu bytes of shared memory", smem);
     if (cudaFuncSetAttribute(tc_gemm_x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
         cudaSuccess)
         return check_launch("tc_gemm_x3(smem attribute)");
-    tc_gemm_x3_kernel<<<1, 128, smem, as_stream(stream)>>>(A, B, D, N, K, a_mn_major, b_mn_major, variant,
-                                                           ncols, a_region, b_region, status);
+    tc_gemm_x3_kernel<<<1, 128, smem, as_stream(stream)>>>(A, B, D, N, K, M, a_mn_major, b_mn_major,
+                                                           variant, ncols, a_region, b_region, status);
     return check_launch("tc_gemm_x3");
 }

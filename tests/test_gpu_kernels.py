@@ -171,7 +171,7 @@ def test_march_bit_exact(dev, p_occ):
     np.testing.assert_array_equal(ri.cpu().numpy(), rri)
     np.testing.assert_array_equal(t0.cpu().numpy(), rt0)
     np.testing.assert_array_equal(t1.cpu().numpy(), rt1)
-    assert st == 0 and not ovf
+    assert int(st) == 0 and not ovf
     if p_occ == 0.0:
         assert off[-1].item() == 0
 
@@ -200,7 +200,7 @@ def test_march_step_cap_sets_status(dev):
     ri, t0, t1, off, st = ops.march(torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev),
                                     torch.zeros(2, device=dev), torch.full((2,), 1e10, device=dev),
                                     0.01, max_steps=1000)
-    assert st & 1
+    assert int(st) & 1
     assert np.all(np.diff(off.cpu().numpy()) == 1000)
 
 
