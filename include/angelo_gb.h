@@ -190,11 +190,10 @@ int angelo_accumulate_bwd(const float *weights, const float *values, int32_t cha
 
 /* ------------------------------------------------------------ fused VolumeSDF */
 
-/* Prepared geometry-MLP operands: bf16 hi/lo tensor-core fragments of every
- * layer (forward and backward order), fp32 biases.  Layout by query. */
+/* Prepared geometry-MLP operands: fp32 biases and output row 0, and the
+ * three layers as bf16 hi/lo tensor-core operands.  Layout by query. */
 typedef struct {
     int32_t k_tiles1, n_hidden, n_tiles3, k_tiles3b, out_dim;
-    int64_t off_w1f, off_w2f, off_w3f, off_w1b, off_w2b, off_w3b;
     int64_t off_b1, off_b2, off_b3, off_w3row0;
     /* tensor-core (tcgen05) operands: W1 (64 x 16*k_tiles1), W2 (64 x 64),
      * W3 (16*k_tiles3b x 64) in the K-major core-matrix layout, bf16 hi then lo */
@@ -261,23 +260,26 @@ int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32_t active_l
 
 /* ------------------------------------------------- tensor-core building block */
 
-/* D (128 x N, fp32, row-major) = A (128 x K) * B (N x K)^T on the 5th-
- * generation tensor cores (tcgen05.mma, operands in shared memory, fp32
- * accumulation in tensor memory) with both operands split into bf16 hi/lo
- * (three products).  a_mn_major / b_mn_major stage the operand MN-major
- * (0: K-major); variant 0 is the descriptor convention the fused kernels use,
- * 1 exchanges the descriptor's two core-matrix strides (a layout self-check).
- * N in 16..256 (multiple of 16), K in 16..64 (multiple of 16).  *status
- * (zeroed by the caller) becomes 1 if the completion wait timed out.  No
- * counterpart in the reference: it pins the layouts the fused MLP kernels
- * rely on. */
 /* Number of CTAs of the tensor-core kernels that stopped waiting for an MMA
  * completion (bounded mbarrier waits) since the last reset; synchronous, -1
  * on a CUDA error.  A diagnostic counter: the one piece of mutable device
  * state of the library besides the allocation-free scan's workspace. */
 int64_t angelo_tc_timeouts(int32_t reset);
 
-int angelo_tc_gemm_x3(const float *A, const float *B, float *D, int32_t N, int32_t K,
+/* A (M x K) * B (N x K)^T, M = 64 or 128, on the 5th-generation tensor
+ * cores (tcgen05.mma, operands in shared memory, fp32 accumulation in tensor
+ * memory) with both operands split into bf16 hi/lo (three products).  D
+ * (128 x W, fp32, row-major, W = N for M = 128 and 2N for M = 64) receives
+ * every tensor-memory lane of the accumulator's first W columns: for M = 128
+ * lane i is row i of the product.
+ * a_mn_major / b_mn_major stage the operand MN-major (0: K-major); variant 0
+ * is the descriptor convention the fused kernels use, 1 exchanges the
+ * descriptor's two core-matrix strides (a layout self-check).  N in 16..256
+ * (multiple of 16; at most 128 for M = 64), K in 16..64 (multiple of 16).
+ * *status (zeroed by the caller) becomes 1 if the completion wait timed out.
+ * No counterpart in the reference: it pins the layouts the fused MLP kernels
+ * rely on. */
+int angelo_tc_gemm_x3(const float *A, const float *B, float *D, int32_t M, int32_t N, int32_t K,
                       int32_t a_mn_major, int32_t b_mn_major, int32_t variant, int32_t *status,
                       void *stream);
 

@@ -42,8 +42,6 @@ class GridDesc(ctypes.Structure):
 class SdfNetLayout(ctypes.Structure):
     _fields_ = [("k_tiles1", c_i32), ("n_hidden", c_i32), ("n_tiles3", c_i32),
                 ("k_tiles3b", c_i32), ("out_dim", c_i32),
-                ("off_w1f", c_i64), ("off_w2f", c_i64), ("off_w3f", c_i64),
-                ("off_w1b", c_i64), ("off_w2b", c_i64), ("off_w3b", c_i64),
                 ("off_b1", c_i64), ("off_b2", c_i64), ("off_b3", c_i64),
                 ("off_w3row0", c_i64), ("off_tcw1", c_i64), ("off_tcw2", c_i64),
                 ("off_tcw3", c_i64), ("bytes", c_i64)]
@@ -95,7 +93,8 @@ SIGNATURES = {
                                        c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_i32, c_i32, c_vp,
                                        c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
     "angelo_tc_timeouts": (c_i64, [c_i32]),
-    "angelo_tc_gemm_x3": (c_i32, [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp, c_vp]),
+    "angelo_tc_gemm_x3": (c_i32, [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp,
+                                  c_vp]),
     "angelo_adamw_step": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_f32, c_f32, c_f32,
                                   c_f32, c_f32, c_vp]),
     "angelo_radiance_net_bytes": (c_i64, [c_i32]),

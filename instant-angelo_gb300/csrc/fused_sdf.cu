@@ -40,32 +40,23 @@
 using namespace angelo;
 
 // angelo_sdf_net_layout (include/angelo_gb.h): k_tiles1 = first-layer k-tiles
-// (1 + levels/8), n_tiles3 = output n-tiles (width padded to 8), k_tiles3b =
-// output width padded to 16 in k-tiles; byte offsets of the forward and
-// backward B fragments (hi then lo of each), biases and output row 0.
+// of 16 columns (1 + levels/8), n_tiles3 = output width in tiles of 8,
+// k_tiles3b = output width in tiles of 16; byte offsets of the fp32 biases,
+// the fp32 output row 0 and the three tensor-core operands.
 
 namespace {
 
-constexpr int kWarps = 8;
-constexpr int kThreads = kWarps * 32;
 constexpr int kEncThreads = 128;
 constexpr int kState = 16;      // per sample: sdf of the 13 evaluations, shifted point (3)
 constexpr int kBState = 8;      // per sample, backward: dL/dshifted (3), dL/dnormal from curvature (3)
-constexpr int kStageRows = kWarps * 16;
-constexpr int kStageLd = 72;    // bf16 row stride of staged 64-wide operands (conflict-free ldmatrix)
 constexpr uint32_t kAggregateRes = 300;  // levels up to this resolution aggregate their atomics
 
 enum Group { kPoint = 0, kFD = 1, kCurv = 2 };
 
-struct NetSmem {
-    const uint2 *w1f, *w2f, *w3f;  // hi at [0, n), lo at [n, 2n)
-    const float *b1, *b2, *b3;
-};
-
 // ------------------------------------------------------------------- prep
-// Effective fp32 weights (after weight normalisation) -> bf16 hi/lo B
-// fragments.  W1 columns are permuted from the reference order [xyz(3),
-// hash(2L)] to the kernel order [hash(2L), xyz(3), 0...].
+// Effective fp32 weights (after weight normalisation) -> bf16 hi/lo
+// tensor-core operands.  W1 columns are permuted from the reference order
+// [xyz(3), hash(2L)] to the kernel order [hash(2L), xyz(3), 0...].
 
 __device__ __forceinline__ float w1_kernel_col(const float *W1, int in_dim, int n_hash, int n, int k) {
     int src;
@@ -83,69 +74,26 @@ __device__ __forceinline__ float layer_w(int layer, int n, int k, const float *W
     return (n < out_dim && k < 64) ? W3[n * 64 + k] : 0.0f;
 }
 
-__global__ void sdf_prep_kernel(const float *__restrict__ W1, const float *__restrict__ b1,
-                                const float *__restrict__ W2, const float *__restrict__ b2,
-                                const float *__restrict__ W3, const float *__restrict__ b3,
-                                int in_dim, int n_hash, angelo_sdf_net_layout lay,
-                                char *__restrict__ net) {
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = tid & 31;
-    const int r = lane >> 2, c = (lane & 3) * 2;
-    int frag = tid >> 5;
-    // forward fragments: B[k][n] = W[n][k]
-    struct Spec {
-        int layer, kt, nt;
-        int64_t off;
-        bool bwd;
-    };
-    const int K1 = lay.k_tiles1, NT3 = lay.n_tiles3, KT3 = lay.k_tiles3b;
-    const int nh = lay.n_hidden;
-    // enumerate all fragments: fwd L1 (K1 x 8), fwd L2 (4 x 8), fwd L3 (4 x NT3),
-    // bwd L1 (4 x 2*K1), bwd L2 (4 x 8), bwd L3 (KT3 x 8)
-    const int counts[6] = {K1 * 8, nh == 2 ? 32 : 0, 4 * NT3, 4 * 2 * K1, nh == 2 ? 32 : 0, KT3 * 8};
-    int which = 0;
-    while (which < 6 && frag >= counts[which]) frag -= counts[which++];
-    if (which >= 6) {
-        // biases and the fp32 row 0 of the output layer
-        int j = frag * 32 + lane;
-        float *fb1 = reinterpret_cast<float *>(net + lay.off_b1);
-        float *fb2 = reinterpret_cast<float *>(net + lay.off_b2);
-        float *fb3 = reinterpret_cast<float *>(net + lay.off_b3);
-        float *fr0 = reinterpret_cast<float *>(net + lay.off_w3row0);
-        if (j < 64) fb1[j] = b1[j];
-        else if (j < 128) { if (nh == 2) fb2[j - 64] = b2[j - 64]; }
-        else if (j < 128 + 8 * NT3) { const int o = j - 128; fb3[o] = o < lay.out_dim ? b3[o] : 0.f; }
-        else if (j < 192 + 8 * NT3) { const int o = j - 128 - 8 * NT3; fr0[o] = W3[o]; }
-        return;
+// fp32 biases (zero padded) and row 0 of the output layer
+__global__ void sdf_prep_vec_kernel(const float *__restrict__ b1, const float *__restrict__ b2,
+                                    const float *__restrict__ W3, const float *__restrict__ b3,
+                                    angelo_sdf_net_layout lay, char *__restrict__ net) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int NT3 = lay.n_tiles3;
+    float *fb1 = reinterpret_cast<float *>(net + lay.off_b1);
+    float *fb2 = reinterpret_cast<float *>(net + lay.off_b2);
+    float *fb3 = reinterpret_cast<float *>(net + lay.off_b3);
+    float *fr0 = reinterpret_cast<float *>(net + lay.off_w3row0);
+    if (j < 64) {
+        fb1[j] = b1[j];
+    } else if (j < 128) {
+        fb2[j - 64] = lay.n_hidden == 2 ? b2[j - 64] : 0.f;
+    } else if (j < 128 + 8 * NT3) {
+        const int o = j - 128;
+        fb3[o] = o < lay.out_dim ? b3[o] : 0.f;
+    } else if (j < 192 + 8 * NT3) {
+        fr0[j - 128 - 8 * NT3] = W3[j - 128 - 8 * NT3];
     }
-    const int layer = which % 3 + 1;
-    const bool bwd = which >= 3;
-    int NT;
-    int64_t off;
-    if (!bwd) {
-        NT = layer == 3 ? NT3 : 8;
-        off = layer == 1 ? lay.off_w1f : (layer == 2 ? lay.off_w2f : lay.off_w3f);
-    } else {
-        NT = layer == 1 ? 2 * K1 : 8;
-        off = layer == 1 ? lay.off_w1b : (layer == 2 ? lay.off_w2b : lay.off_w3b);
-    }
-    const int kt = frag / NT, nt = frag % NT;
-    const int KT = !bwd ? (layer == 1 ? K1 : 4) : (layer == 3 ? KT3 : 4);
-    float v[4];
-    for (int i = 0; i < 4; ++i) {
-        const int k = kt * 16 + c + (i & 1) + (i >> 1) * 8;  // reg0: k=c,c+1; reg1: k=c+8,c+9
-        const int n = nt * 8 + r;
-        // forward: B[k][n] = W[n][k]; backward (dX = dY W): B[k=out][n=in] = W[k][n]
-        v[i] = !bwd ? layer_w(layer, n, k, W1, W2, W3, in_dim, n_hash, lay.out_dim)
-                    : layer_w(layer, k, n, W1, W2, W3, in_dim, n_hash, lay.out_dim);
-    }
-    const Split s0 = split2(v[0], v[1]);
-    const Split s1 = split2(v[2], v[3]);
-    uint2 *dst = reinterpret_cast<uint2 *>(net + off);
-    const int64_t n_frag = frag_count(KT, NT);
-    const int64_t idx = (int64_t)(kt * NT + nt) * 32 + lane;
-    dst[idx] = make_uint2(s0.hi, s1.hi);
-    dst[n_frag + idx] = make_uint2(s0.lo, s1.lo);
 }
 
 // tcgen05 operands of the three layers (Y = X W^T, kernel column order):
@@ -338,77 +286,6 @@ __global__ void __launch_bounds__(kEncThreads) stencil_encode_kernel(const __gri
             }
             P.X[xidx(P, e0 + k, l, s)] = f;
         }
-    }
-}
-
-// ------------------------------------------------------------ MLP operands
-// A fragments of the first layer for rows g, g+8 of a 16-sample tile: hash
-// levels q + 4j (k-tile j/2, upper half when j is odd) from X, the xyz k-tile
-// (columns 2L + {0,1,2} = x*2-1; q = 0 holds (x, y), q = 1 holds (z, 0)).
-
-template <int KH>
-struct AFrag {
-    uint32_t hi[KH + 1][4];
-    uint32_t lo[KH + 1][4];
-};
-
-template <int KH>
-__device__ __forceinline__ void load_x(const SdfParams &P, int e, int64_t s0, bool v0, bool v1, int lane,
-                                       const float xc0[3], const float xc1[3], AFrag<KH> &A) {
-    const int g = lane >> 2, q = lane & 3;
-#pragma unroll
-    for (int j = 0; j < 2 * KH; ++j) {
-        const int l = q + 4 * j;
-        float2 f0 = make_float2(0.f, 0.f), f1 = make_float2(0.f, 0.f);
-        if (l < P.active) {
-            if (v0) f0 = __ldg(P.X + xidx(P, e, l, s0 + g));
-            if (v1) f1 = __ldg(P.X + xidx(P, e, l, s0 + g + 8));
-        }
-        const Split a = split2(f0.x, f0.y), b = split2(f1.x, f1.y);
-        const int kt = j >> 1, h = (j & 1) * 2;
-        A.hi[kt][h] = a.hi;
-        A.lo[kt][h] = a.lo;
-        A.hi[kt][h + 1] = b.hi;
-        A.lo[kt][h + 1] = b.lo;
-    }
-    float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
-    if (q == 0) {
-        a0 = x2m1(xc0[0]);
-        a1 = x2m1(xc0[1]);
-        b0 = x2m1(xc1[0]);
-        b1 = x2m1(xc1[1]);
-    } else if (q == 1) {
-        a0 = x2m1(xc0[2]);
-        b0 = x2m1(xc1[2]);
-    }
-    const Split sa = split2(a0, a1), sb = split2(b0, b1);
-    A.hi[KH][0] = sa.hi;
-    A.lo[KH][0] = sa.lo;
-    A.hi[KH][1] = sb.hi;
-    A.lo[KH][1] = sb.lo;
-    A.hi[KH][2] = A.hi[KH][3] = A.lo[KH][2] = A.lo[KH][3] = 0u;
-}
-
-// Output layer restricted to the first NTO n-tiles
-template <int NTO>
-__device__ __forceinline__ void out_layer(const uint32_t (&hh)[4][4], const uint32_t (&hl)[4][4],
-                                          const uint2 *wf, int NT3, const float *bias, int lane,
-                                          float (&D)[NTO][4]) {
-    const int c = (lane & 3) * 2;
-    const int64_t n_frag = frag_count(4, NT3);
-#pragma unroll
-    for (int nt = 0; nt < NTO; ++nt) {
-        D[nt][0] = D[nt][1] = D[nt][2] = D[nt][3] = 0.f;
-#pragma unroll
-        for (int kt = 0; kt < 4; ++kt) {
-            const int64_t i = (int64_t)(kt * NT3 + nt) * 32 + lane;
-            mma_x3(D[nt], hh[kt], hl[kt], wf[i], wf[n_frag + i]);
-        }
-        const float b0 = bias[nt * 8 + c], b1 = bias[nt * 8 + c + 1];
-        D[nt][0] += b0;
-        D[nt][1] += b1;
-        D[nt][2] += b0;
-        D[nt][3] += b1;
     }
 }
 
@@ -716,445 +593,485 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
     if (warp == 0) tc::tmem_dealloc(tmem, Sh::tmem_cols);
 }
 
-// -------------------------------------------------------------- MLP backward
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void ldsm_x4_t(uint32_t (&r)[4], const void *p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(smem_u32(p)));
-}
-
-__device__ __forceinline__ void ldsm_x2_t(uint32_t (&r)[2], const void *p) {
-    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
-                 : "=r"(r[0]), "=r"(r[1])
-                 : "r"(smem_u32(p)));
-}
-
-// Store split A fragments (KT k-tiles, rows g and g+8 of this warp's 16) into
-// row-major bf16 staging arrays hi/lo with row stride ld.
-template <int KT>
-__device__ __forceinline__ void stage_a(const uint32_t (&h)[KT][4], const uint32_t (&l)[KT][4], uint16_t *hi,
-                                        uint16_t *lo, int ld, int row0, int lane) {
-    const int g = lane >> 2, c = (lane & 3) * 2;
-#pragma unroll
-    for (int kt = 0; kt < KT; ++kt) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            const int row = row0 + g + ((i & 1) << 3);
-            const int col = kt * 16 + ((i >> 1) << 3) + c;
-            *reinterpret_cast<uint32_t *>(hi + row * ld + col) = h[kt][i];
-            *reinterpret_cast<uint32_t *>(lo + row * ld + col) = l[kt][i];
-        }
-    }
-}
-
-// acc[i] += dZ^T B over the kStageRows staged rows, for output tile (mt, nt0 + i):
-// A = dZ^T (m = unit, k = row) read transposed from the row-major dZ staging,
-// B (k = row, n = input column) read transposed from the row-major input staging.
-template <int NTW>
-__device__ __forceinline__ void staged_dw(float (&acc)[NTW][4], const uint16_t *zh, const uint16_t *zl,
-                                          const uint16_t *bh, const uint16_t *bl, int ldb, int mt, int nt0,
-                                          int lane) {
-    const int i8 = lane >> 3, j8 = lane & 7;
-#pragma unroll 2
-    for (int k0 = 0; k0 < kStageRows; k0 += 16) {
-        const int arow = k0 + j8 + ((i8 >> 1) << 3), acol = mt * 16 + ((i8 & 1) << 3);
-        uint32_t ah[4], al[4];
-        ldsm_x4_t(ah, zh + arow * kStageLd + acol);
-        ldsm_x4_t(al, zl + arow * kStageLd + acol);
-        const int brow = k0 + j8 + ((i8 & 1) << 3);
-#pragma unroll
-        for (int i = 0; i < NTW; ++i) {
-            uint32_t b_h[2], b_l[2];
-            ldsm_x2_t(b_h, bh + brow * ldb + (nt0 + i) * 8);
-            ldsm_x2_t(b_l, bl + brow * ldb + (nt0 + i) * 8);
-            mma_x3(acc[i], ah, al, make_uint2(b_h[0], b_h[1]), make_uint2(b_l[0], b_l[1]));
-        }
-    }
-}
-
-struct BwdWarp {
-    float base[16][3];
-    float ds[16][13];   // dL/d(sdf) of each evaluation
-};
-
-struct BwdSmem {
-    const uint2 *w1f, *w2f, *w1b, *w2b, *w3b;
-    const float *b1, *b2, *w3row0;
-    float *dW3, *db1, *db2, *db3;  // shared fp32 accumulators, kernel order
-    uint16_t *zh, *zl, *bh, *bl;   // staging
-};
+// ------------------------------------------------------ MLP backward (tcgen05)
+// A CTA of 16 warps owns 128 consecutive samples through every evaluation of
+// the group, with the forward kernel's thread layout (row r = tensor-memory
+// lane r, four threads per row, one 16-column slice each).  Per evaluation
+// the forward is recomputed and the backward runs as tensor-core rounds:
+//
+//   Z1 = X W1^T                     (two hidden layers:)  Z2 = H1 W2^T
+//   dH of the last hidden layer: dY W3 for the point (a product), ds w3row0
+//   for a stencil tap (rank one, in registers)
+//   dH1 = dZ2 W2,  dW2 += dZ2^T H1,  db2 += dZ2^T 1
+//   dX = dZ1 W1,   dW1 += dZ1^T X,   db1 += dZ1^T 1,  point: dW3^T += H^T dY
+//
+// A stencil tap adds ds H to row 0 of dW3 in fp32 (a warp reduce-scatter over
+// the rows): the taps come in +h / -h pairs whose sum cancels to the
+// difference of two nearby activations, which bf16x3 operands would resolve
+// only to ~2^-17 of the activation.
+// Each activation is staged once as a bf16 hi/lo K-major [sample][column]
+// operand; the same bytes are the MN-major operand of the weight-gradient
+// products over the 128 samples.  The weight gradients and the bias sums stay
+// in tensor memory (M = 64 accumulators) for the CTA's whole loop and are
+// added to the global gradient once.  Every round commits the product the
+// next epilogue reads to mbarrier 0 and the weight-gradient products to
+// mbarrier 1, so the epilogue overlaps them; operands are rewritten only after
+// mbarrier 1 completed.
 
 template <int KH, int NH, int NT3>
-struct BwdShape {
-    static constexpr int KT3 = (NT3 + 1) / 2;
-    static constexpr int XS = 16 * (KH + 1) + 8;      // staged input row stride (bf16)
-    static constexpr int OUTP = 16 * KT3;
-    static constexpr int64_t w1f = 2 * (KH + 1) * 8 * 32 * 8;
-    static constexpr int64_t w2f = NH == 2 ? 2 * 4 * 8 * 32 * 8 : 0;
-    static constexpr int64_t w1b = 2 * 4 * (2 * (KH + 1)) * 32 * 8;
-    static constexpr int64_t w2b = NH == 2 ? 2 * 4 * 8 * 32 * 8 : 0;
-    static constexpr int64_t w3b = 2 * KT3 * 8 * 32 * 8;
-    static constexpr int64_t vec = (3 * 64) * 4;
-    static constexpr int64_t acc = (OUTP * 64 + 64 + 64 + OUTP) * 4;
-    static constexpr int64_t stage1 = (int64_t)kStageRows * (kStageLd + XS) * 2 * 2;
-    static constexpr int64_t stage2 = NH == 2 ? (int64_t)kStageRows * (kStageLd + kStageLd) * 2 * 2 : 0;
-    static constexpr int64_t stage = stage1 > stage2 ? stage1 : stage2;
-    static constexpr int64_t off_w2f = w1f, off_w1b = off_w2f + w2f, off_w2b = off_w1b + w1b,
-                             off_w3b = off_w2b + w2b, off_vec = off_w3b + w3b, off_acc = off_vec + vec,
-                             off_stage = (off_acc + acc + 15) / 16 * 16, off_warp = off_stage + stage;
-    static constexpr int64_t bytes = off_warp + kWarps * sizeof(BwdWarp);
+struct TcBwdShape {
+    static constexpr int K1 = 16 * (KH + 1);
+    static constexpr int N3 = 16 * ((NT3 + 1) / 2);
+    // bytes of one (hi or lo) half of each operand
+    static constexpr uint32_t w1 = 64 * K1 * 2, w2 = NH == 2 ? 64 * 64 * 2 : 0, w3 = N3 * 64 * 2;
+    static constexpr uint32_t x = 128 * K1 * 2, h = 128 * 64 * 2, y = 128 * N3 * 2, ones = 128 * 16 * 2;
+    static constexpr uint32_t off_w1 = 0, off_w2 = off_w1 + 2 * w1, off_w3 = off_w2 + 2 * w2,
+                              off_x = off_w3 + 2 * w3,
+                              off_h1 = off_x + 2 * x,                        // H1, then dZ1 (two layers)
+                              off_h2 = off_h1 + 2 * h,                       // H2 (two layers)
+                              off_z = off_h2 + (NH == 2 ? 2 * h : 0),        // dZ of the last layer
+                              off_y = off_z + 2 * h,                         // dY
+                              off_ones = off_y + 2 * y,                      // column 0 = 1, hi only
+                              off_vec = off_ones + ones,                     // b1, b2, W3 row 0
+                              off_ds = off_vec + 3 * 64 * 4,                 // dL/dsdf [7][128]
+                              off_db3 = off_ds + 7 * 128 * 4,
+                              off_w3g = off_db3 + N3 * 4,                    // taps' dW3 row 0
+                              off_bar = off_w3g + 64 * 4, bytes = off_bar + 32;
+    // tensor-memory columns: per evaluation A, B; CTA-resident gradients
+    static constexpr uint32_t tA = 0, tB = 64, tW1 = 128, tW2 = tW1 + K1, tW3 = tW2 + (NH == 2 ? 64 : 0),
+                              tb1 = tW3 + N3, tb2 = tb1 + 16, used = tb2 + (NH == 2 ? 16 : 0),
+                              tmem_cols = used <= 256 ? 256 : 512;
 };
 
-template <int KH, int NH, int NT3, int GROUP>
-__global__ void __launch_bounds__(kThreads, 1) sdf_mlp_bwd_kernel(const __grid_constant__ SdfParams P) {
-    using Sh = BwdShape<KH, NH, NT3>;
-    constexpr int KT3 = Sh::KT3;
-    extern __shared__ __align__(1024) char smem[];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const angelo_sdf_net_layout &nl = P.nl;
-    auto copy16 = [&](int64_t dst, int64_t src, int64_t bytes) {
-        for (int64_t i = tid * 16; i < bytes; i += kThreads * 16)
-            *reinterpret_cast<uint4 *>(smem + dst + i) = *reinterpret_cast<const uint4 *>(P.net + src + i);
-    };
-    copy16(0, nl.off_w1f, Sh::w1f);
-    if (NH == 2) copy16(Sh::off_w2f, nl.off_w2f, Sh::w2f);
-    copy16(Sh::off_w1b, nl.off_w1b, Sh::w1b);
-    if (NH == 2) copy16(Sh::off_w2b, nl.off_w2b, Sh::w2b);
-    if (GROUP != kCurv) copy16(Sh::off_w3b, nl.off_w3b, Sh::w3b);
-    float *vec = reinterpret_cast<float *>(smem + Sh::off_vec);
-    for (int i = tid; i < 64; i += kThreads) {
-        vec[i] = reinterpret_cast<const float *>(P.net + nl.off_b1)[i];
-        vec[64 + i] = NH == 2 ? reinterpret_cast<const float *>(P.net + nl.off_b2)[i] : 0.f;
-        vec[128 + i] = reinterpret_cast<const float *>(P.net + nl.off_w3row0)[i];
-    }
-    float *acc = reinterpret_cast<float *>(smem + Sh::off_acc);
-    const int n_acc = Sh::OUTP * 64 + 64 + 64 + Sh::OUTP;
-    for (int i = tid; i < n_acc; i += kThreads) acc[i] = 0.f;
-    BwdSmem S;
-    S.w1f = reinterpret_cast<const uint2 *>(smem);
-    S.w2f = reinterpret_cast<const uint2 *>(smem + Sh::off_w2f);
-    S.w1b = reinterpret_cast<const uint2 *>(smem + Sh::off_w1b);
-    S.w2b = reinterpret_cast<const uint2 *>(smem + Sh::off_w2b);
-    S.w3b = reinterpret_cast<const uint2 *>(smem + Sh::off_w3b);
-    S.b1 = vec;
-    S.b2 = vec + 64;
-    S.w3row0 = vec + 128;
-    S.dW3 = acc;
-    S.db1 = acc + Sh::OUTP * 64;
-    S.db2 = S.db1 + 64;
-    S.db3 = S.db2 + 64;
-    // staging: phase 2 (two hidden layers) dZ2 | H1, phase 1 dZ1 | X
-    uint16_t *zh = reinterpret_cast<uint16_t *>(smem + Sh::off_stage);
-    uint16_t *zl = zh + kStageRows * kStageLd;
-    uint16_t *b1h = zl + kStageRows * kStageLd, *b1l = b1h + kStageRows * Sh::XS;
-    uint16_t *b2h = b1h, *b2l = b2h + kStageRows * kStageLd;
-    BwdWarp &ws = reinterpret_cast<BwdWarp *>(smem + Sh::off_warp)[warp];
-    __syncthreads();
+// an operand staged as bf16 [rows][C] (kmajor_offset(r, c, C)), hi and lo
+// halves `half` bytes apart, as the descriptor fields of one K step of 16
+struct TcOp {
+    uint32_t hi, lo, lbo, sbo, step;
+};
+// read K-major: K = C, M (or N) = rows
+__device__ __forceinline__ TcOp op_k(uint32_t hi, uint32_t half, int C) {
+    return TcOp{hi, hi + half, 128u, 16u * (uint32_t)C, 256u};
+}
+// read as the transposed operand (MN-major): M (or N) = C, K = rows
+__device__ __forceinline__ TcOp op_t(uint32_t hi, uint32_t half, int C) {
+    return TcOp{hi, hi + half, 16u * (uint32_t)C, 128u, 32u * (uint32_t)C};
+}
 
-    // dW tiles owned by this warp: unit block mt = warp / 2, n-tiles nt1 ..
-    // nt1 + KH of the first layer and nt2 .. nt2 + 3 of the second
-    const int mt = warp >> 1, nt1 = (warp & 1) * (KH + 1), nt2 = (warp & 1) * 4;
-    float acc1[KH + 1][4], acc2[4][4];
+// D (+)= A B^T over KSTEPS steps of 16 in bf16x3 (lo*hi + hi*lo + hi*hi); with
+// b_exact, B is exact in bf16 and its lo product is left out.  One thread.
+template <int KSTEPS>
+__device__ __forceinline__ void tc_mma(uint32_t d, const TcOp &a, const TcOp &b, uint32_t idesc, bool acc,
+                                       bool b_exact = false) {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int ks = 0; ks < KSTEPS; ++ks) {
+        const uint64_t ah = tc::smem_desc(a.hi + ks * a.step, a.lbo, a.sbo);
+        const uint64_t al = tc::smem_desc(a.lo + ks * a.step, a.lbo, a.sbo);
+        const uint64_t bh = tc::smem_desc(b.hi + ks * b.step, b.lbo, b.sbo);
+        tc::mma_bf16(d, al, bh, idesc, (acc || ks > 0) ? 1u : 0u);
+        if (!b_exact) tc::mma_bf16(d, ah, tc::smem_desc(b.lo + ks * b.step, b.lbo, b.sbo), idesc, 1u);
+        tc::mma_bf16(d, ah, bh, idesc, 1u);
+    }
+}
+
+// Column sums over the warp's 32 lanes of v[0..15] (lane = row): afterwards
+// lanes 2c and 2c + 1 hold the sum of column col(2c), 16 shuffles.
+__device__ __forceinline__ float warp_colsum16(const float (&v)[16], int lane, int *col) {
+    float a[8], b[4], c[2];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            if (i < KH + 1) acc1[i][j] = 0.f;
-            acc2[i][j] = 0.f;
+    for (int j = 0; j < 8; ++j) {
+        const bool up = lane & 16;
+        const float keep = up ? v[j + 8] : v[j], send = up ? v[j] : v[j + 8];
+        a[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const bool up = lane & 8;
+        const float keep = up ? a[j + 4] : a[j], send = up ? a[j] : a[j + 4];
+        b[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+        const bool up = lane & 4;
+        const float keep = up ? b[j + 2] : b[j], send = up ? b[j] : b[j + 2];
+        c[j] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
+    }
+    const bool up = lane & 2;
+    float r = (up ? c[1] : c[0]) + __shfl_xor_sync(0xffffffffu, up ? c[0] : c[1], 2);
+    r += __shfl_xor_sync(0xffffffffu, r, 1);
+    *col = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+    return r;
+}
+
+// dL/dsdf of the evaluations of GROUP of sample s (ds[e - e0]), from the
+// incoming gradients and the stencil state kept by the forward; the curvature
+// group stores dL/dnormal of the curvature for the FD pass (bstate 3..5).
+template <int GROUP>
+__device__ __forceinline__ void sample_ds(const SdfParams &P, int64_t s, float (&ds)[7]) {
+    const float r_ = P.radius, eps = P.eps;
+    const float *st = P.state + s * kState;
+#pragma unroll
+    for (int i = 0; i < 7; ++i) ds[i] = 0.f;
+    if (GROUP == kCurv) {
+        // curvature (models/geometry.py:247-251) back to the six
+        // shifted-stencil SDFs
+        float gr[3], gs[3], n[3], ns[3], dns[3], dgs[3];
+        const float gn = fd_grad(st + 1, eps, gr);
+        const float gsn = fd_grad(st + 7, eps, gs);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            n[d] = gr[d] / fmaxf(gn, 1e-12f);
+            ns[d] = gs[d] / fmaxf(gsn, 1e-12f);
+        }
+        const float dot = n[0] * ns[0] + n[1] * ns[1] + n[2] * ns[2];
+        const float lo = -1.0f + 1e-6f, hi = 1.0f - 1e-6f;
+        const float dotc = fminf(fmaxf(dot, lo), hi);
+        const float dang = P.g_laplace ? P.g_laplace[s] / 3.14159265358979f : 0.f;
+        const float ddot = (dot >= lo && dot <= hi) ? -dang / sqrtf(1.0f - dotc * dotc) : 0.f;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            P.bstate[s * kBState + 3 + d] = ddot * ns[d];
+            dns[d] = ddot * n[d];
+        }
+        normalize_bwd(gs, gsn, ns, dns, dgs);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float h = coincident_taps(st[13 + d], r_, eps) ? 0.f : __fdiv_rn(0.5f * dgs[d], eps);
+            ds[2 * d] = h;
+            ds[2 * d + 1] = -h;
+        }
+        return;
+    }
+    ds[0] = P.g_sdf ? P.g_sdf[s] : 0.f;
+    if (GROUP == kFD) {
+        // FD gradient (and, with curvature, the normal that set the tangent
+        // shift) back to the six stencil SDFs
+        float gr[3], n[3], dn[3] = {0.f, 0.f, 0.f}, dg[3];
+        const float gn = fd_grad(st + 1, eps, gr);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) n[d] = gr[d] / fmaxf(gn, 1e-12f);
+        if (P.with_laplace) {
+            const float *rd = P.rdir + s * 3;
+            const float *bs = P.bstate + s * kBState;
+            const float rn = fmaxf(sqrtf(rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2]), 1e-12f);
+            float rdn[3], dtg[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                rdn[d] = rd[d] / rn;
+                dtg[d] = bs[d] * eps;
+                dn[d] = bs[3 + d];
+            }
+            // t = n x rd  ->  dL/dn += rd x dL/dt
+            dn[0] += rdn[1] * dtg[2] - rdn[2] * dtg[1];
+            dn[1] += rdn[2] * dtg[0] - rdn[0] * dtg[2];
+            dn[2] += rdn[0] * dtg[1] - rdn[1] * dtg[0];
+        }
+        normalize_bwd(gr, gn, n, dn, dg);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float gin = P.g_grad ? P.g_grad[s * 3 + d] : 0.f;
+            const float h = coincident_taps(P.pos[s * 3 + d], r_, eps) ? 0.f : __fdiv_rn(0.5f * (dg[d] + gin), eps);
+            ds[1 + 2 * d] = h;
+            ds[2 + 2 * d] = -h;
         }
     }
+}
+
+template <int KH, int NH, int NT3, int GROUP>
+__global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __grid_constant__ SdfParams P) {
+    using Sh = TcBwdShape<KH, NH, NT3>;
+    constexpr int K1 = Sh::K1, N3 = Sh::N3;
+    extern __shared__ __align__(1024) char smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int row = (warp & 3) * 32 + lane, slice = warp >> 2;   // row of the tile, 16-column slice
+    const angelo_sdf_net_layout &nl = P.nl;
+    auto copy16 = [&](uint32_t dst, int64_t src, uint32_t bytes) {
+        for (uint32_t i = tid * 16; i < bytes; i += kTcThreads * 16)
+            *reinterpret_cast<uint4 *>(smem + dst + i) = *reinterpret_cast<const uint4 *>(P.net + src + i);
+    };
+    copy16(Sh::off_w1, nl.off_tcw1, 2 * Sh::w1);
+    if (NH == 2) copy16(Sh::off_w2, nl.off_tcw2, 2 * Sh::w2);
+    copy16(Sh::off_w3, nl.off_tcw3, 2 * Sh::w3);
+    float *vec = reinterpret_cast<float *>(smem + Sh::off_vec);   // b1 [64], b2 [64], W3 row 0 [64]
+    for (int i = tid; i < 192; i += kTcThreads) {
+        float v;
+        if (i < 64) v = reinterpret_cast<const float *>(P.net + nl.off_b1)[i];
+        else if (i < 128) v = NH == 2 ? reinterpret_cast<const float *>(P.net + nl.off_b2)[i - 64] : 0.f;
+        else v = reinterpret_cast<const float *>(P.net + nl.off_w3row0)[i - 128];
+        vec[i] = v;
+    }
+    uint16_t *ones = reinterpret_cast<uint16_t *>(smem + Sh::off_ones);
+    for (int i = tid; i < 128 * 16; i += kTcThreads)
+        ones[tc::kmajor_offset(i >> 4, i & 15, 16) >> 1] = (i & 15) == 0 ? (uint16_t)0x3F80u : (uint16_t)0u;
+    float *ds = reinterpret_cast<float *>(smem + Sh::off_ds);
+    float *db3 = reinterpret_cast<float *>(smem + Sh::off_db3);
+    for (int i = tid; i < N3; i += kTcThreads) db3[i] = 0.f;
+    float *w3g = reinterpret_cast<float *>(smem + Sh::off_w3g);
+    for (int i = tid; i < 64; i += kTcThreads) w3g[i] = 0.f;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + Sh::off_bar);   // [0] epilogue, [1] round
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 2);
+    char *xh = smem + Sh::off_x, *xl = xh + Sh::x, *h1h = smem + Sh::off_h1, *h1l = h1h + Sh::h;
+    char *h2h = smem + Sh::off_h2, *h2l = h2h + Sh::h, *zh = smem + Sh::off_z, *zl = zh + Sh::h;
+    char *yh = smem + Sh::off_y, *yl = yh + Sh::y;
+    if (warp == 0) {
+        tc::tmem_alloc(slot, Sh::tmem_cols);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+    }
+    tc_publish();
+    const uint32_t tmem = *slot;
+    const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+    // the CTA-resident gradient accumulators start at zero
+    for (uint32_t b = slice; b < (Sh::used - Sh::tW1) / 16; b += 4) tc::st16_zero(tmem + lane_off + Sh::tW1 + 16 * b);
+    tc_publish();
+
+    const uint32_t sW1 = tc::smem_addr(smem + Sh::off_w1), sW2 = tc::smem_addr(smem + Sh::off_w2),
+                   sW3 = tc::smem_addr(smem + Sh::off_w3), sX = tc::smem_addr(xh), sH1 = tc::smem_addr(h1h),
+                   sH2 = tc::smem_addr(h2h), sZ = tc::smem_addr(zh), sY = tc::smem_addr(yh),
+                   sOnes = tc::smem_addr(ones);
+    const TcOp W1k = op_k(sW1, Sh::w1, K1), W1t = op_t(sW1, Sh::w1, K1);
+    const TcOp W2k = op_k(sW2, Sh::w2, 64), W2t = op_t(sW2, Sh::w2, 64), W3t = op_t(sW3, Sh::w3, 64);
+    const TcOp Xk = op_k(sX, Sh::x, K1), Xt = op_t(sX, Sh::x, K1);
+    const TcOp H1k = op_k(sH1, Sh::h, 64), H1t = op_t(sH1, Sh::h, 64), H2t = op_t(sH2, Sh::h, 64);
+    const TcOp Zk = op_k(sZ, Sh::h, 64), Zt = op_t(sZ, Sh::h, 64);
+    const TcOp Yk = op_k(sY, Sh::y, N3), Yt = op_t(sY, Sh::y, N3), Ones = op_t(sOnes, 0u, 16);
+    // dZ1 lives in the H1 staging with two hidden layers, in the dZ staging with one
+    const TcOp D1k = NH == 2 ? H1k : Zk, D1t = NH == 2 ? H1t : Zt, HLt = NH == 2 ? H2t : H1t;
+    constexpr uint32_t id_fwd = tc::idesc_bf16_f32(128, 64);
+    constexpr uint32_t id_dh = tc::idesc_bf16_f32(128, 64, 0, 1), id_dx = tc::idesc_bf16_f32(128, K1, 0, 1);
+    constexpr uint32_t id_w1 = tc::idesc_bf16_f32(64, K1, 1, 1), id_w2 = tc::idesc_bf16_f32(64, 64, 1, 1);
+    constexpr uint32_t id_w3 = tc::idesc_bf16_f32(64, N3, 1, 1), id_16 = tc::idesc_bf16_f32(64, 16, 1, 1);
 
     constexpr int e0 = GROUP == kCurv ? 7 : 0;
     constexpr int ne = GROUP == kPoint ? 1 : (GROUP == kFD ? 7 : 6);
-    const int g = lane >> 2, q = lane & 3, c = q * 2;
     const float r_ = P.radius, eps = P.eps;
     const float inv2r = 1.0f / __fsub_rn(r_, -r_);
-    const int64_t n_tiles = (P.S + 15) / 16;
-    // CTA-uniform loop (the staged dW GEMM synchronises the CTA); tiles past
-    // the end have no valid rows and contribute zeros
-    for (int64_t tb = (int64_t)blockIdx.x * kWarps; tb < n_tiles; tb += (int64_t)gridDim.x * kWarps) {
-        const int64_t s0 = (tb + warp) * 16;
-        if (lane < 16) {
-            const int64_t s = s0 + lane;
-            const bool v = s < P.S;
-            const float *st = P.state + s * kState;
-            const float *src = GROUP == kCurv ? st + 13 : P.pos + s * 3;
+    const int od = nl.out_dim;
+    uint32_t ph0 = 0, ph1 = 0;
+    bool alive = true;
+    const int64_t n_tiles = (P.S + 127) / 128;
+    const int64_t my_tiles = (int64_t)blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const int64_t n_items = my_tiles * ne;
+    float g1[16];            // softplus' of this thread's layer-1 slice, kept for dZ1
+    float dsh[3] = {0.f, 0.f, 0.f};
+    for (int64_t k = 0; k < n_items; ++k) {
+        const int64_t s = (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row;
+        const bool v = s < P.S;
+        const int i = (int)(k % ne), e = e0 + i;
+        const bool point = GROUP != kCurv && e == 0;
+        float base[3], xc[3];
+        int m;
+        {
+            const float *src = GROUP == kCurv ? P.state + s * kState + 13 : P.pos + s * 3;
 #pragma unroll
-            for (int d = 0; d < 3; ++d) ws.base[lane][d] = v ? src[d] : 0.f;
-            for (int e = 0; e < 13; ++e) ws.ds[lane][e] = 0.f;
-            if (v && GROUP == kCurv) {
-                // curvature (models/geometry.py:247-251) back to the six
-                // shifted-stencil SDFs; dL/dnormal from it kept for the FD pass
-                float gr[3], gs[3], n[3], ns[3], dns[3], dgs[3];
-                const float gn = fd_grad(st + 1, eps, gr);
-                const float gsn = fd_grad(st + 7, eps, gs);
+            for (int d = 0; d < 3; ++d) base[d] = v ? src[d] : 0.f;
+        }
+        tap_point(r_, eps, base, e, xc, &m);
+        // layer-1 operand (slice q < KH: hash levels 8q .. 8q + 7; slice KH:
+        // xyz), loaded while the previous evaluation's last products run
+        float xv[16];
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    n[d] = gr[d] / fmaxf(gn, 1e-12f);
-                    ns[d] = gs[d] / fmaxf(gsn, 1e-12f);
-                }
-                const float dot = n[0] * ns[0] + n[1] * ns[1] + n[2] * ns[2];
-                const float lo = -1.0f + 1e-6f, hi = 1.0f - 1e-6f;
-                const float dotc = fminf(fmaxf(dot, lo), hi);
-                const float dang = P.g_laplace ? P.g_laplace[s] / 3.14159265358979f : 0.f;
-                const float ddot = (dot >= lo && dot <= hi) ? -dang / sqrtf(1.0f - dotc * dotc) : 0.f;
+        for (int j = 0; j < 16; ++j) xv[j] = 0.f;
+        if (slice < KH) {
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    P.bstate[s * kBState + 3 + d] = ddot * ns[d];
-                    dns[d] = ddot * n[d];
-                }
-                normalize_bwd(gs, gsn, ns, dns, dgs);
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    const float h = coincident_taps(st[13 + d], r_, eps) ? 0.f : __fdiv_rn(0.5f * dgs[d], eps);
-                    ws.ds[lane][7 + 2 * d] = h;
-                    ws.ds[lane][8 + 2 * d] = -h;
-                }
+            for (int j = 0; j < 8; ++j) {
+                const int l = 8 * slice + j;
+                const float2 f = (v && l < P.active) ? __ldg(P.X + xidx(P, e, l, s)) : make_float2(0.f, 0.f);
+                xv[2 * j] = f.x;
+                xv[2 * j + 1] = f.y;
             }
-            if (v && GROUP != kCurv) {
-                ws.ds[lane][0] = P.g_sdf ? P.g_sdf[s] : 0.f;
-                if (GROUP == kFD) {
-                    // FD gradient (and, with curvature, the normal that set the
-                    // tangent shift) back to the six stencil SDFs
-                    float gr[3], n[3], dn[3] = {0.f, 0.f, 0.f}, dg[3];
-                    const float gn = fd_grad(st + 1, eps, gr);
+        } else if (slice == KH) {
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) n[d] = gr[d] / fmaxf(gn, 1e-12f);
-                    if (P.with_laplace) {
-                        const float *rd = P.rdir + s * 3;
-                        const float *bs = P.bstate + s * kBState;
-                        const float rn = fmaxf(sqrtf(rd[0] * rd[0] + rd[1] * rd[1] + rd[2] * rd[2]), 1e-12f);
-                        float rdn[3], dtg[3];
+            for (int d = 0; d < 3; ++d) xv[d] = x2m1(xc[d]);
+        }
+        if (k > 0) {
+            if (!(alive = tc_wait_all(&bar[1], ph1))) break;
+            ph1 ^= 1;
+        }
+        if (slice <= KH) stage16(xh, xl, row, 16 * slice, K1, xv);
+        if (i == 0) {
+            if (slice == 0) {
+                float d7[7];
+                if (v) sample_ds<GROUP>(P, s, d7);
+                else
+                    for (int j = 0; j < 7; ++j) d7[j] = 0.f;
+                for (int j = 0; j < ne; ++j) ds[j * 128 + row] = d7[j];
+            }
+            dsh[0] = dsh[1] = dsh[2] = 0.f;
+        }
+        if (point) {
+            // dY: the output row's gradient (dL/dfeature, column 0 also dL/dsdf)
+            // and its column sums (db3)
+            const float d0 = v && P.g_sdf ? P.g_sdf[s] : 0.f;
+            for (int q = slice; q < N3 / 16; q += 4) {
+                float yv[16];
 #pragma unroll
-                        for (int d = 0; d < 3; ++d) {
-                            rdn[d] = rd[d] / rn;
-                            dtg[d] = bs[d] * eps;
-                            dn[d] = bs[3 + d];
-                        }
-                        // t = n x rd  ->  dL/dn += rd x dL/dt
-                        dn[0] += rdn[1] * dtg[2] - rdn[2] * dtg[1];
-                        dn[1] += rdn[2] * dtg[0] - rdn[0] * dtg[2];
-                        dn[2] += rdn[0] * dtg[1] - rdn[1] * dtg[0];
-                    }
-                    normalize_bwd(gr, gn, n, dn, dg);
+                for (int j = 0; j < 16; ++j) {
+                    const int col = 16 * q + j;
+                    float g = (v && col < od && P.g_feature) ? P.g_feature[s * P.gfeat_stride + col] : 0.f;
+                    if (col == 0) g += d0;
+                    yv[j] = g;
+                }
+                stage16(yh, yl, row, 16 * q, N3, yv);
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        const float gin = P.g_grad ? P.g_grad[s * 3 + d] : 0.f;
-                        const float h = coincident_taps(P.pos[s * 3 + d], r_, eps)
-                                            ? 0.f
-                                            : __fdiv_rn(0.5f * (dg[d] + gin), eps);
-                        ws.ds[lane][1 + 2 * d] = h;
-                        ws.ds[lane][2 + 2 * d] = -h;
-                    }
+                for (int j = 0; j < 16; ++j) {
+                    float a = yv[j];
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+                    if (lane == 0 && a != 0.f) red_add(db3 + 16 * q + j, a);
                 }
             }
         }
-        __syncwarp();
-        const bool v0 = s0 + g < P.S, v1 = s0 + g + 8 < P.S;
-        float dsh0[3] = {0.f, 0.f, 0.f}, dsh1[3] = {0.f, 0.f, 0.f};
-#pragma unroll 1
-        for (int i = 0; i < ne; ++i) {
-            const int e = e0 + i;
-            float xc0[3], xc1[3];
-            int m0, m1;
-            tap_point(r_, eps, ws.base[g], e, xc0, &m0);
-            tap_point(r_, eps, ws.base[g + 8], e, xc1, &m1);
-            AFrag<KH> X;
-            load_x<KH>(P, e, s0, v0, v1, lane, xc0, xc1, X);
-            // recompute the activations
-            float Z1[8][4];
-            hidden_layer<KH + 1>(X.hi, X.lo, S.w1f, S.b1, lane, Z1);
-            uint32_t h1h[4][4], h1l[4][4];
-            activate(Z1, h1h, h1l);
-            float Z2[8][4];
-            uint32_t h2h[4][4], h2l[4][4];
-            if (NH == 2) {
-                hidden_layer<4>(h1h, h1l, S.w2f, S.b2, lane, Z2);
-                activate(Z2, h2h, h2l);
+        tc_publish();
+        // round 1: Z1 (one hidden layer, point: also dH1 = dY W3)
+        if (tid == 0) {
+            tc_mma<K1 / 16>(tmem + Sh::tA, Xk, W1k, id_fwd, false);
+            if (NH == 1 && point) tc_mma<N3 / 16>(tmem + Sh::tB, Yk, W3t, id_dh, false);
+            tc::commit(&bar[0]);
+        }
+        if (!(alive = tc_wait_all(&bar[0], ph0))) break;
+        ph0 ^= 1;
+        float hl[16];   // this slice of the last hidden layer's activations
+        {
+            float z[16];
+            tc::ld16(tmem + lane_off + Sh::tA + 16 * slice, z);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) softplus100_both(z[j] + vec[16 * slice + j], &hl[j], &g1[j]);
+            stage16(h1h, h1l, row, 16 * slice, 64, hl);
+        }
+        if (NH == 2) {
+            tc_publish();
+            // round 2: Z2 (point: also dH2 = dY W3)
+            if (tid == 0) {
+                tc_mma<4>(tmem + Sh::tB, H1k, W2k, id_fwd, false);
+                if (point) tc_mma<N3 / 16>(tmem + Sh::tA, Yk, W3t, id_dh, false);
+                tc::commit(&bar[0]);
             }
-            const uint32_t(&hlh)[4][4] = NH == 2 ? h2h : h1h;
-            const uint32_t(&hll)[4][4] = NH == 2 ? h2l : h1l;
-            const float(&Zl)[8][4] = NH == 2 ? Z2 : Z1;
-            // dL/dH of the last hidden layer
-            float dH[8][4];
-            if (GROUP != kCurv && e == 0) {
-                // the point: the whole output row (dL/dfeature; column 0 also dL/dsdf)
-                const int od = nl.out_dim;
-                auto gval = [&](int row, int col, bool valid) -> float {
-                    if (!valid || col >= od) return 0.f;
-                    float v = P.g_feature ? P.g_feature[(s0 + row) * P.gfeat_stride + col] : 0.f;
-                    if (col == 0) v += ws.ds[row][0];
-                    return v;
-                };
-                uint32_t yh[KT3][4], yl[KT3][4];
+            if (!(alive = tc_wait_all(&bar[0], ph0))) break;
+            ph0 ^= 1;
+        }
+        {
+            // last hidden layer: H (two layers: staged for dW3), dH, dZ
+            float gl[16], dh[16];
+            if (NH == 2) {
+                float z[16];
+                tc::ld16(tmem + lane_off + Sh::tB + 16 * slice, z);
 #pragma unroll
-                for (int kt = 0; kt < KT3; ++kt) {
-#pragma unroll
-                    for (int hf = 0; hf < 2; ++hf) {
-                        const int col = kt * 16 + hf * 8 + c;
-                        const Split a = split2(gval(g, col, v0), gval(g, col + 1, v0));
-                        const Split b = split2(gval(g + 8, col, v1), gval(g + 8, col + 1, v1));
-                        yh[kt][hf * 2] = a.hi;
-                        yl[kt][hf * 2] = a.lo;
-                        yh[kt][hf * 2 + 1] = b.hi;
-                        yl[kt][hf * 2 + 1] = b.lo;
-                    }
-                }
-                mm_nobias<KT3, 8>(yh, yl, S.w3b, 8, lane, dH);
-                accumulate_dw<KT3, 4>(yh, yl, hlh, hll, S.dW3, 64, lane);
-                float Y[2 * KT3][4];
-#pragma unroll
-                for (int nt = 0; nt < 2 * KT3; ++nt) {
-                    const int col = nt * 8 + c;
-                    Y[nt][0] = gval(g, col, v0);
-                    Y[nt][1] = gval(g, col + 1, v0);
-                    Y[nt][2] = gval(g + 8, col, v1);
-                    Y[nt][3] = gval(g + 8, col + 1, v1);
-                }
-                accumulate_db<2 * KT3>(Y, S.db3, lane);
+                for (int j = 0; j < 16; ++j) softplus100_both(z[j] + vec[64 + 16 * slice + j], &hl[j], &gl[j]);
+                if (point) stage16(h2h, h2l, row, 16 * slice, 64, hl);
             } else {
-                // a stencil tap: only the SDF column carries a gradient
-                const float dy0 = v0 ? ws.ds[g][e] : 0.f, dy1 = v1 ? ws.ds[g + 8][e] : 0.f;
-                float part[8][2];
 #pragma unroll
-                for (int nt = 0; nt < 8; ++nt) {
-                    const int col = nt * 8 + c;
-                    const float w0 = S.w3row0[col], w1 = S.w3row0[col + 1];
-                    dH[nt][0] = dy0 * w0;
-                    dH[nt][1] = dy0 * w1;
-                    dH[nt][2] = dy1 * w0;
-                    dH[nt][3] = dy1 * w1;
-                    part[nt][0] = dy0 * softplus100(Zl[nt][0]) + dy1 * softplus100(Zl[nt][2]);
-                    part[nt][1] = dy0 * softplus100(Zl[nt][1]) + dy1 * softplus100(Zl[nt][3]);
+                for (int j = 0; j < 16; ++j) gl[j] = g1[j];
+            }
+            if (point) {
+                tc::ld16(tmem + lane_off + (NH == 2 ? Sh::tA : Sh::tB) + 16 * slice, dh);
+            } else {
+                const float d = ds[i * 128 + row];
+                float part[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    dh[j] = d * vec[128 + 16 * slice + j];
+                    part[j] = d * hl[j];
                 }
-#pragma unroll
-                for (int nt = 0; nt < 8; ++nt) {
-#pragma unroll
-                    for (int o = 4; o < 32; o <<= 1) {
-                        part[nt][0] += __shfl_xor_sync(0xffffffffu, part[nt][0], o);
-                        part[nt][1] += __shfl_xor_sync(0xffffffffu, part[nt][1], o);
-                    }
-                }
-                if (lane < 4) {
-#pragma unroll
-                    for (int nt = 0; nt < 8; ++nt) {
-                        red_add(S.dW3 + nt * 8 + lane * 2, part[nt][0]);
-                        red_add(S.dW3 + nt * 8 + lane * 2 + 1, part[nt][1]);
-                    }
-                }
-                // the taps' SDF-bias gradient, sum_e ds_e, is exactly zero (each
-                // axis contributes +h and -h): it is not accumulated, so that
-                // large cancelling terms do not round into the bias
+                int col;
+                const float sum = warp_colsum16(part, lane, &col);
+                if ((lane & 1) == 0 && sum != 0.f) red_add(w3g + 16 * slice + col, sum);
             }
 #pragma unroll
-            for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-                for (int k = 0; k < 4; ++k) dH[nt][k] *= softplus100_grad(Zl[nt][k]);
-            uint32_t dzh[4][4], dzl[4][4];
-            c_to_a(dH, dzh, dzl);
-            if (NH == 2) {
-                accumulate_db<8>(dH, S.db2, lane);
-                stage_a<4>(dzh, dzl, zh, zl, kStageLd, warp * 16, lane);
-                stage_a<4>(h1h, h1l, b2h, b2l, kStageLd, warp * 16, lane);
-                __syncthreads();
-                staged_dw<4>(acc2, zh, zl, b2h, b2l, kStageLd, mt, nt2, lane);
-                __syncthreads();
-                mm_nobias<4, 8>(dzh, dzl, S.w2b, 8, lane, dH);
-#pragma unroll
-                for (int nt = 0; nt < 8; ++nt)
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) dH[nt][k] *= softplus100_grad(Z1[nt][k]);
-                c_to_a(dH, dzh, dzl);
+            for (int j = 0; j < 16; ++j) dh[j] *= gl[j];
+            stage16(zh, zl, row, 16 * slice, 64, dh);
+        }
+        tc_publish();
+        if (NH == 2) {
+            // round 3: dH1 (epilogue), then dW2, db2, dW3
+            if (tid == 0) {
+                tc_mma<4>(tmem + Sh::tA, Zk, W2t, id_dh, false);
+                tc::commit(&bar[0]);
+                tc_mma<8>(tmem + Sh::tW2, Zt, H1t, id_w2, true);
+                tc_mma<8>(tmem + Sh::tb2, Zt, Ones, id_16, true, true);
+                if (point) tc_mma<8>(tmem + Sh::tW3, HLt, Yt, id_w3, true);
+                tc::commit(&bar[1]);
             }
-            accumulate_db<8>(dH, S.db1, lane);
-            stage_a<4>(dzh, dzl, zh, zl, kStageLd, warp * 16, lane);
-            stage_a<KH + 1>(X.hi, X.lo, b1h, b1l, Sh::XS, warp * 16, lane);
-            __syncthreads();
-            staged_dw<KH + 1>(acc1, zh, zl, b1h, b1l, Sh::XS, mt, nt1, lane);
-            __syncthreads();
-            // dL/dX: hash columns (n-tiles 0 .. 2KH-1; lane q holds level 4 nt + q)
-            // and, for the curvature taps, the xyz n-tile
-            constexpr int NTX = 2 * KH + (GROUP == kCurv ? 1 : 0);
-            float dX[NTX][4];
-            mm_nobias<4, NTX>(dzh, dzl, S.w1b, 2 * (KH + 1), lane, dX);
+            if (!(alive = tc_wait_all(&bar[0], ph0))) break;
+            ph0 ^= 1;
+            float dz[16];
+            tc::ld16(tmem + lane_off + Sh::tA + 16 * slice, dz);
 #pragma unroll
-            for (int nt = 0; nt < 2 * KH; ++nt) {
-                const int l = nt * 4 + q;
-                if (l < P.active) {
-                    if (v0) P.dX[xidx(P, e, l, s0 + g)] = make_float2(dX[nt][0], dX[nt][1]);
-                    if (v1) P.dX[xidx(P, e, l, s0 + g + 8)] = make_float2(dX[nt][2], dX[nt][3]);
-                }
-            }
-            if (GROUP == kCurv) {
-                // xyz columns x*2-1: q = 0 holds (x, y), q = 1 holds z
-                float d0[3] = {0.f, 0.f, 0.f}, d1[3] = {0.f, 0.f, 0.f};
-                if (q == 0) {
-                    d0[0] = 2.f * dX[NTX - 1][0];
-                    d0[1] = 2.f * dX[NTX - 1][1];
-                    d1[0] = 2.f * dX[NTX - 1][2];
-                    d1[1] = 2.f * dX[NTX - 1][3];
-                } else if (q == 1) {
-                    d0[2] = 2.f * dX[NTX - 1][0];
-                    d1[2] = 2.f * dX[NTX - 1][2];
-                }
+            for (int j = 0; j < 16; ++j) dz[j] *= g1[j];
+            // H1 is read by dW2: rewrite it as dZ1 after the round completed
+            if (!(alive = tc_wait_all(&bar[1], ph1))) break;
+            ph1 ^= 1;
+            stage16(h1h, h1l, row, 16 * slice, 64, dz);
+            tc_publish();
+        }
+        // last round: dX (epilogue), then dW1, db1 (one hidden layer: dW3)
+        if (tid == 0) {
+            tc_mma<4>(tmem + Sh::tB, D1k, W1t, id_dx, false);
+            tc::commit(&bar[0]);
+            tc_mma<8>(tmem + Sh::tW1, D1t, Xt, id_w1, true);
+            tc_mma<8>(tmem + Sh::tb1, D1t, Ones, id_16, true, true);
+            if (NH == 1 && point) tc_mma<8>(tmem + Sh::tW3, HLt, Yt, id_w3, true);
+            tc::commit(&bar[1]);
+        }
+        if (!(alive = tc_wait_all(&bar[0], ph0))) break;
+        ph0 ^= 1;
+        if (slice <= KH) {
+            float dx[16];
+            tc::ld16(tmem + lane_off + Sh::tB + 16 * slice, dx);
+            if (slice < KH) {
+                // dL/dX of hash levels 8 slice .. 8 slice + 7
 #pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    if ((m0 >> d) & 1) dsh0[d] += d0[d] * inv2r;
-                    if ((m1 >> d) & 1) dsh1[d] += d1[d] * inv2r;
+                for (int j = 0; j < 8; ++j) {
+                    const int l = 8 * slice + j;
+                    if (v && l < P.active) P.dX[xidx(P, e, l, s)] = make_float2(dx[2 * j], dx[2 * j + 1]);
+                }
+            } else if (GROUP == kCurv) {
+                // xyz columns x*2-1 to dL/dshifted; the scatter pass adds the
+                // hash grid's positional derivative atomically
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    if ((m >> d) & 1) dsh[d] += 2.f * dx[d] * inv2r;
+                if (i == ne - 1 && v) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) P.bstate[s * kBState + d] = dsh[d];
                 }
             }
         }
-        if (GROUP == kCurv) {
-            // dL/dshifted from the xyz columns; the scatter pass adds the hash
-            // grid's positional derivative atomically
-#pragma unroll
-            for (int d = 0; d < 3; ++d) {
-#pragma unroll
-                for (int o = 1; o < 4; o <<= 1) {
-                    dsh0[d] += __shfl_xor_sync(0xffffffffu, dsh0[d], o);
-                    dsh1[d] += __shfl_xor_sync(0xffffffffu, dsh1[d], o);
-                }
-            }
-            if (q == 0) {
-#pragma unroll
-                for (int d = 0; d < 3; ++d) {
-                    if (v0) P.bstate[(s0 + g) * kBState + d] = dsh0[d];
-                    if (v1) P.bstate[(s0 + g + 8) * kBState + d] = dsh1[d];
-                }
-            }
-        }
-        __syncwarp();
     }
-    // one flush per CTA: register-held dW1 / dW2 tiles, shared dW3 and biases
+    if (alive && n_items > 0) alive = tc_wait_all(&bar[1], ph1);
+    if (alive) {
+        // add the CTA's gradients: tensor-memory rows 16 (warp % 4) + lane
+        const int unit = 16 * (warp & 3) + lane;
+        float *dW2 = P.d_net + 64 * K1, *dW3 = dW2 + 64 * 64, *db1 = dW3 + N3 * 64, *db2 = db1 + 64,
+              *dB3 = db2 + 64;
+        for (uint32_t b = slice; b < (Sh::used - Sh::tW1) / 16; b += 4) {
+            const uint32_t c0 = Sh::tW1 + 16 * b;
+            float w[16];
+            __syncwarp();
+            tc::ld16(tmem + lane_off + c0, w);
+#pragma unroll
+            for (int j = 0; j < 16 && lane < 16; ++j) {
+                const uint32_t c = c0 + j;
+                float *dst = nullptr;
+                if (c < Sh::tW2) dst = P.d_net + unit * K1 + (c - Sh::tW1);
+                else if (c < Sh::tW3) dst = dW2 + unit * 64 + (c - Sh::tW2);
+                else if (c < Sh::tb1) dst = dW3 + (c - Sh::tW3) * 64 + unit;
+                else if (c == Sh::tb1) dst = db1 + unit;
+                else if (NH == 2 && c == Sh::tb2) dst = db2 + unit;
+                if (dst && w[j] != 0.f) atomicAdd(dst, w[j]);
+            }
+        }
+        for (int o = tid; o < N3; o += kTcThreads)
+            if (db3[o] != 0.f) atomicAdd(dB3 + o, db3[o]);
+        for (int h = tid; h < 64; h += kTcThreads)
+            if (w3g[h] != 0.f) atomicAdd(dW3 + h, w3g[h]);
+    }
+    if (!alive && tid == 0) atomicAdd(&g_tc_timeouts, 1u);
+    tc::fence_before_sync();
     __syncthreads();
-    const int K1c = 16 * (KH + 1);
-#pragma unroll
-    for (int i = 0; i < KH + 1; ++i) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const int row = mt * 16 + g + ((j >> 1) << 3), col = (nt1 + i) * 8 + c + (j & 1);
-            if (acc1[i][j] != 0.f) atomicAdd(P.d_net + row * K1c + col, acc1[i][j]);
-        }
-    }
-    if (NH == 2) {
-#pragma unroll
-        for (int i = 0; i < 4; ++i) {
-#pragma unroll
-            for (int j = 0; j < 4; ++j) {
-                const int row = mt * 16 + g + ((j >> 1) << 3), col = (nt2 + i) * 8 + c + (j & 1);
-                if (acc2[i][j] != 0.f) atomicAdd(P.d_net + 64 * K1c + row * 64 + col, acc2[i][j]);
-            }
-        }
-    }
-    for (int i = tid; i < n_acc; i += kThreads) {
-        const float v = acc[i];
-        if (v != 0.f) atomicAdd(P.d_net + 64 * K1c + 64 * 64 + i, v);
-    }
+    if (warp == 0) tc::tmem_dealloc(tmem, Sh::tmem_cols);
 }
 
 // ------------------------------------------------------------------ scatter
@@ -1297,12 +1214,6 @@ extern "C" int angelo_sdf_net_layout_query(int32_t n_levels, int32_t n_hidden, i
     L.out_dim = out_dim;
     int64_t o = 0;
     auto take = [&](int64_t bytes) { const int64_t r = o; o += (bytes + 15) / 16 * 16; return r; };
-    L.off_w1f = take(2 * frag_count(L.k_tiles1, 8) * 8);
-    L.off_w2f = take(n_hidden == 2 ? 2 * frag_count(4, 8) * 8 : 0);
-    L.off_w3f = take(2 * frag_count(4, L.n_tiles3) * 8);
-    L.off_w1b = take(2 * frag_count(4, 2 * L.k_tiles1) * 8);
-    L.off_w2b = take(n_hidden == 2 ? 2 * frag_count(4, 8) * 8 : 0);
-    L.off_w3b = take(2 * frag_count(L.k_tiles3b, 8) * 8);
     L.off_b1 = take(64 * 4);
     L.off_b2 = take(64 * 4);
     L.off_b3 = take(8 * L.n_tiles3 * 4);
@@ -1322,12 +1233,8 @@ extern "C" int angelo_sdf_prep(const angelo_sdf_net_layout *lay, int32_t n_level
     ANGELO_REQUIRE(lay->n_hidden == 1 || (W2 && b2), "sdf_prep: missing hidden layer 2");
     ANGELO_REQUIRE(in_dim == 3 + 2 * n_levels, "sdf_prep: in_dim %d != 3 + 2*levels", in_dim);
     const int K1 = lay->k_tiles1, nh = lay->n_hidden;
-    const int frags = K1 * 8 + (nh == 2 ? 32 : 0) + 4 * lay->n_tiles3 + 4 * 2 * K1 +
-                      (nh == 2 ? 32 : 0) + lay->k_tiles3b * 8;
-    const int extra = (192 + 8 * lay->n_tiles3 + 31) / 32;
-    const int threads = (frags + extra) * 32;
-    sdf_prep_kernel<<<blocks_for(threads, 256), 256, 0, as_stream(stream)>>>(
-        W1, b1, W2, b2, W3, b3, in_dim, 2 * n_levels, *lay, reinterpret_cast<char *>(net));
+    sdf_prep_vec_kernel<<<1, 192 + 8 * lay->n_tiles3, 0, as_stream(stream)>>>(
+        b1, b2, W3, b3, *lay, reinterpret_cast<char *>(net));
     const int tc_elems = 64 * 16 * K1 + (nh == 2 ? 64 * 64 : 0) + 16 * lay->k_tiles3b * 64;
     sdf_prep_tc_kernel<<<blocks_for(tc_elems, 256), 256, 0, as_stream(stream)>>>(
         W1, W2, W3, in_dim, 2 * n_levels, *lay, reinterpret_cast<char *>(net));
@@ -1363,22 +1270,6 @@ int launch_scatter(const SdfParams &P, cudaStream_t s) {
     return check_launch("sdf_stencil_scatter");
 }
 
-template <typename K>
-int persistent_grid(K k, size_t smem, const SdfParams &P, const char *what, int *grid) {
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-        return check_launch(what);
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kThreads, smem);
-    if (per_sm < 1) {
-        set_error("%s: %zu bytes of shared memory do not fit an SM", what, smem);
-        return ANGELO_E_UNSUPPORTED;
-    }
-    const int64_t tiles = (P.S + 15) / 16;
-    const int64_t want = (tiles + kWarps - 1) / kWarps;
-    *grid = (int)std::min<int64_t>(want, (int64_t)sm_count() * per_sm);
-    return ANGELO_OK;
-}
-
 template <int KH, int NH, int NT3, int GROUP>
 int launch_mlp_fwd(const SdfParams &P, cudaStream_t s) {
     const size_t smem = TcFwdShape<KH, NH, NT3>::bytes;
@@ -1405,12 +1296,22 @@ int launch_mlp_fwd(const SdfParams &P, cudaStream_t s) {
 
 template <int KH, int NH, int NT3, int GROUP>
 int launch_mlp_bwd(const SdfParams &P, cudaStream_t s) {
-    const size_t smem = BwdShape<KH, NH, NT3>::bytes;
-    auto k = sdf_mlp_bwd_kernel<KH, NH, NT3, GROUP>;
-    int grid = 0;
-    const int rc = persistent_grid(k, smem, P, "sdf_mlp_bwd", &grid);
-    if (rc != ANGELO_OK) return rc;
-    k<<<grid, kThreads, smem, s>>>(P);
+    const size_t smem = TcBwdShape<KH, NH, NT3>::bytes;
+    auto k = sdf_mlp_bwd_tc_kernel<KH, NH, NT3, GROUP>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+        return check_launch("sdf_mlp_bwd(smem attribute)");
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kTcThreads, smem);
+    if (per_sm < 1) {
+        set_error("sdf_mlp_bwd: %zu bytes of shared memory do not fit an SM", smem);
+        return ANGELO_E_UNSUPPORTED;
+    }
+    // each CTA holds TcBwdShape::tmem_cols of the SM's 512 tensor-memory columns
+    per_sm = std::min(per_sm, (int)(512 / TcBwdShape<KH, NH, NT3>::tmem_cols));
+    const int64_t tiles = (P.S + 127) / 128;
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm);
+    k<<<grid, kTcThreads, smem, s>>>(P);
     return check_launch("sdf_mlp_bwd");
 }
 

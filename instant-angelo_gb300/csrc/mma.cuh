@@ -76,4 +76,14 @@ __device__ __forceinline__ float softplus100_grad(float z) {
     return x > 20.0f ? 1.0f : __fdividef(1.0f, 1.0f + __expf(-x));
 }
 
+// softplus100(z) and its derivative from one exponential: the derivative as
+// e / (1 + e), e = e^(100 z), the form of torch's softplus backward.
+__device__ __forceinline__ void softplus100_both(float z, float *sp, float *grad) {
+    const float x = 100.0f * z;
+    const float e = __expf(fminf(x, 20.0f));
+    const float q = 1.0f + e;
+    *sp = x > 20.0f ? z : (x < -15.0f ? e : __logf(q)) * 0.01f;
+    *grad = x > 20.0f ? 1.0f : __fdividef(e, q);
+}
+
 }  // namespace angelo

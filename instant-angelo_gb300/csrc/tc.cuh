@@ -15,8 +15,9 @@
 // 8 K-rows) and SBO the stride along M (between 8-element chunks).
 //
 // Accumulator (M = 128, cta_group::1): row i of D is tensor-memory lane i,
-// column j is the allocation's column base + j (fp32).  Warp w may read only
-// lanes 32 (w % 4) .. 32 (w % 4) + 31.
+// column j is the allocation's column base + j (fp32).  M = 64: row i is lane
+// 32 (i / 16) + i % 16 (lanes 16 .. 31 of each quarter are not written).
+// Warp w may read only lanes 32 (w % 4) .. 32 (w % 4) + 31.
 #pragma once
 
 #include <stdint.h>
@@ -152,6 +153,17 @@ __device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
         : "memory");
 #pragma unroll
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ---- accumulator stores: zeros into this thread's lane, 16 consecutive
+// columns (completed by tcgen05.wait::st in the same statement)
+__device__ __forceinline__ void st16_zero(uint32_t taddr) {
+    const uint32_t z = 0u;
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1,%1};\n"
+        "tcgen05.wait::st.sync.aligned;\n" ::"r"(taddr),
+        "r"(z)
+        : "memory");
 }
 
 }  // namespace tc

@@ -23,19 +23,23 @@ def dev():
     return torch.device("cuda:0")
 
 
-def _gemm(dev, N, K, a_mn, b_mn, variant, seed=0):
+def _run(dev, M, N, K, a_mn, b_mn, variant, seed=0):
     from angelo_gb._lib import call
     from angelo_gb.ops import _p, _s
     g = torch.Generator(device="cpu").manual_seed(seed)
-    A = torch.randn(128, K, generator=g).to(dev)
+    A = torch.randn(M, K, generator=g).to(dev)
     B = torch.randn(N, K, generator=g).to(dev)
-    D = torch.full((128, N), float("nan"), device=dev)
+    D = torch.full((128, 2 * N if M == 64 else N), float("nan"), device=dev)
     st = torch.zeros(1, dtype=torch.int32, device=dev)
-    call("angelo_tc_gemm_x3", _p(A), _p(B), _p(D), N, K, a_mn, b_mn, variant, _p(st), _s(dev))
+    call("angelo_tc_gemm_x3", _p(A), _p(B), _p(D), M, N, K, a_mn, b_mn, variant, _p(st), _s(dev))
     torch.cuda.synchronize()
-    ref = A.double() @ B.double().T
-    err = ((D.double() - ref).abs().max() / ref.abs().max()).item()
-    return int(st.item()), err
+    return int(st.item()), A.double() @ B.double().T, D.double()
+
+
+def _gemm(dev, N, K, a_mn, b_mn, variant, seed=0):
+    st, ref, D = _run(dev, 128, N, K, a_mn, b_mn, variant, seed)
+    err = ((D - ref).abs().max() / ref.abs().max()).item()
+    return st, err
 
 
 @pytest.mark.parametrize("N,K", [(16, 16), (64, 48), (80, 64), (128, 32), (256, 64)])
@@ -67,3 +71,36 @@ def test_tc_layout_variant_report(dev):
         assert st == 0
         if v == 0:
             assert err < 2e-5
+
+
+def test_tc_m64_accumulator_layout(dev):
+    """M = 64: every row of the product is found in exactly one tensor-memory
+    (lane, column block); the mapping is printed (the layout an M = 64
+    kernel would read)."""
+    st, ref, D = _run(dev, 64, 32, 32, 0, 0, 0, seed=3)
+    assert st == 0
+    found = []
+    for i in range(64):
+        hits = []
+        for b in range(2):                        # the row's two 16-column blocks
+            hits.append([(lane, c0) for lane in range(128) for c0 in range(0, 64 - 15)
+                         if torch.allclose(D[lane, c0:c0 + 16], ref[i, 16 * b:16 * b + 16],
+                                           rtol=1e-4, atol=1e-4)])
+        found.append(hits)
+    print("\nM=64 row -> [(lane, first column) of its column blocks]:")
+    for i, h in enumerate(found):
+        print(i, h)
+    assert all(len(h[0]) >= 1 and len(h[1]) >= 1 for h in found)
+
+
+@pytest.mark.parametrize("N,K", [(48, 64), (64, 64), (80, 32), (16, 64)])
+def test_tc_m64_mn_major_weight_gradient(dev, N, K):
+    """The weight-gradient products of the backward MLP: M = 64 units, both
+    operands MN-major (transposed [sample][column] stagings), read back with
+    row i in tensor-memory lane 32 (i / 16) + i % 16."""
+    st, ref, D = _run(dev, 64, N, K, 1, 1, 0, seed=5)
+    assert st == 0
+    lanes = torch.tensor([32 * (i // 16) + i % 16 for i in range(64)])
+    got = D[lanes, :N]
+    err = ((got - ref).abs().max() / ref.abs().max()).item()
+    assert err < 2e-5, err
