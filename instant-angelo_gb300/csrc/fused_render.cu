@@ -21,20 +21,23 @@
 #include "common.cuh"
 #include "mlp.cuh"
 #include "sh.cuh"
+#include "tc.cuh"
+#include "tc_mlp.cuh"
 
 using namespace angelo;
 
 namespace {
 
-constexpr int kRW = 8;               // warps per CTA
-constexpr int kRT = kRW * 32;
-constexpr int kXCols = 96;           // staged input width (6 k-tiles)
+constexpr int kXCols = 96;           // widest staged input (6 k-tiles)
 
 struct RadLayout {
     int k_tiles1;   // input k-tiles (ceil(in_dim / 16))
     int in_dim;
     int feat_dim;   // width of the feature input
-    int64_t off_w1f, off_w2f, off_w3f, off_w1b, off_w2b, off_w3b, off_b1, off_b2, off_b3, bytes;
+    // tensor-core operands, bf16 hi then lo, K-major [n][k] (Y = X W^T): W1
+    // 64 x 16 k_tiles1, W2 64 x 64, W3 16 x 64 (rows 3 .. 15 zero); fp32 b1,
+    // b2, b3 (16) and W3 (3 x 64)
+    int64_t off_tw1, off_tw2, off_tw3, off_b1, off_b2, off_b3, off_w3, bytes;
 };
 
 RadLayout rad_layout(int feat_dim) {
@@ -44,15 +47,13 @@ RadLayout rad_layout(int feat_dim) {
     L.k_tiles1 = (L.in_dim + 15) / 16;
     int64_t o = 0;
     auto take = [&](int64_t b) { const int64_t r = o; o += (b + 15) / 16 * 16; return r; };
-    L.off_w1f = take(2 * frag_count(L.k_tiles1, 8) * 8);
-    L.off_w2f = take(2 * frag_count(4, 8) * 8);
-    L.off_w3f = take(2 * frag_count(4, 1) * 8);
-    L.off_w1b = take(2 * frag_count(4, 2 * L.k_tiles1) * 8);
-    L.off_w2b = take(2 * frag_count(4, 8) * 8);
-    L.off_w3b = take(2 * frag_count(1, 8) * 8);
+    L.off_tw1 = take(2 * 64 * 16 * L.k_tiles1 * 2);
+    L.off_tw2 = take(2 * 64 * 64 * 2);
+    L.off_tw3 = take(2 * 16 * 64 * 2);
     L.off_b1 = take(64 * 4);
     L.off_b2 = take(64 * 4);
-    L.off_b3 = take(8 * 4);
+    L.off_b3 = take(16 * 4);
+    L.off_w3 = take(3 * 64 * 4);
     L.bytes = o;
     return L;
 }
@@ -66,43 +67,36 @@ __device__ __forceinline__ float rad_w(int layer, int n, int k, const float *W1,
 
 __global__ void rad_prep_kernel(const float *W1, const float *b1, const float *W2, const float *b2,
                                 const float *W3, const float *b3, RadLayout L, char *net) {
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = tid & 31, r = lane >> 2, c = (lane & 3) * 2;
-    int frag = tid >> 5;
-    const int K1 = L.k_tiles1;
-    const int counts[6] = {K1 * 8, 32, 4, 4 * 2 * K1, 32, 8};
-    int which = 0;
-    while (which < 6 && frag >= counts[which]) frag -= counts[which++];
-    if (which >= 6) {
-        const int j = frag * 32 + lane;
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int K1 = 16 * L.k_tiles1;
+    const int n1 = 64 * K1, n2 = 64 * 64, n3 = 16 * 64;
+    int layer, n, k, K;
+    int64_t off, half;
+    if (i < n1) {
+        layer = 1, K = K1, n = i / K1, k = i % K1, off = L.off_tw1, half = (int64_t)n1 * 2;
+    } else if ((i -= n1) < n2) {
+        layer = 2, K = 64, n = i / 64, k = i % 64, off = L.off_tw2, half = (int64_t)n2 * 2;
+    } else if ((i -= n2) < n3) {
+        layer = 3, K = 64, n = i / 64, k = i % 64, off = L.off_tw3, half = (int64_t)n3 * 2;
+    } else {
+        i -= n3;
         float *fb1 = reinterpret_cast<float *>(net + L.off_b1);
         float *fb2 = reinterpret_cast<float *>(net + L.off_b2);
         float *fb3 = reinterpret_cast<float *>(net + L.off_b3);
-        if (j < 64) fb1[j] = b1[j];
-        else if (j < 128) fb2[j - 64] = b2[j - 64];
-        else if (j < 136) fb3[j - 128] = j - 128 < 3 ? b3[j - 128] : 0.f;
+        float *fw3 = reinterpret_cast<float *>(net + L.off_w3);
+        if (i < 64) fb1[i] = b1[i];
+        else if (i < 128) fb2[i - 64] = b2[i - 64];
+        else if (i < 144) fb3[i - 128] = i - 128 < 3 ? b3[i - 128] : 0.f;
+        else if (i < 144 + 192) fw3[i - 144] = W3[i - 144];
         return;
     }
-    const int layer = which % 3 + 1;
-    const bool bwd = which >= 3;
-    const int NT = !bwd ? (layer == 3 ? 1 : 8) : (layer == 1 ? 2 * K1 : 8);
-    const int KT = !bwd ? (layer == 1 ? K1 : 4) : (layer == 3 ? 1 : 4);
-    const int64_t off = !bwd ? (layer == 1 ? L.off_w1f : layer == 2 ? L.off_w2f : L.off_w3f)
-                             : (layer == 1 ? L.off_w1b : layer == 2 ? L.off_w2b : L.off_w3b);
-    const int kt = frag / NT, nt = frag % NT;
-    float v[4];
-    for (int i = 0; i < 4; ++i) {
-        const int k = kt * 16 + c + (i & 1) + (i >> 1) * 8;
-        const int n = nt * 8 + r;
-        v[i] = !bwd ? rad_w(layer, n, k, W1, W2, W3, L.in_dim) : rad_w(layer, k, n, W1, W2, W3, L.in_dim);
-    }
-    const Split s0 = split2(v[0], v[1]), s1 = split2(v[2], v[3]);
-    uint2 *dst = reinterpret_cast<uint2 *>(net + off);
-    const int64_t n_frag = frag_count(KT, NT);
-    const int64_t idx = (int64_t)(kt * NT + nt) * 32 + lane;
-    dst[idx] = make_uint2(s0.hi, s1.hi);
-    dst[n_frag + idx] = make_uint2(s0.lo, s1.lo);
+    const Split sp = split2(rad_w(layer, n, k, W1, W2, W3, L.in_dim), 0.0f);
+    const uint32_t o = tc::kmajor_offset(n, k, K);
+    *reinterpret_cast<uint16_t *>(net + off + o) = (uint16_t)(sp.hi & 0xFFFFu);
+    *reinterpret_cast<uint16_t *>(net + off + half + o) = (uint16_t)(sp.lo & 0xFFFFu);
 }
+
+int rad_prep_threads(const RadLayout &L) { return 64 * 16 * L.k_tiles1 + 64 * 64 + 16 * 64 + 144 + 192; }
 
 struct RadParams {
     RadLayout L;
@@ -121,264 +115,431 @@ struct RadParams {
     float *d_net;
 };
 
-struct RadWarp {
-    float x[16][kXCols];
-    float dual_g[16][3];
-    float dn[16][3];
-};
+__device__ unsigned int g_rad_tc_timeouts;   // CTAs that stopped waiting for the tensor cores
 
 __device__ __forceinline__ float sigm(float v) { return 1.0f / (1.0f + __expf(-v)); }
 
-// stage the 16 input rows of a tile: [feature, SH, normal, 0...]
-__device__ __forceinline__ void stage_rows(const RadParams &P, RadWarp &w, int64_t s0, int lane) {
+// SH4 of the viewing direction as the reference feeds it ((d + 1) / 2, then
+// the encoder's 2 x - 1) and the unit normal of the SDF gradient, for sample s
+__device__ __forceinline__ void rad_sh_normal(const RadParams &P, int64_t s, float sh[16], float nrm[3]) {
+    const float *d = P.rays_d + (int64_t)P.ray_idx[s] * 3;
+    const float x = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(d[0], 1.f), 2.f), 2.f), 1.f);
+    const float y = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(d[1], 1.f), 2.f), 2.f), 1.f);
+    const float z = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(d[2], 1.f), 2.f), 2.f), 1.f);
+    sh4_eval(x, y, z, sh);
+    const float *g = P.grad + s * 3;
+    const float gn = fmaxf(sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]), 1e-12f);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) nrm[k] = g[k] / gn;
+}
+
+// The input row [feature (F), SH (16), normal (3), 0 ...] of sample s, the
+// 16-column blocks slice, slice + 4, ... of it staged K-major (16 KT1 columns)
+template <int KT1>
+__device__ __forceinline__ void rad_stage_x(const RadParams &P, int64_t s, bool v, int row, int slice, char *xh,
+                                            char *xl) {
     const int F = P.L.feat_dim;
-    for (int i = lane; i < 16 * kXCols; i += 32) {
-        const int row = i / kXCols, col = i % kXCols;
-        const int64_t s = s0 + row;
-        float v = 0.f;
-        if (s < P.S && col < F) v = P.feature[s * P.feat_stride + col];
-        w.x[row][col] = v;
-    }
-    __syncwarp();
-    if (lane < 16) {
-        const int64_t s = s0 + lane;
-        float sh[16], nrm[3] = {0.f, 0.f, 0.f};
-        if (s < P.S) {
-            const float *d = P.rays_d + (int64_t)P.ray_idx[s] * 3;
-            const float x = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(d[0], 1.f), 2.f), 2.f), 1.f);
-            const float y = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(d[1], 1.f), 2.f), 2.f), 1.f);
-            const float z = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(d[2], 1.f), 2.f), 2.f), 1.f);
-            sh4_eval(x, y, z, sh);
-            const float *g = P.grad + s * 3;
-            const float gn = fmaxf(sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]), 1e-12f);
-            for (int k = 0; k < 3; ++k) nrm[k] = g[k] / gn;
-        } else {
-            for (int k = 0; k < 16; ++k) sh[k] = 0.f;
+    for (int b = slice; b < KT1; b += 4) {
+        const int c0 = 16 * b;
+        float x[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) x[j] = (v && c0 + j < F) ? P.feature[s * P.feat_stride + c0 + j] : 0.f;
+        if (v && c0 + 16 > F && c0 < F + 19) {
+            float sh[16], nrm[3];
+            rad_sh_normal(P, s, sh, nrm);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int c = c0 + j - F;
+                if (c >= 0 && c < 16) x[j] = sh[c];
+                else if (c >= 16 && c < 19) x[j] = nrm[c - 16];
+            }
         }
-        for (int k = 0; k < 16; ++k) w.x[lane][F + k] = sh[k];
-        for (int k = 0; k < 3; ++k) w.x[lane][F + 16 + k] = nrm[k];
+        stage16(xh, xl, row, c0, 16 * KT1, x);
     }
-    __syncwarp();
 }
 
 template <int KT1>
-__device__ __forceinline__ void rows_to_a(const RadWarp &w, int lane, uint32_t (&ah)[KT1][4],
-                                          uint32_t (&al)[KT1][4]) {
-    const int r = lane >> 2, c = (lane & 3) * 2;
-#pragma unroll
-    for (int kt = 0; kt < KT1; ++kt)
-#pragma unroll
-        for (int hf = 0; hf < 2; ++hf) {
-            const int col = kt * 16 + hf * 8 + c;
-            const Split a = split2(w.x[r][col], w.x[r][col + 1]);
-            const Split b = split2(w.x[r + 8][col], w.x[r + 8][col + 1]);
-            ah[kt][hf * 2] = a.hi;
-            al[kt][hf * 2] = a.lo;
-            ah[kt][hf * 2 + 1] = b.hi;
-            al[kt][hf * 2 + 1] = b.lo;
-        }
-}
-
-struct RadNet {
-    const uint2 *w1f, *w2f, *w3f, *w1b, *w2b, *w3b;
-    const float *b1, *b2, *b3;
+struct RadShape {
+    static constexpr int K1 = 16 * KT1;
+    // bytes of one (hi or lo) half
+    static constexpr uint32_t w1 = 64 * K1 * 2, w2 = 64 * 64 * 2, w3 = 16 * 64 * 2;
+    static constexpr uint32_t x = 128 * K1 * 2, h = 128 * 64 * 2, y = 128 * 16 * 2, ones = 128 * 16 * 2;
+    static constexpr uint32_t off_w1 = 0, off_w2 = 2 * w1, off_w3 = off_w2 + 2 * w2, off_x = off_w3 + 2 * w3;
+    // forward: one activation staging (H1, then H2)
+    static constexpr uint32_t f_h = off_x + 2 * x, f_vec = f_h + 2 * h, f_bar = f_vec + 144 * 4,
+                              f_bytes = f_bar + 16;
+    // backward
+    static constexpr uint32_t b_h1 = off_x + 2 * x,   // H1, then dZ1
+        b_h2 = b_h1 + 2 * h, b_z = b_h2 + 2 * h, b_y = b_z + 2 * h, b_ones = b_y + 2 * y,
+                              b_vec = b_ones + ones,                 // b1, b2, b3 (16), W3 (3 x 64)
+        b_db3 = b_vec + (144 + 192) * 4, b_bar = b_db3 + 16 * 4, b_bytes = b_bar + 32;
+    // backward tensor-memory columns
+    static constexpr uint32_t tA = 0, tB = 64, tW1 = tB + (K1 > 64 ? K1 : 64), tW2 = tW1 + K1, tW3 = tW2 + 64,
+                              tb1 = tW3 + 16, tb2 = tb1 + 16, used = tb2 + 16;
 };
 
-__device__ __forceinline__ RadNet rad_net(const char *base, const RadLayout &L) {
-    RadNet n;
-    n.w1f = reinterpret_cast<const uint2 *>(base + L.off_w1f);
-    n.w2f = reinterpret_cast<const uint2 *>(base + L.off_w2f);
-    n.w3f = reinterpret_cast<const uint2 *>(base + L.off_w3f);
-    n.w1b = reinterpret_cast<const uint2 *>(base + L.off_w1b);
-    n.w2b = reinterpret_cast<const uint2 *>(base + L.off_w2b);
-    n.w3b = reinterpret_cast<const uint2 *>(base + L.off_w3b);
-    n.b1 = reinterpret_cast<const float *>(base + L.off_b1);
-    n.b2 = reinterpret_cast<const float *>(base + L.off_b2);
-    n.b3 = reinterpret_cast<const float *>(base + L.off_b3);
-    return n;
-}
-
+// Radiance forward on tcgen05 (models/texture.py:23-58 with the dual colour of
+// :100-149): per 128-sample tile, Z1 = X W1^T, ReLU, Z2 = H1 W2^T, ReLU,
+// out = H2 W3^T, sigmoid (+ sigmoid(feature[1:4])).  The next tile's input is
+// staged while the current tile's later layers run.
 template <int KT1>
-__global__ void __launch_bounds__(kRT, 1) rad_fwd_kernel(const __grid_constant__ RadParams P) {
-    extern __shared__ __align__(16) char smem[];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int64_t i = tid * 16; i < P.L.bytes; i += kRT * 16)
-        *reinterpret_cast<uint4 *>(smem + i) = *reinterpret_cast<const uint4 *>(P.net + i);
-    RadWarp &w = reinterpret_cast<RadWarp *>(smem + P.L.bytes)[warp];
-    __syncthreads();
-    const RadNet N = rad_net(smem, P.L);
-    const int r = lane >> 2, q = lane & 3;
-    const int64_t tiles = (P.S + 15) / 16;
-    for (int64_t t = (int64_t)blockIdx.x * kRW + warp; t < tiles; t += (int64_t)gridDim.x * kRW) {
-        const int64_t s0 = t * 16;
-        stage_rows(P, w, s0, lane);
-        uint32_t xh[KT1][4], xl[KT1][4];
-        rows_to_a<KT1>(w, lane, xh, xl);
-        float Z[8][4];
-        uint32_t hh[4][4], hl[4][4];
-        hidden_layer<KT1>(xh, xl, N.w1f, N.b1, lane, Z);
-        activate_relu(Z, hh, hl);
-        hidden_layer<4>(hh, hl, N.w2f, N.b2, lane, Z);
-        activate_relu(Z, hh, hl);
-        float D[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int kt = 0; kt < 4; ++kt) {
-            const int64_t i = (int64_t)kt * 32 + lane;
-            mma_x3(D, hh[kt], hl[kt], N.w3f[i], N.w3f[4 * 32 + i]);
+__global__ void __launch_bounds__(kTcThreads, 1) rad_fwd_tc_kernel(const __grid_constant__ RadParams P) {
+    using Sh = RadShape<KT1>;
+    constexpr int K1 = Sh::K1;
+    extern __shared__ __align__(1024) char smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int row = (warp & 3) * 32 + lane, slice = warp >> 2;
+    const RadLayout &L = P.L;
+    auto copy16 = [&](uint32_t dst, int64_t src, uint32_t bytes) {
+        for (uint32_t i = tid * 16; i < bytes; i += kTcThreads * 16)
+            *reinterpret_cast<uint4 *>(smem + dst + i) = *reinterpret_cast<const uint4 *>(P.net + src + i);
+    };
+    copy16(Sh::off_w1, L.off_tw1, 2 * Sh::w1);
+    copy16(Sh::off_w2, L.off_tw2, 2 * Sh::w2);
+    copy16(Sh::off_w3, L.off_tw3, 2 * Sh::w3);
+    float *vec = reinterpret_cast<float *>(smem + Sh::f_vec);   // b1 [64], b2 [64], b3 [16]
+    for (int i = tid; i < 144; i += kTcThreads)
+        vec[i] = i < 64 ? reinterpret_cast<const float *>(P.net + L.off_b1)[i]
+                 : i < 128 ? reinterpret_cast<const float *>(P.net + L.off_b2)[i - 64]
+                           : reinterpret_cast<const float *>(P.net + L.off_b3)[i - 128];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + Sh::f_bar);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 1);
+    char *xh = smem + Sh::off_x, *xl = xh + Sh::x, *hh = smem + Sh::f_h, *hl = hh + Sh::h;
+    if (warp == 0) {
+        tc::tmem_alloc(slot, 128);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) tc::mbar_init(bar, 1);
+    tc_publish();
+    const uint32_t tmem = *slot;
+    const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+    const uint32_t sW1 = tc::smem_addr(smem + Sh::off_w1), sW2 = tc::smem_addr(smem + Sh::off_w2),
+                   sW3 = tc::smem_addr(smem + Sh::off_w3), sX = tc::smem_addr(xh), sH = tc::smem_addr(hh);
+    const TcOp Xk = op_k(sX, Sh::x, K1), Hk = op_k(sH, Sh::h, 64);
+    const TcOp W1k = op_k(sW1, Sh::w1, K1), W2k = op_k(sW2, Sh::w2, 64), W3k = op_k(sW3, Sh::w3, 64);
+    constexpr uint32_t id64 = tc::idesc_bf16_f32(128, 64), id16 = tc::idesc_bf16_f32(128, 16);
+    uint32_t phase = 0;
+    bool alive = true;
+    const int64_t n_tiles = (P.S + 127) / 128;
+    if ((int64_t)blockIdx.x < n_tiles) rad_stage_x<KT1>(P, blockIdx.x * 128 + row, blockIdx.x * 128 + row < P.S,
+                                                       row, slice, xh, xl);
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const int64_t s = t * 128 + row;
+        const bool v = s < P.S;
+        tc_publish();
+        if (tid == 0) {
+            tc_mma<KT1>(tmem, Xk, W1k, id64, false);
+            tc::commit(bar);
         }
-        const int c = q * 2;
-        if (q < 2) {
+        if (!(alive = tc_wait_all(bar, phase))) break;
+        phase ^= 1;
+        // the input staging is free: the next tile's
+        const int64_t tn = t + gridDim.x;
+        if (tn < n_tiles) rad_stage_x<KT1>(P, tn * 128 + row, tn * 128 + row < P.S, row, slice, xh, xl);
+#pragma unroll 1
+        for (int layer = 0; layer < 2; ++layer) {
+            float z[16];
+            tc::ld16(tmem + lane_off + 64 * layer + 16 * slice, z);
 #pragma unroll
-            for (int rr = 0; rr < 2; ++rr) {
-                const int64_t s = s0 + r + 8 * rr;
-                if (s >= P.S) continue;
+            for (int j = 0; j < 16; ++j) z[j] = fmaxf(z[j] + vec[64 * layer + 16 * slice + j], 0.f);
+            stage16(hh, hl, row, 16 * slice, 64, z);
+            tc_publish();
+            if (tid == 0) {
+                if (layer == 0) tc_mma<4>(tmem + 64, Hk, W2k, id64, false);
+                else tc_mma<4>(tmem, Hk, W3k, id16, false);
+                tc::commit(bar);
+            }
+            if (!(alive = tc_wait_all(bar, phase))) break;
+            phase ^= 1;
+        }
+        if (!alive) break;
+        if (slice == 0) {
+            float o[16];
+            tc::ld16(tmem + lane_off, o);
+            if (v) {
 #pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    const int col = c + k;
-                    if (col >= 3) continue;
-                    float v = sigm(D[2 * rr + k] + N.b3[col]);
-                    if (P.dual) v += sigm(P.feature[s * P.feat_stride + 1 + col]);
-                    P.rgb[s * 3 + col] = v;
+                for (int c = 0; c < 3; ++c) {
+                    float val = sigm(o[c] + vec[128 + c]);
+                    if (P.dual) val += sigm(P.feature[s * P.feat_stride + 1 + c]);
+                    P.rgb[s * 3 + c] = val;
                 }
             }
         }
-        __syncwarp();
+    }
+    if (!alive && tid == 0) atomicAdd(&g_rad_tc_timeouts, 1u);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, 128);
+}
+
+// dL/dX block b (columns 16 b ..) of sample s: dL/dfeature (plus the dual
+// colour's sigmoid term on columns 1..3) and, from the normal columns,
+// dL/dgrad through normalize (models/texture.py:35)
+__device__ __forceinline__ void rad_dx_out(const RadParams &P, int64_t s, int b, const float (&dx)[16],
+                                           const float (&dual_g)[3]) {
+    const int F = P.L.feat_dim;
+    float dn[3] = {0.f, 0.f, 0.f};
+    bool has_n = false;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int c = 16 * b + j;
+        if (c < F) {
+            float o = dx[j];
+            if (P.dual && c >= 1 && c <= 3) o += dual_g[c - 1];
+            P.d_feature[s * P.feat_stride + c] = o;
+        } else if (c >= F + 16 && c < F + 19) {
+            dn[c - F - 16] = dx[j];
+            has_n = true;
+        }
+    }
+    if (!has_n) return;
+    const float *g = P.grad + s * 3;
+    const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    const float den = fmaxf(gn, 1e-12f);
+    float n[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) n[k] = g[k] / den;
+    if (gn >= 1e-12f) {
+        const float nd = n[0] * dn[0] + n[1] * dn[1] + n[2] * dn[2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) P.d_grad[s * 3 + k] = (dn[k] - n[k] * nd) / gn;
+    } else {
+#pragma unroll
+        for (int k = 0; k < 3; ++k) P.d_grad[s * 3 + k] = dn[k] / 1e-12f;
     }
 }
 
+// Radiance backward on tcgen05: the forward recomputed per 128-sample tile,
+// then dY through the output sigmoid, dH2 = dY W3 (rank three, in registers),
+// dH1 = dZ2 W2 with dW2 += dZ2^T H1, db2 and dW3^T += H2^T dY, dX = dZ1 W1
+// with dW1 += dZ1^T X and db1; the weight gradients stay in tensor memory
+// (M = 64 accumulators) for the CTA's whole loop; dX gives dL/dfeature and,
+// through the normalisation, dL/dgrad.
 template <int KT1>
-__global__ void __launch_bounds__(kRT, 1) rad_bwd_kernel(const __grid_constant__ RadParams P) {
-    extern __shared__ __align__(16) char smem[];
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    for (int64_t i = tid * 16; i < P.L.bytes; i += kRT * 16)
-        *reinterpret_cast<uint4 *>(smem + i) = *reinterpret_cast<const uint4 *>(P.net + i);
-    const int K1cols = 16 * KT1;
-    float *acc = reinterpret_cast<float *>(smem + P.L.bytes);
-    const int n1 = 64 * K1cols, n2 = 64 * 64, n3 = 16 * 64;
-    const int n_acc = n1 + n2 + n3 + 64 + 64 + 16;
-    float *dW1 = acc, *dW2 = acc + n1, *dW3 = acc + n1 + n2;
-    float *db1 = acc + n1 + n2 + n3, *db2 = db1 + 64, *db3 = db2 + 64;
-    for (int i = tid; i < n_acc; i += kRT) acc[i] = 0.f;
-    RadWarp &w = reinterpret_cast<RadWarp *>(acc + ((n_acc + 3) / 4) * 4)[warp];
-    __syncthreads();
-    const RadNet N = rad_net(smem, P.L);
-    const int r = lane >> 2, q = lane & 3, c = q * 2;
-    const int F = P.L.feat_dim;
-    const int64_t tiles = (P.S + 15) / 16;
-    for (int64_t t = (int64_t)blockIdx.x * kRW + warp; t < tiles; t += (int64_t)gridDim.x * kRW) {
-        const int64_t s0 = t * 16;
-        stage_rows(P, w, s0, lane);
-        uint32_t xh[KT1][4], xl[KT1][4];
-        rows_to_a<KT1>(w, lane, xh, xl);
-        float Z1[8][4], Z2[8][4];
-        uint32_t h1h[4][4], h1l[4][4], h2h[4][4], h2l[4][4];
-        hidden_layer<KT1>(xh, xl, N.w1f, N.b1, lane, Z1);
-        activate_relu(Z1, h1h, h1l);
-        hidden_layer<4>(h1h, h1l, N.w2f, N.b2, lane, Z2);
-        activate_relu(Z2, h2h, h2l);
-        float D[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-        for (int kt = 0; kt < 4; ++kt) {
-            const int64_t i = (int64_t)kt * 32 + lane;
-            mma_x3(D, h2h[kt], h2l[kt], N.w3f[i], N.w3f[4 * 32 + i]);
+__global__ void __launch_bounds__(kTcThreads, 1) rad_bwd_tc_kernel(const __grid_constant__ RadParams P) {
+    using Sh = RadShape<KT1>;
+    constexpr int K1 = Sh::K1;
+    extern __shared__ __align__(1024) char smem[];
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int row = (warp & 3) * 32 + lane, slice = warp >> 2;
+    const RadLayout &L = P.L;
+    auto copy16 = [&](uint32_t dst, int64_t src, uint32_t bytes) {
+        for (uint32_t i = tid * 16; i < bytes; i += kTcThreads * 16)
+            *reinterpret_cast<uint4 *>(smem + dst + i) = *reinterpret_cast<const uint4 *>(P.net + src + i);
+    };
+    copy16(Sh::off_w1, L.off_tw1, 2 * Sh::w1);
+    copy16(Sh::off_w2, L.off_tw2, 2 * Sh::w2);
+    copy16(Sh::off_w3, L.off_tw3, 2 * Sh::w3);
+    float *vec = reinterpret_cast<float *>(smem + Sh::b_vec);   // b1 [64], b2 [64], b3 [16], W3 [3][64]
+    for (int i = tid; i < 144 + 192; i += kTcThreads)
+        vec[i] = i < 64 ? reinterpret_cast<const float *>(P.net + L.off_b1)[i]
+                 : i < 128 ? reinterpret_cast<const float *>(P.net + L.off_b2)[i - 64]
+                 : i < 144 ? reinterpret_cast<const float *>(P.net + L.off_b3)[i - 128]
+                           : reinterpret_cast<const float *>(P.net + L.off_w3)[i - 144];
+    const float *w3f = vec + 144;
+    uint16_t *ones = reinterpret_cast<uint16_t *>(smem + Sh::b_ones);
+    fill_ones_operand(ones, tid, kTcThreads);
+    float *db3 = reinterpret_cast<float *>(smem + Sh::b_db3);
+    for (int i = tid; i < 16; i += kTcThreads) db3[i] = 0.f;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem + Sh::b_bar);   // [0] epilogue, [1] round
+    uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 2);
+    char *xh = smem + Sh::off_x, *xl = xh + Sh::x, *h1h = smem + Sh::b_h1, *h1l = h1h + Sh::h;
+    char *h2h = smem + Sh::b_h2, *h2l = h2h + Sh::h, *zh = smem + Sh::b_z, *zl = zh + Sh::h;
+    char *yh = smem + Sh::b_y, *yl = yh + Sh::y;
+    if (warp == 0) {
+        tc::tmem_alloc(slot, 512);
+        tc::tmem_relinquish();
+    }
+    if (tid == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+    }
+    tc_publish();
+    const uint32_t tmem = *slot;
+    const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
+    tmem_zero(tmem + lane_off, Sh::tW1, Sh::used, slice);
+    tc_publish();
+    const uint32_t sW1 = tc::smem_addr(smem + Sh::off_w1), sW2 = tc::smem_addr(smem + Sh::off_w2),
+                   sW3 = tc::smem_addr(smem + Sh::off_w3), sX = tc::smem_addr(xh), sH1 = tc::smem_addr(h1h),
+                   sH2 = tc::smem_addr(h2h), sZ = tc::smem_addr(zh), sY = tc::smem_addr(yh),
+                   sOnes = tc::smem_addr(ones);
+    const TcOp W1k = op_k(sW1, Sh::w1, K1), W1t = op_t(sW1, Sh::w1, K1);
+    const TcOp W2k = op_k(sW2, Sh::w2, 64), W2t = op_t(sW2, Sh::w2, 64), W3k = op_k(sW3, Sh::w3, 64);
+    const TcOp Xk = op_k(sX, Sh::x, K1), Xt = op_t(sX, Sh::x, K1);
+    const TcOp H1k = op_k(sH1, Sh::h, 64), H1t = op_t(sH1, Sh::h, 64), H2k = op_k(sH2, Sh::h, 64),
+               H2t = op_t(sH2, Sh::h, 64);
+    const TcOp Zk = op_k(sZ, Sh::h, 64), Zt = op_t(sZ, Sh::h, 64), Yt = op_t(sY, Sh::y, 16),
+               Ones = op_t(sOnes, 0u, 16);
+    constexpr uint32_t id64 = tc::idesc_bf16_f32(128, 64), id_out = tc::idesc_bf16_f32(128, 16);
+    constexpr uint32_t id_dh = tc::idesc_bf16_f32(128, 64, 0, 1), id_dx = tc::idesc_bf16_f32(128, K1, 0, 1);
+    constexpr uint32_t id_w1 = tc::idesc_bf16_f32(64, K1, 1, 1), id_w2 = tc::idesc_bf16_f32(64, 64, 1, 1),
+                       id_16 = tc::idesc_bf16_f32(64, 16, 1, 1);
+    uint32_t ph0 = 0, ph1 = 0;
+    bool alive = true;
+    const int64_t n_tiles = (P.S + 127) / 128;
+    bool first = true;
+    for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
+        const int64_t s = t * 128 + row;
+        const bool v = s < P.S;
+        if (!first) {
+            if (!(alive = tc_wait_all(&bar[1], ph1))) break;
+            ph1 ^= 1;
         }
-        // dL/d(out) through the sigmoid; dual colour: dL/dfeature[1..3]
-        float dY[1][4] = {{0.f, 0.f, 0.f, 0.f}};
-#pragma unroll
-        for (int rr = 0; rr < 2; ++rr) {
-            const int64_t s = s0 + r + 8 * rr;
-#pragma unroll
-            for (int k = 0; k < 2; ++k) {
-                const int col = c + k;
-                if (col >= 3 || s >= P.S) continue;
-                const float g = P.g_rgb[s * 3 + col];
-                const float sg = sigm(D[2 * rr + k] + N.b3[col]);
-                dY[0][2 * rr + k] = g * sg * (1.f - sg);
-                if (P.dual) {
-                    const float sf = sigm(P.feature[s * P.feat_stride + 1 + col]);
-                    w.dual_g[r + 8 * rr][col] = g * sf * (1.f - sf);
-                }
-            }
+        first = false;
+        rad_stage_x<KT1>(P, s, v, row, slice, xh, xl);
+        tc_publish();
+        // forward, recomputed: Z1, Z2, out
+        if (tid == 0) {
+            tc_mma<KT1>(tmem + Sh::tA, Xk, W1k, id64, false);
+            tc::commit(&bar[0]);
         }
-        uint32_t yh[1][4], yl[1][4];
+        if (!(alive = tc_wait_all(&bar[0], ph0))) break;
+        ph0 ^= 1;
+        uint32_t m1 = 0, m2 = 0;   // ReLU masks of this slice
         {
-            const Split a = split2(dY[0][0], dY[0][1]), b = split2(dY[0][2], dY[0][3]);
-            yh[0][0] = a.hi;
-            yl[0][0] = a.lo;
-            yh[0][1] = b.hi;
-            yl[0][1] = b.lo;
-            yh[0][2] = yh[0][3] = yl[0][2] = yl[0][3] = 0u;
+            float z[16];
+            tc::ld16(tmem + lane_off + Sh::tA + 16 * slice, z);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                z[j] += vec[16 * slice + j];
+                m1 |= (z[j] > 0.f ? 1u : 0u) << j;
+                z[j] = fmaxf(z[j], 0.f);
+            }
+            stage16(h1h, h1l, row, 16 * slice, 64, z);
         }
-        float dH[8][4];
-        mm_nobias<1, 8>(yh, yl, N.w3b, 8, lane, dH);
-        accumulate_dw<1, 4>(yh, yl, h2h, h2l, dW3, 64, lane);
-        accumulate_db<1>(dY, db3, lane);
+        tc_publish();
+        if (tid == 0) {
+            tc_mma<4>(tmem + Sh::tB, H1k, W2k, id64, false);
+            tc::commit(&bar[0]);
+        }
+        if (!(alive = tc_wait_all(&bar[0], ph0))) break;
+        ph0 ^= 1;
+        {
+            float z[16];
+            tc::ld16(tmem + lane_off + Sh::tB + 16 * slice, z);
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+            for (int j = 0; j < 16; ++j) {
+                z[j] += vec[64 + 16 * slice + j];
+                m2 |= (z[j] > 0.f ? 1u : 0u) << j;
+                z[j] = fmaxf(z[j], 0.f);
+            }
+            stage16(h2h, h2l, row, 16 * slice, 64, z);
+        }
+        tc_publish();
+        if (tid == 0) {
+            tc_mma<4>(tmem + Sh::tA, H2k, W3k, id_out, false);
+            tc::commit(&bar[0]);
+        }
+        if (!(alive = tc_wait_all(&bar[0], ph0))) break;
+        ph0 ^= 1;
+        // dL/d(out) through the sigmoid, dH2 = dY W3, dZ2; the dual colour's
+        // dL/dfeature[1..3] is kept by slice 0 for the dX epilogue
+        float dual_g[3] = {0.f, 0.f, 0.f};
+        {
+            float o[16], dy[3];
+            tc::ld16(tmem + lane_off + Sh::tA, o);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) dH[nt][i] = Z2[nt][i] > 0.f ? dH[nt][i] : 0.f;
-        uint32_t dzh[4][4], dzl[4][4];
-        c_to_a(dH, dzh, dzl);
-        accumulate_dw<4, 4>(dzh, dzl, h1h, h1l, dW2, 64, lane);
-        accumulate_db<8>(dH, db2, lane);
-        mm_nobias<4, 8>(dzh, dzl, N.w2b, 8, lane, dH);
+            for (int c = 0; c < 3; ++c) {
+                const float sg = sigm(o[c] + vec[128 + c]);
+                dy[c] = v ? P.g_rgb[s * 3 + c] * sg * (1.f - sg) : 0.f;
+            }
+            float dz[16];
 #pragma unroll
-        for (int nt = 0; nt < 8; ++nt)
+            for (int j = 0; j < 16; ++j) {
+                const int u = 16 * slice + j;
+                const float dh = dy[0] * w3f[u] + dy[1] * w3f[64 + u] + dy[2] * w3f[128 + u];
+                dz[j] = (m2 >> j) & 1u ? dh : 0.f;
+            }
+            stage16(zh, zl, row, 16 * slice, 64, dz);
+            if (slice == 0) {
+                float yv[16];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) dH[nt][i] = Z1[nt][i] > 0.f ? dH[nt][i] : 0.f;
-        c_to_a(dH, dzh, dzl);
-        accumulate_dw<4, KT1>(dzh, dzl, xh, xl, dW1, K1cols, lane);
-        accumulate_db<8>(dH, db1, lane);
-        float dX[2 * KT1][4];
-        mm_nobias<4, 2 * KT1>(dzh, dzl, N.w1b, 2 * KT1, lane, dX);
-        __syncwarp();
-        // dL/dfeature and dL/dnormal
+                for (int j = 0; j < 16; ++j) yv[j] = j < 3 ? dy[j] : 0.f;
+                stage16(yh, yl, row, 0, 16, yv);
 #pragma unroll
-        for (int nt = 0; nt < 2 * KT1; ++nt) {
+                for (int c = 0; c < 3; ++c) {
+                    float a = dy[c];
 #pragma unroll
-            for (int rr = 0; rr < 2; ++rr) {
-                const int row = r + 8 * rr;
-                const int64_t s = s0 + row;
-                if (s >= P.S) continue;
+                    for (int off = 1; off < 32; off <<= 1) a += __shfl_xor_sync(0xffffffffu, a, off);
+                    if (lane == 0 && a != 0.f) red_add(db3 + c, a);
+                }
+                if (P.dual && v) {
 #pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    const int col = nt * 8 + c + k;
-                    const float v = dX[nt][2 * rr + k];
-                    if (col < F) {
-                        float o = v;
-                        if (P.dual && col >= 1 && col <= 3) o += w.dual_g[row][col - 1];
-                        P.d_feature[s * P.feat_stride + col] = o;
-                    } else if (col >= F + 16 && col < F + 19) {
-                        w.dn[row][col - F - 16] = v;
+                    for (int c = 0; c < 3; ++c) {
+                        const float sf = sigm(P.feature[s * P.feat_stride + 1 + c]);
+                        dual_g[c] = P.g_rgb[s * 3 + c] * sf * (1.f - sf);
                     }
                 }
             }
         }
-        __syncwarp();
-        if (lane < 16 && s0 + lane < P.S) {
-            const int64_t s = s0 + lane;
-            const float *g = P.grad + s * 3;
-            const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-            const float den = fmaxf(gn, 1e-12f);
-            float n[3], dn[3];
-            for (int k = 0; k < 3; ++k) {
-                n[k] = g[k] / den;
-                dn[k] = w.dn[lane][k];
-            }
-            if (gn >= 1e-12f) {
-                const float nd = n[0] * dn[0] + n[1] * dn[1] + n[2] * dn[2];
-                for (int k = 0; k < 3; ++k) P.d_grad[s * 3 + k] = (dn[k] - n[k] * nd) / gn;
-            } else {
-                for (int k = 0; k < 3; ++k) P.d_grad[s * 3 + k] = dn[k] / 1e-12f;
+        tc_publish();
+        // dH1 (epilogue), then dW2, db2, dW3
+        if (tid == 0) {
+            tc_mma<4>(tmem + Sh::tA, Zk, W2t, id_dh, false);
+            tc::commit(&bar[0]);
+            tc_mma<8>(tmem + Sh::tW2, Zt, H1t, id_w2, true);
+            tc_mma<8>(tmem + Sh::tb2, Zt, Ones, id_16, true, true);
+            tc_mma<8>(tmem + Sh::tW3, H2t, Yt, id_16, true);
+            tc::commit(&bar[1]);
+        }
+        if (!(alive = tc_wait_all(&bar[0], ph0))) break;
+        ph0 ^= 1;
+        {
+            float dz[16];
+            tc::ld16(tmem + lane_off + Sh::tA + 16 * slice, dz);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) dz[j] = (m1 >> j) & 1u ? dz[j] : 0.f;
+            if (!(alive = tc_wait_all(&bar[1], ph1))) break;
+            ph1 ^= 1;
+            stage16(h1h, h1l, row, 16 * slice, 64, dz);   // H1 -> dZ1
+        }
+        tc_publish();
+        // dX (epilogue), then dW1, db1
+        if (tid == 0) {
+            tc_mma<4>(tmem + Sh::tB, H1k, W1t, id_dx, false);
+            tc::commit(&bar[0]);
+            tc_mma<8>(tmem + Sh::tW1, H1t, Xt, id_w1, true);
+            tc_mma<8>(tmem + Sh::tb1, H1t, Ones, id_16, true, true);
+            tc::commit(&bar[1]);
+        }
+        if (!(alive = tc_wait_all(&bar[0], ph0))) break;
+        ph0 ^= 1;
+        for (int b = slice; b < KT1; b += 4) {
+            float dx[16];
+            __syncwarp();
+            tc::ld16(tmem + lane_off + Sh::tB + 16 * b, dx);
+            if (v) rad_dx_out(P, s, b, dx, dual_g);
+        }
+    }
+    if (alive && !first) alive = tc_wait_all(&bar[1], ph1);
+    if (alive) {
+        // add the CTA's gradients: tensor-memory rows 16 (warp % 4) + lane
+        const int unit = 16 * (warp & 3) + lane;
+        float *dW2 = P.d_net + 64 * K1, *dW3 = dW2 + 64 * 64, *db1 = dW3 + 16 * 64, *db2 = db1 + 64,
+              *dB3 = db2 + 64;
+        for (uint32_t c0 = Sh::tW1 + 16 * slice; c0 < Sh::used; c0 += 64) {
+            float w[16];
+            __syncwarp();
+            tc::ld16(tmem + lane_off + c0, w);
+#pragma unroll
+            for (int j = 0; j < 16 && lane < 16; ++j) {
+                const uint32_t c = c0 + j;
+                float *dst = nullptr;
+                if (c < Sh::tW2) dst = P.d_net + unit * K1 + (c - Sh::tW1);
+                else if (c < Sh::tW3) dst = dW2 + unit * 64 + (c - Sh::tW2);
+                else if (c < Sh::tb1) dst = dW3 + (c - Sh::tW3) * 64 + unit;
+                else if (c == Sh::tb1) dst = db1 + unit;
+                else if (c == Sh::tb2) dst = db2 + unit;
+                if (dst && w[j] != 0.f) atomicAdd(dst, w[j]);
             }
         }
-        __syncwarp();
+        for (int o = tid; o < 16; o += kTcThreads)
+            if (db3[o] != 0.f) atomicAdd(dB3 + o, db3[o]);
     }
+    if (!alive && tid == 0) atomicAdd(&g_rad_tc_timeouts, 1u);
+    tc::fence_before_sync();
     __syncthreads();
-    for (int i = tid; i < n_acc; i += kRT) {
-        const float v = acc[i];
-        if (v != 0.f) atomicAdd(P.d_net + i, v);
-    }
+    if (warp == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 // ------------------------------------------------------------ compositing
@@ -631,6 +792,19 @@ __global__ void __launch_bounds__(256) comp_bwd_kernel(const __grid_constant__ C
 
 // ------------------------------------------------------------------ host API
 
+namespace angelo {
+// CTAs of the radiance kernels that stopped waiting for the tensor cores
+int64_t radiance_tc_timeouts(int reset) {
+    unsigned int v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_rad_tc_timeouts, sizeof(v)) != cudaSuccess) return -1;
+    if (reset) {
+        const unsigned int z = 0;
+        if (cudaMemcpyToSymbol(g_rad_tc_timeouts, &z, sizeof(z)) != cudaSuccess) return -1;
+    }
+    return (int64_t)v;
+}
+}  // namespace angelo
+
 extern "C" int64_t angelo_radiance_net_bytes(int32_t feat_dim) {
     if (feat_dim < 1 || feat_dim + 19 > kXCols) return -1;
     return rad_layout(feat_dim).bytes;
@@ -648,8 +822,7 @@ extern "C" int angelo_radiance_prep(int32_t feat_dim, const float *W1, const flo
                    feat_dim);
     ANGELO_REQUIRE(W1 && b1 && W2 && b2 && W3 && b3 && net, "radiance_prep: null pointer");
     const RadLayout L = rad_layout(feat_dim);
-    const int frags = L.k_tiles1 * 8 + 32 + 4 + 4 * 2 * L.k_tiles1 + 32 + 8 + 5;
-    rad_prep_kernel<<<blocks_for((int64_t)frags * 32, 256), 256, 0, as_stream(stream)>>>(
+    rad_prep_kernel<<<blocks_for(rad_prep_threads(L), 256), 256, 0, as_stream(stream)>>>(
         W1, b1, W2, b2, W3, b3, L, reinterpret_cast<char *>(net));
     return check_launch("radiance_prep");
 }
@@ -657,22 +830,25 @@ extern "C" int angelo_radiance_prep(int32_t feat_dim, const float *W1, const flo
 namespace {
 template <int KT1, bool BWD>
 int launch_rad(const RadParams &P, cudaStream_t st) {
-    const int n_acc = 64 * 16 * KT1 + 64 * 64 + 16 * 64 + 64 + 64 + 16;
-    const size_t smem = P.L.bytes + (BWD ? ((n_acc + 3) / 4) * 16 : 0) + kRW * sizeof(RadWarp);
-    auto k = BWD ? rad_bwd_kernel<KT1> : rad_fwd_kernel<KT1>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    using Sh = RadShape<KT1>;
+    const size_t smem = BWD ? Sh::b_bytes : Sh::f_bytes;
+    auto k = BWD ? rad_bwd_tc_kernel<KT1> : rad_fwd_tc_kernel<KT1>;
+    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
         return check_launch("radiance(smem attribute)");
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kRT, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kTcThreads, smem);
     if (per_sm < 1) {
         set_error("radiance: %zu bytes of shared memory do not fit an SM", smem);
         return ANGELO_E_UNSUPPORTED;
     }
-    const int64_t want = ((P.S + 15) / 16 + kRW - 1) / kRW;
-    const int grid = (int)std::min<int64_t>(want, (int64_t)sms * per_sm);
-    k<<<grid, kRT, smem, st>>>(P);
+    // tensor memory: the backward holds all 512 columns of an SM, the forward 128
+    per_sm = std::min(per_sm, BWD ? 1 : 4);
+    const int64_t tiles = (P.S + 127) / 128;
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)sms * per_sm);
+    k<<<grid, kTcThreads, smem, st>>>(P);
     return check_launch(BWD ? "radiance_bwd" : "radiance_fwd");
 }
 

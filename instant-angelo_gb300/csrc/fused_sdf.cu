@@ -36,6 +36,7 @@
 #include "common.cuh"
 #include "mlp.cuh"
 #include "tc.cuh"
+#include "tc_mlp.cuh"
 
 using namespace angelo;
 
@@ -309,9 +310,6 @@ __device__ __forceinline__ float fd_grad(const float *s6, float eps, float g[3])
 
 __device__ unsigned int g_tc_timeouts;   // CTAs that stopped waiting for the tensor cores
 
-constexpr uint32_t kTcWaitPolls = 1u << 24;
-constexpr int kTcThreads = 512;
-
 template <int KH, int NH, int NT3>
 struct TcFwdShape {
     static constexpr int K1 = 16 * (KH + 1);
@@ -325,57 +323,6 @@ struct TcFwdShape {
                               bytes = off_bar + 16;
     static constexpr uint32_t tmem_cols = 256;   // Z1 [0, 64), Z2 [64, 128), output [128, 128 + N3)
 };
-
-// D (128 x N) = A (128 x 16 KSTEPS) * B (N x 16 KSTEPS)^T in bf16x3, one thread
-template <int KSTEPS>
-__device__ __forceinline__ void tc_layer(uint32_t d_tmem, uint32_t a_hi, uint32_t a_lo, uint32_t a_sbo,
-                                         uint32_t b_hi, uint32_t b_lo, uint32_t b_sbo, uint32_t idesc) {
-#pragma unroll
-    for (int ks = 0; ks < KSTEPS; ++ks) {
-        const uint32_t o = ks * 256;
-        const uint64_t ah = tc::smem_desc(a_hi + o, 128, a_sbo), al = tc::smem_desc(a_lo + o, 128, a_sbo);
-        const uint64_t bh = tc::smem_desc(b_hi + o, 128, b_sbo), bl = tc::smem_desc(b_lo + o, 128, b_sbo);
-        tc::mma_bf16(d_tmem, al, bh, idesc, ks > 0 ? 1u : 0u);
-        tc::mma_bf16(d_tmem, ah, bl, idesc, 1u);
-        tc::mma_bf16(d_tmem, ah, bh, idesc, 1u);
-    }
-}
-
-// Every thread waits for the mbarrier phase; false (the same in every thread)
-// when some thread gave up.
-__device__ __forceinline__ bool tc_wait_all(uint64_t *bar, uint32_t phase) {
-    const bool ok = tc::mbar_wait(bar, phase, kTcWaitPolls);
-    const int failed = __syncthreads_or(!ok);
-    tc::fence_after_sync();
-    return failed == 0;
-}
-
-// Operand writes of every thread visible to the tensor cores, then thread 0
-// may issue (after this, all threads have also finished their tensor-memory
-// reads of the previous phase).
-__device__ __forceinline__ void tc_publish() {
-    tc::fence_proxy_async_smem();
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-}
-
-// 16 consecutive columns c0 .. c0 + 15 (c0 % 16 == 0) of row r of a K-major
-// operand with K columns, split into bf16 hi and lo
-__device__ __forceinline__ void stage16(char *hi, char *lo, int r, int c0, int K, const float (&v)[16]) {
-    uint32_t h[8], l[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const Split sp = split2(v[2 * i], v[2 * i + 1]);
-        h[i] = sp.hi;
-        l[i] = sp.lo;
-    }
-    const uint32_t o0 = tc::kmajor_offset(r, c0, K), o1 = tc::kmajor_offset(r, c0 + 8, K);
-    *reinterpret_cast<uint4 *>(hi + o0) = make_uint4(h[0], h[1], h[2], h[3]);
-    *reinterpret_cast<uint4 *>(hi + o1) = make_uint4(h[4], h[5], h[6], h[7]);
-    *reinterpret_cast<uint4 *>(lo + o0) = make_uint4(l[0], l[1], l[2], l[3]);
-    *reinterpret_cast<uint4 *>(lo + o1) = make_uint4(l[4], l[5], l[6], l[7]);
-}
 
 template <int KH, int NH, int NT3, int GROUP>
 __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid_constant__ SdfParams P) {
@@ -477,7 +424,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
         {
             tc_publish();
             if (tid == 0) {
-                tc_layer<K1 / 16>(tmem, sA1h, sA1l, 16 * K1, sW1h, sW1l, 16 * K1, id_hidden);
+                tc_mma<K1 / 16>(tmem, op_k(sA1h, Sh::a1, K1), op_k(sW1h, Sh::w1, K1), id_hidden, false);
                 tc::commit(bar);
             }
             if (!(alive = tc_wait_all(bar, phase))) break;
@@ -499,11 +446,11 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
                 tc_publish();
                 if (tid == 0) {
                     if (layer + 1 < NH)
-                        tc_layer<4>(tmem + 64, sA2h, sA2l, 1024, sW2h, sW2l, 1024, id_hidden);
+                        tc_mma<4>(tmem + 64, op_k(sA2h, Sh::a2, 64), op_k(sW2h, Sh::w2, 64), id_hidden, false);
                     else if (GROUP != kCurv && e == 0 && P.with_feature)
-                        tc_layer<4>(tmem + 128, sA2h, sA2l, 1024, sW3h, sW3l, 1024, id_out_main);
+                        tc_mma<4>(tmem + 128, op_k(sA2h, Sh::a2, 64), op_k(sW3h, Sh::w3, 64), id_out_main, false);
                     else
-                        tc_layer<4>(tmem + 128, sA2h, sA2l, 1024, sW3h, sW3l, 1024, id_out_tap);
+                        tc_mma<4>(tmem + 128, op_k(sA2h, Sh::a2, 64), op_k(sW3h, Sh::w3, 64), id_out_tap, false);
                     tc::commit(bar);
                 }
                 if (!(alive = tc_wait_all(bar, phase))) break;
@@ -643,65 +590,6 @@ struct TcBwdShape {
                               tmem_cols = used <= 256 ? 256 : 512;
 };
 
-// an operand staged as bf16 [rows][C] (kmajor_offset(r, c, C)), hi and lo
-// halves `half` bytes apart, as the descriptor fields of one K step of 16
-struct TcOp {
-    uint32_t hi, lo, lbo, sbo, step;
-};
-// read K-major: K = C, M (or N) = rows
-__device__ __forceinline__ TcOp op_k(uint32_t hi, uint32_t half, int C) {
-    return TcOp{hi, hi + half, 128u, 16u * (uint32_t)C, 256u};
-}
-// read as the transposed operand (MN-major): M (or N) = C, K = rows
-__device__ __forceinline__ TcOp op_t(uint32_t hi, uint32_t half, int C) {
-    return TcOp{hi, hi + half, 16u * (uint32_t)C, 128u, 32u * (uint32_t)C};
-}
-
-// D (+)= A B^T over KSTEPS steps of 16 in bf16x3 (lo*hi + hi*lo + hi*hi); with
-// b_exact, B is exact in bf16 and its lo product is left out.  One thread.
-template <int KSTEPS>
-__device__ __forceinline__ void tc_mma(uint32_t d, const TcOp &a, const TcOp &b, uint32_t idesc, bool acc,
-                                       bool b_exact = false) {
-#pragma unroll
-    for (int ks = 0; ks < KSTEPS; ++ks) {
-        const uint64_t ah = tc::smem_desc(a.hi + ks * a.step, a.lbo, a.sbo);
-        const uint64_t al = tc::smem_desc(a.lo + ks * a.step, a.lbo, a.sbo);
-        const uint64_t bh = tc::smem_desc(b.hi + ks * b.step, b.lbo, b.sbo);
-        tc::mma_bf16(d, al, bh, idesc, (acc || ks > 0) ? 1u : 0u);
-        if (!b_exact) tc::mma_bf16(d, ah, tc::smem_desc(b.lo + ks * b.step, b.lbo, b.sbo), idesc, 1u);
-        tc::mma_bf16(d, ah, bh, idesc, 1u);
-    }
-}
-
-// Column sums over the warp's 32 lanes of v[0..15] (lane = row): afterwards
-// lanes 2c and 2c + 1 hold the sum of column col(2c), 16 shuffles.
-__device__ __forceinline__ float warp_colsum16(const float (&v)[16], int lane, int *col) {
-    float a[8], b[4], c[2];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-        const bool up = lane & 16;
-        const float keep = up ? v[j + 8] : v[j], send = up ? v[j] : v[j + 8];
-        a[j] = keep + __shfl_xor_sync(0xffffffffu, send, 16);
-    }
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const bool up = lane & 8;
-        const float keep = up ? a[j + 4] : a[j], send = up ? a[j] : a[j + 4];
-        b[j] = keep + __shfl_xor_sync(0xffffffffu, send, 8);
-    }
-#pragma unroll
-    for (int j = 0; j < 2; ++j) {
-        const bool up = lane & 4;
-        const float keep = up ? b[j + 2] : b[j], send = up ? b[j] : b[j + 2];
-        c[j] = keep + __shfl_xor_sync(0xffffffffu, send, 4);
-    }
-    const bool up = lane & 2;
-    float r = (up ? c[1] : c[0]) + __shfl_xor_sync(0xffffffffu, up ? c[0] : c[1], 2);
-    r += __shfl_xor_sync(0xffffffffu, r, 1);
-    *col = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
-    return r;
-}
-
 // dL/dsdf of the evaluations of GROUP of sample s (ds[e - e0]), from the
 // incoming gradients and the stencil state kept by the forward; the curvature
 // group stores dL/dnormal of the curvature for the FD pass (bstate 3..5).
@@ -800,8 +688,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
         vec[i] = v;
     }
     uint16_t *ones = reinterpret_cast<uint16_t *>(smem + Sh::off_ones);
-    for (int i = tid; i < 128 * 16; i += kTcThreads)
-        ones[tc::kmajor_offset(i >> 4, i & 15, 16) >> 1] = (i & 15) == 0 ? (uint16_t)0x3F80u : (uint16_t)0u;
+    fill_ones_operand(ones, tid, kTcThreads);
     float *ds = reinterpret_cast<float *>(smem + Sh::off_ds);
     float *db3 = reinterpret_cast<float *>(smem + Sh::off_db3);
     for (int i = tid; i < N3; i += kTcThreads) db3[i] = 0.f;
@@ -824,7 +711,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
     const uint32_t tmem = *slot;
     const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
     // the CTA-resident gradient accumulators start at zero
-    for (uint32_t b = slice; b < (Sh::used - Sh::tW1) / 16; b += 4) tc::st16_zero(tmem + lane_off + Sh::tW1 + 16 * b);
+    tmem_zero(tmem + lane_off, Sh::tW1, Sh::used, slice);
     tc_publish();
 
     const uint32_t sW1 = tc::smem_addr(smem + Sh::off_w1), sW2 = tc::smem_addr(smem + Sh::off_w2),
@@ -1417,6 +1304,10 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
     return ANGELO_E_UNSUPPORTED;
 }
 
+namespace angelo {
+int64_t radiance_tc_timeouts(int reset);   // fused_render.cu
+}
+
 extern "C" int64_t angelo_tc_timeouts(int32_t reset) {
     unsigned int v = 0;
     if (cudaMemcpyFromSymbol(&v, g_tc_timeouts, sizeof(v)) != cudaSuccess) return -1;
@@ -1424,7 +1315,8 @@ extern "C" int64_t angelo_tc_timeouts(int32_t reset) {
         const unsigned int z = 0;
         if (cudaMemcpyToSymbol(g_tc_timeouts, &z, sizeof(z)) != cudaSuccess) return -1;
     }
-    return (int64_t)v;
+    const int64_t r = angelo::radiance_tc_timeouts(reset);
+    return r < 0 ? -1 : (int64_t)v + r;
 }
 
 extern "C" int64_t angelo_sdf_grad_size(const angelo_sdf_net_layout *nl) {
