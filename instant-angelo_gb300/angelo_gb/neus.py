@@ -65,10 +65,16 @@ class OccupancyGrid(nn.Module):
         self.res = int(resolution)
         self.num_cells = self.res ** 3
         self.register_buffer("roi_aabb", torch.as_tensor(roi_aabb, dtype=torch.float32).clone())
+        # host copy of the box, so that a march needs no device read
+        self.roi = tuple(float(v) for v in self.roi_aabb)
         self.register_buffer("occs", torch.zeros(self.num_cells))
         self.register_buffer("bits", torch.zeros((self.num_cells + 31) // 32, dtype=torch.int32))
         self.contraction_type = contraction_type
         self.jitter_fn = lambda t: torch.rand_like(t, dtype=torch.float32)
+
+    def _load_from_state_dict(self, state_dict, prefix, *args, **kwargs):
+        super()._load_from_state_dict(state_dict, prefix, *args, **kwargs)
+        self.roi = tuple(float(v) for v in self.roi_aabb.cpu())
 
     @property
     def binary(self):
@@ -229,7 +235,7 @@ class NeuSModel(nn.Module):
                 t_min = t_min + self.stratified_fn(t_min) * self.render_step_size
             if self.config.grid_prune:
                 g = self.occupancy_grid
-                grid = dict(roi=g.roi_aabb.tolist(), res=(g.res,) * 3, bits=g.bits)
+                grid = dict(roi=g.roi, res=(g.res,) * 3, bits=g.bits)
             else:
                 grid = dict(roi=ops.UNBOUNDED_ROI, res=(1, 1, 1), bits=None)
             ri, t0, t1, offsets, _ = ops.march(rays_o, rays_d, t_min, t_max, self.render_step_size,

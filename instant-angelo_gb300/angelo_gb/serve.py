@@ -110,7 +110,7 @@ def _t_range(model, o, d):
 def _grid_desc(model):
     if model.config.grid_prune:
         g = model.occupancy_grid
-        return ops.make_grid_desc(g.roi_aabb.tolist(), (g.res,) * 3, g.bits)
+        return ops.make_grid_desc(g.roi, (g.res,) * 3, g.bits)
     return ops.make_grid_desc(ops.UNBOUNDED_ROI, (1, 1, 1), None)
 
 
@@ -137,7 +137,7 @@ def render_exact(model, rays, bg):
     t_min, t_max = _t_range(model, o, d)
     if model.config.grid_prune:
         g = model.occupancy_grid
-        grid = dict(roi=g.roi_aabb.tolist(), res=(g.res,) * 3, bits=g.bits)
+        grid = dict(roi=g.roi, res=(g.res,) * 3, bits=g.bits)
     else:
         grid = dict(roi=ops.UNBOUNDED_ROI, res=(1, 1, 1), bits=None)
     ri, t0, t1, offsets, _ = ops.march(o, d, t_min, t_max, model.render_step_size, cone_angle=0.0,

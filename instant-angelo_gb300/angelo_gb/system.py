@@ -6,7 +6,6 @@ Lightning loop are outside the path."""
 from __future__ import annotations
 
 import torch
-import torch.nn.functional as F
 
 from .config import scheduled_value, to_config
 from .optim import AdamW
@@ -15,8 +14,10 @@ from .optim import AdamW
 def loss_terms(out, rgb, eikonal_weight=0.1, curvature_weight=5e-4, rgb_mse_weight=10.0):
     """Weighted loss terms of systems/neus.py:130-159 (the ones the hot path
     seeds).  Returns (total, dict of unweighted terms)."""
-    valid = out["rays_valid_full"][..., 0]
-    l_rgb = F.mse_loss(out["comp_rgb_full"][valid], rgb[valid])
+    # F.mse_loss over the valid rays (systems/neus.py:130), as a masked
+    # mean: no device-to-host read of the valid count inside the step
+    valid = out["rays_valid_full"][..., 0:1].to(rgb.dtype)
+    l_rgb = (((out["comp_rgb_full"] - rgb) ** 2) * valid).sum() / (valid.sum() * rgb.shape[-1])
     l_eik = ((torch.linalg.norm(out["sdf_grad_samples"], ord=2, dim=-1) - 1.0) ** 2).mean()
     total = l_rgb * rgb_mse_weight + l_eik * eikonal_weight
     terms = {"rgb_mse": l_rgb, "eikonal": l_eik}
