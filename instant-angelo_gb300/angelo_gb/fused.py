@@ -371,7 +371,7 @@ def neus_forward(model, rays_o, rays_d, ri, t0, t1, offsets, n_rays):
     out = {
         "comp_rgb": comp_rgb, "comp_normal": comp_normal, "opacity": opacity, "depth": depth,
         "rays_valid": opacity > 0,
-        "num_samples": torch.as_tensor([len(t0)], dtype=torch.int32, device=rays_o.device),
+        "num_samples": torch.full((1,), len(t0), dtype=torch.int32, device=rays_o.device),
     }
     if model.training:
         out.update({"sdf_samples": sdf, "sdf_grad_samples": sdf_grad, "weights": weights,
@@ -408,7 +408,7 @@ def _plain_render(model, rays_o, rays_d, ray_indices, t0, t1, offsets, sdf, sdf_
     comp_normal = torch.where(rays_fg, comp_normal, torch.zeros_like(comp_normal))
     out = {"comp_rgb": comp_rgb, "comp_normal": comp_normal, "opacity": opacity, "depth": depth,
            "rays_valid": opacity > 0,
-           "num_samples": torch.as_tensor([len(t0)], dtype=torch.int32, device=rays_o.device)}
+           "num_samples": torch.full((1,), len(t0), dtype=torch.int32, device=rays_o.device)}
     if model.training:
         out.update({"sdf_samples": sdf, "sdf_grad_samples": sdf_grad,
                     "weights": weights.view(-1), "points": mid.view(-1),

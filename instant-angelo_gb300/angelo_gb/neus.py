@@ -274,7 +274,7 @@ class NeuSModel(nn.Module):
         out = {
             "comp_rgb": comp_rgb, "comp_normal": comp_normal, "opacity": opacity,
             "depth": depth, "rays_valid": opacity > 0,
-            "num_samples": torch.as_tensor([len(t0)], dtype=torch.int32, device=rays.device),
+            "num_samples": torch.full((1,), len(t0), dtype=torch.int32, device=rays.device),
         }
         if self.training:
             out.update({"sdf_samples": sdf, "sdf_grad_samples": sdf_grad,

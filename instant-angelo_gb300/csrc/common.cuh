@@ -38,6 +38,36 @@ inline unsigned blocks_for(int64_t n, int threads) {
     return (unsigned)((n + threads - 1) / threads);
 }
 
+// Launch configuration of a persistent kernel with `smem` bytes of dynamic
+// shared memory, set up once per device (attributes, occupancy, SM count)
+// and reused by later launches on that device.
+struct PersistentLaunch {
+    int device = -1;
+    int per_sm = 0;
+    int sms = 0;
+};
+
+template <typename K>
+inline int persistent_setup(K kernel, size_t smem, int threads, PersistentLaunch &c, const char *what) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return check_launch(what);
+    if (c.device == dev) return ANGELO_OK;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+        cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
+        return check_launch(what);
+    int per_sm = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (per_sm < 1) {
+        set_error("%s: %zu bytes of shared memory do not fit an SM", what, smem);
+        return ANGELO_E_UNSUPPORTED;
+    }
+    c.per_sm = per_sm;
+    c.sms = sms > 0 ? sms : 1;
+    c.device = dev;
+    return ANGELO_OK;
+}
+
 // ------------------------------------------------------------- hash grid math
 //
 // tcnn HashGrid per-level arithmetic for 3 input dims (the reference's

@@ -1,11 +1,12 @@
 // Fused radiance network and fused compositing.
 //
-// Radiance (models/texture.py:23-58): per sample the input row
-// [feature, SH4((d+1)/2), normalize(grad)] is staged in shared memory, the
-// ReLU MLP runs on tensor cores (bf16x3, fp32 accumulation), and the output
-// sigmoid (plus sigmoid(feature[1:4]) for the dual-colour network) is applied
-// in the epilogue.  The backward recomputes the activations from the same
-// inputs (no stash) and returns dL/dfeature, dL/dgrad and dL/dW.
+// Radiance (models/texture.py:23-58): per 128-sample tile the input rows
+// [feature, SH4((d+1)/2), normalize(grad)] are staged in shared memory as
+// bf16 hi/lo operands, the ReLU MLP runs on the tcgen05 tensor cores (bf16x3,
+// fp32 accumulation in tensor memory), and the output sigmoid (plus
+// sigmoid(feature[1:4]) for the dual-colour network) is applied in the
+// epilogue.  The backward recomputes the activations from the same inputs (no
+// stash) and returns dL/dfeature, dL/dgrad and dL/dW.
 //
 // Compositing (models/neus.py:117-139, 234-248 with nerfacc 0.3.3 weights):
 // one warp per ray walks the ray's samples in chunks of 32: NeuS alpha from
@@ -833,21 +834,13 @@ int launch_rad(const RadParams &P, cudaStream_t st) {
     using Sh = RadShape<KT1>;
     const size_t smem = BWD ? Sh::b_bytes : Sh::f_bytes;
     auto k = BWD ? rad_bwd_tc_kernel<KT1> : rad_fwd_tc_kernel<KT1>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
-        return check_launch("radiance(smem attribute)");
-    int dev = 0, sms = 0, per_sm = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kTcThreads, smem);
-    if (per_sm < 1) {
-        set_error("radiance: %zu bytes of shared memory do not fit an SM", smem);
-        return ANGELO_E_UNSUPPORTED;
-    }
+    static PersistentLaunch cfg;
+    const int rc = persistent_setup(k, smem, kTcThreads, cfg, BWD ? "radiance_bwd" : "radiance_fwd");
+    if (rc != ANGELO_OK) return rc;
     // tensor memory: the backward holds all 512 columns of an SM, the forward 128
-    per_sm = std::min(per_sm, BWD ? 1 : 4);
+    const int per_sm = std::min(cfg.per_sm, BWD ? 1 : 4);
     const int64_t tiles = (P.S + 127) / 128;
-    const int grid = (int)std::min<int64_t>(tiles, (int64_t)sms * per_sm);
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)cfg.sms * per_sm);
     k<<<grid, kTcThreads, smem, st>>>(P);
     return check_launch(BWD ? "radiance_bwd" : "radiance_fwd");
 }

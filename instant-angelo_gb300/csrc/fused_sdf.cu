@@ -1134,12 +1134,6 @@ namespace {
 constexpr int kSmallKH = 1, kSmallNH = 1, kSmallNT3 = 2;   // 8 levels, 1 hidden layer, 13 outputs
 constexpr int kFullKH = 2, kFullNH = 2, kFullNT3 = 9;      // 16 levels, 2 hidden layers, 65 outputs
 
-int sm_count() {
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return std::max(sms, 1);
-}
 
 template <int GROUP>
 int launch_encode(const SdfParams &P, cudaStream_t s) {
@@ -1161,44 +1155,31 @@ template <int KH, int NH, int NT3, int GROUP>
 int launch_mlp_fwd(const SdfParams &P, cudaStream_t s) {
     const size_t smem = TcFwdShape<KH, NH, NT3>::bytes;
     auto k = sdf_mlp_fwd_kernel<KH, NH, NT3, GROUP>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
-        return check_launch("sdf_mlp_fwd(smem attribute)");
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kTcThreads, smem);
-    if (per_sm < 1) {
-        set_error("sdf_mlp_fwd: %zu bytes of shared memory do not fit an SM", smem);
-        return ANGELO_E_UNSUPPORTED;
-    }
+    static PersistentLaunch cfg;
+    const int rc = persistent_setup(k, smem, kTcThreads, cfg, "sdf_mlp_fwd");
+    if (rc != ANGELO_OK) return rc;
     // two CTAs per SM: their registers (2 x 512 x 64) and shared memory
     // (2 x 115 KB) fit, and each holds 256 of the SM's 512 tensor-memory
     // columns (the occupancy query answers 1 here); CTAs beyond what the SMs
     // hold run as a later wave of the persistent loop
-    per_sm = 2;
     const int64_t tiles = (P.S + 127) / 128;
-    const int grid = (int)std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm);
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)cfg.sms * 2);
     k<<<grid, kTcThreads, smem, s>>>(P);
     return check_launch("sdf_mlp_fwd");
 }
 
 template <int KH, int NH, int NT3, int GROUP>
 int launch_mlp_bwd(const SdfParams &P, cudaStream_t s) {
-    const size_t smem = TcBwdShape<KH, NH, NT3>::bytes;
+    using Sh = TcBwdShape<KH, NH, NT3>;
     auto k = sdf_mlp_bwd_tc_kernel<KH, NH, NT3, GROUP>;
-    if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-        cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, 100) != cudaSuccess)
-        return check_launch("sdf_mlp_bwd(smem attribute)");
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kTcThreads, smem);
-    if (per_sm < 1) {
-        set_error("sdf_mlp_bwd: %zu bytes of shared memory do not fit an SM", smem);
-        return ANGELO_E_UNSUPPORTED;
-    }
-    // each CTA holds TcBwdShape::tmem_cols of the SM's 512 tensor-memory columns
-    per_sm = std::min(per_sm, (int)(512 / TcBwdShape<KH, NH, NT3>::tmem_cols));
+    static PersistentLaunch cfg;
+    const int rc = persistent_setup(k, Sh::bytes, kTcThreads, cfg, "sdf_mlp_bwd");
+    if (rc != ANGELO_OK) return rc;
+    // each CTA holds Sh::tmem_cols of the SM's 512 tensor-memory columns
+    const int per_sm = std::min(cfg.per_sm, (int)(512 / Sh::tmem_cols));
     const int64_t tiles = (P.S + 127) / 128;
-    const int grid = (int)std::min<int64_t>(tiles, (int64_t)sm_count() * per_sm);
-    k<<<grid, kTcThreads, smem, s>>>(P);
+    const int grid = (int)std::min<int64_t>(tiles, (int64_t)cfg.sms * per_sm);
+    k<<<grid, kTcThreads, Sh::bytes, s>>>(P);
     return check_launch("sdf_mlp_bwd");
 }
 
