@@ -743,22 +743,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
     const int64_t n_items = my_tiles * ne;
     float g1[16];            // softplus' of this thread's layer-1 slice, kept for dZ1
     float dsh[3] = {0.f, 0.f, 0.f};
-    for (int64_t k = 0; k < n_items; ++k) {
+    constexpr int kDsSlice = 3;   // slice that runs a tile's ds prologue (stages no input)
+    // layer-1 operand of item k (slice q < KH: hash levels 8q .. 8q + 7; slice
+    // KH: xyz) into registers; issued two rounds before it is staged
+    auto load_x = [&](int64_t k, float (&xv)[16]) {
         const int64_t s = (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row;
         const bool v = s < P.S;
-        const int i = (int)(k % ne), e = e0 + i;
-        const bool point = GROUP != kCurv && e == 0;
-        float base[3], xc[3];
-        int m;
-        {
-            const float *src = GROUP == kCurv ? P.state + s * kState + 13 : P.pos + s * 3;
-#pragma unroll
-            for (int d = 0; d < 3; ++d) base[d] = v ? src[d] : 0.f;
-        }
-        tap_point(r_, eps, base, e, xc, &m);
-        // layer-1 operand (slice q < KH: hash levels 8q .. 8q + 7; slice KH:
-        // xyz), loaded while the previous evaluation's last products run
-        float xv[16];
+        const int e = e0 + (int)(k % ne);
 #pragma unroll
         for (int j = 0; j < 16; ++j) xv[j] = 0.f;
         if (slice < KH) {
@@ -770,8 +761,31 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
                 xv[2 * j + 1] = f.y;
             }
         } else if (slice == KH) {
+            float b[3], xc[3];
+            int m;
+            const float *src = GROUP == kCurv ? P.state + s * kState + 13 : P.pos + s * 3;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) b[d] = v ? src[d] : 0.f;
+            tap_point(r_, eps, b, e, xc, &m);
 #pragma unroll
             for (int d = 0; d < 3; ++d) xv[d] = x2m1(xc[d]);
+        }
+    };
+    float xv[16];
+    if (n_items > 0) load_x(0, xv);
+    for (int64_t k = 0; k < n_items; ++k) {
+        const int64_t s = (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row;
+        const bool v = s < P.S;
+        const int i = (int)(k % ne), e = e0 + i;
+        const bool point = GROUP != kCurv && e == 0;
+        int m = 7;
+        if (GROUP == kCurv && slice == 0) {
+            // which coordinates of this tap passed the clamp (for dL/dshifted)
+            float base[3], xc[3];
+            const float *src = P.state + s * kState + 13;
+#pragma unroll
+            for (int d = 0; d < 3; ++d) base[d] = v ? src[d] : 0.f;
+            tap_point(r_, eps, base, e, xc, &m);
         }
         if (k > 0) {
             if (!(alive = tc_wait_all(&bar[1], ph1))) break;
@@ -779,7 +793,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
         }
         if (slice <= KH) stage16(xh, xl, row, 16 * slice, K1, xv);
         if (i == 0) {
-            if (slice == 0) {
+            if (slice == kDsSlice) {
                 float d7[7];
                 if (v) sample_ds<GROUP>(P, s, d7);
                 else
@@ -870,6 +884,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             for (int j = 0; j < 16; ++j) dh[j] *= gl[j];
             stage16(zh, zl, row, 16 * slice, 64, dh);
         }
+        // the next item's encodings, in flight during this item's last rounds
+        if (k + 1 < n_items) load_x(k + 1, xv);
         tc_publish();
         if (NH == 2) {
             // round 3: dH1 (epilogue), then dW2, db2, dW3
@@ -904,26 +920,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
         }
         if (!(alive = tc_wait_all(&bar[0], ph0))) break;
         ph0 ^= 1;
-        if (slice <= KH) {
-            float dx[16];
-            tc::ld16(tmem + lane_off + Sh::tB + 16 * slice, dx);
-            if (slice < KH) {
-                // dL/dX of hash levels 8 slice .. 8 slice + 7
+        {
+            // dL/dX of hash levels (CPS / 2) slice .. : all four slices
+            constexpr int CPS = 4 * KH;
+            float dx[CPS];
+            tc::ldn(tmem + lane_off + Sh::tB + CPS * slice, dx);
 #pragma unroll
-                for (int j = 0; j < 8; ++j) {
-                    const int l = 8 * slice + j;
-                    if (v && l < P.active) P.dX[xidx(P, e, l, s)] = make_float2(dx[2 * j], dx[2 * j + 1]);
-                }
-            } else if (GROUP == kCurv) {
-                // xyz columns x*2-1 to dL/dshifted; the scatter pass adds the
-                // hash grid's positional derivative atomically
+            for (int j = 0; j < CPS / 2; ++j) {
+                const int l = (CPS / 2) * slice + j;
+                if (v && l < P.active) P.dX[xidx(P, e, l, s)] = make_float2(dx[2 * j], dx[2 * j + 1]);
+            }
+        }
+        if (GROUP == kCurv && slice == 0) {
+            // xyz columns x*2-1 to dL/dshifted; the scatter pass adds the hash
+            // grid's positional derivative atomically
+            float dx[8];
+            tc::ld8(tmem + lane_off + Sh::tB + 16 * KH, dx);
 #pragma unroll
-                for (int d = 0; d < 3; ++d)
-                    if ((m >> d) & 1) dsh[d] += 2.f * dx[d] * inv2r;
-                if (i == ne - 1 && v) {
+            for (int d = 0; d < 3; ++d)
+                if ((m >> d) & 1) dsh[d] += 2.f * dx[d] * inv2r;
+            if (i == ne - 1 && v) {
 #pragma unroll
-                    for (int d = 0; d < 3; ++d) P.bstate[s * kBState + d] = dsh[d];
-                }
+                for (int d = 0; d < 3; ++d) P.bstate[s * kBState + d] = dsh[d];
             }
         }
     }

@@ -155,6 +155,32 @@ __device__ __forceinline__ void ld16(uint32_t taddr, float (&v)[16]) {
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// this thread's lane, 8 (or 4) consecutive fp32 columns
+__device__ __forceinline__ void ld8(uint32_t taddr, float (&v)[8]) {
+    uint32_t r[8];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void ld4(uint32_t taddr, float (&v)[4]) {
+    uint32_t r[4];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void ldn(uint32_t taddr, float (&v)[8]) { ld8(taddr, v); }
+__device__ __forceinline__ void ldn(uint32_t taddr, float (&v)[4]) { ld4(taddr, v); }
+
 // ---- accumulator stores: zeros into this thread's lane, 16 consecutive
 // columns (completed by tcgen05.wait::st in the same statement)
 __device__ __forceinline__ void st16_zero(uint32_t taddr) {
