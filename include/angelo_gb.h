@@ -155,6 +155,23 @@ int angelo_march_fill(const float *rays_o, const float *rays_d, const float *t_m
                       int64_t capacity, int32_t *ray_indices, float *t_starts, float *t_ends,
                       int32_t *status, void *stream);
 
+/* Single-march variant of passes 1 and 2 (no counterpart in the reference;
+ * same samples): march_record marches every ray once, writing its sample
+ * count to counts and its first per_ray samples as (t_start, t_end) pairs to
+ * scratch[2 * (ray * per_ray + j)]; a ray with more than per_ray samples sets
+ * status bit 2 (use march_fill then).  After the scan, march_compact copies
+ * the recorded samples to the packed outputs (capacity as in march_fill).
+ * per_ray >= ceil(ray length / step) + 2 bounds every ray (each sample
+ * advances t by at least step). */
+int angelo_march_record(const float *rays_o, const float *rays_d, const float *t_min,
+                        const float *t_max, int64_t n_rays, const angelo_grid_t *grid,
+                        float step, float cone_angle, int64_t max_steps, int32_t per_ray,
+                        float *scratch, int32_t *counts, int32_t *status, void *stream);
+int angelo_march_compact(const float *scratch, int32_t per_ray, const int32_t *counts,
+                         const int64_t *offsets, int64_t n_rays, int64_t capacity,
+                         int32_t *ray_indices, float *t_starts, float *t_ends, int32_t *status,
+                         void *stream);
+
 /* ------------------------------------------------------- occupancy update */
 
 /* OccupancyGrid._update's EMA + threshold (models/neus.py:108-109 through
@@ -219,8 +236,10 @@ int64_t angelo_sdf_grad_size(const angelo_sdf_net_layout *lay);
 
 /* Floats of device workspace of the fused VolumeSDF for n samples: the
  * forward's (backward = 0: the hash encodings of every evaluation, level-major
- * float2, and 16 floats of stencil state per sample) or the backward's
- * (backward = 1: dL/d(encodings), same layout, and 8 floats per sample).
+ * float2, 16 floats of stencil state per sample and, with the curvature, the
+ * derivative of each curvature tap's encoding along the three axes, 6 x
+ * levels x 3 float2 per sample) or the backward's (backward = 1:
+ * dL/d(encodings), same layout as the encodings, and 8 floats per sample).
  * -1 on invalid arguments.  Both must be 8-byte aligned. */
 int64_t angelo_sdf_workspace_floats(const angelo_hashgrid_layout_t *lay, int64_t n,
                                     int32_t with_grad, int32_t with_laplace, int32_t backward);
@@ -282,6 +301,15 @@ int64_t angelo_tc_timeouts(int32_t reset);
 int angelo_tc_gemm_x3(const float *A, const float *B, float *D, int32_t M, int32_t N, int32_t K,
                       int32_t a_mn_major, int32_t b_mn_major, int32_t variant, int32_t *status,
                       void *stream);
+
+/* Issue cost of the tensor-core instruction the fused MLPs are built from:
+ * one thread issues n (1..4096) back-to-back tcgen05.mma of shape M x N x 16
+ * (bf16, fp32 accumulation; M 64 or 128, N 16..256, multiple of 16) on
+ * zero operands.  cycles[0] = SM clocks spent issuing, cycles[1] = until
+ * the last product completed.  *status (zeroed by the caller) becomes 1 if
+ * the completion wait timed out.  No counterpart in the reference. */
+int angelo_tc_mma_rate(int32_t M, int32_t N, int32_t n, int64_t *cycles, int32_t *status,
+                       void *stream);
 
 /* ------------------------------------------------------------------- AdamW */
 

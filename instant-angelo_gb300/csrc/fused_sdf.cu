@@ -143,6 +143,8 @@ struct SdfParams {
     int64_t feat_stride;
     // forward workspace
     float2 *X;        // encodings, X[(e * n_levels + l) * S + s]
+    float2 *J;        // curvature taps: d(encoding)/d(cell fraction),
+                      // J[((k * n_levels + l) * 3 + axis) * S + s], k = tap 0..5
     float *state;     // (S, kState): sdf of the 13 evaluations, shifted point
     // backward inputs
     const float *g_sdf, *g_grad, *g_feature, *g_laplace;
@@ -276,6 +278,7 @@ __global__ void __launch_bounds__(kEncThreads) stencil_encode_kernel(const __gri
             const LevelPos p = level_pos(xc[0], xc[1], xc[2], sc);
             const bool aligned = tap_aligned(p, pc, d, &delta);
             float2 f = make_float2(0.f, 0.f);
+            float2 jac[3] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
 #pragma unroll
             for (int cc = 0; cc < 8; ++cc) {
                 const float w = corner_weight(p, cc);
@@ -284,8 +287,25 @@ __global__ void __launch_bounds__(kEncThreads) stencil_encode_kernel(const __gri
                                      : load_entry(P.table, P.tdtype, off + corner_index(P.lay, l, p, cc));
                 f.x = __fmaf_rn(w, v.x, f.x);
                 f.y = __fmaf_rn(w, v.y, f.y);
+                if (GROUP == kCurv) {
+                    // derivative of the trilinear weight along each axis
+#pragma unroll
+                    for (int dd = 0; dd < 3; ++dd) {
+                        float wd = 1.f;
+#pragma unroll
+                        for (int kk = 0; kk < 3; ++kk)
+                            if (kk != dd) wd *= (cc >> kk) & 1 ? p.f[kk] : 1.f - p.f[kk];
+                        wd = (cc >> dd) & 1 ? wd : -wd;
+                        jac[dd].x = __fmaf_rn(wd, v.x, jac[dd].x);
+                        jac[dd].y = __fmaf_rn(wd, v.y, jac[dd].y);
+                    }
+                }
             }
             P.X[xidx(P, e0 + k, l, s)] = f;
+            if (GROUP == kCurv) {
+#pragma unroll
+                for (int dd = 0; dd < 3; ++dd) P.J[((int64_t)(k * P.lay.n_levels + l) * 3 + dd) * P.S + s] = jac[dd];
+            }
         }
     }
 }
@@ -1005,13 +1025,9 @@ __global__ void __launch_bounds__(kEncThreads) stencil_scatter_kernel(const __gr
     float xcc[3];
     clamped_centre(r, base, xcc);
     const LevelPos pc = level_pos(xcc[0], xcc[1], xcc[2], sc);
-    float2 acc[8], vc[8];
+    float2 acc[8];
 #pragma unroll
-    for (int cc = 0; cc < 8; ++cc) {
-        acc[cc] = make_float2(0.f, 0.f);
-        vc[cc] = make_float2(0.f, 0.f);
-        if (GROUP == kCurv && valid) vc[cc] = load_entry(P.table, P.tdtype, off + corner_index(P.lay, l, pc, cc));
-    }
+    for (int cc = 0; cc < 8; ++cc) acc[cc] = make_float2(0.f, 0.f);
     float dsh[3] = {0.f, 0.f, 0.f};
     if (GROUP != kCurv) {
         const float2 gx = valid ? P.dX[xidx(P, 0, l, s)] : make_float2(0.f, 0.f);
@@ -1045,35 +1061,29 @@ __global__ void __launch_bounds__(kEncThreads) stencil_scatter_kernel(const __gr
             tap_point(r, eps, base, e0 + k, xc, &m);
             const LevelPos p = level_pos(xc[0], xc[1], xc[2], sc);
             const bool aligned = tap_aligned(p, pc, d, &delta);
-            float dl[3] = {0.f, 0.f, 0.f};
 #pragma unroll
             for (int cc = 0; cc < 8; ++cc) {
                 const float w = corner_weight(p, cc);
                 const float2 v = make_float2(w * gx.x, w * gx.y);
-                const bool shared = corner_shared(aligned, delta, cc, d);
-                if (shared) centre_add(acc, delta, cc, d, v);
+                if (corner_shared(aligned, delta, cc, d)) centre_add(acc, delta, cc, d, v);
                 else if (live && dt) atomicAdd(dt + off + corner_index(P.lay, l, p, cc), v);
-                if (GROUP == kCurv && live) {
-                    // positional derivative of the interpolation (d w / d frac)
-                    const float2 tv = shared ? centre_value(vc, delta, cc, d)
-                                             : load_entry(P.table, P.tdtype, off + corner_index(P.lay, l, p, cc));
-                    const float gv = gx.x * tv.x + gx.y * tv.y;
+            }
+            if (GROUP == kCurv && live) {
+                // positional derivative of the interpolation: dL/dX . dX/dfrac,
+                // the Jacobian kept by the forward encode
 #pragma unroll
-                    for (int dd = 0; dd < 3; ++dd) {
-                        float wd = 1.f;
-#pragma unroll
-                        for (int kk = 0; kk < 3; ++kk)
-                            if (kk != dd) wd *= (cc >> kk) & 1 ? p.f[kk] : 1.f - p.f[kk];
-                        dl[dd] += ((cc >> dd) & 1 ? wd : -wd) * gv;
-                    }
+                for (int dd = 0; dd < 3; ++dd) {
+                    const float2 jv = P.J[((int64_t)(k * P.lay.n_levels + l) * 3 + dd) * P.S + s];
+                    if ((m >> dd) & 1) dsh[dd] += sc * (gx.x * jv.x + gx.y * jv.y);
                 }
             }
-            if (GROUP == kCurv) {
-#pragma unroll
-                for (int dd = 0; dd < 3; ++dd)
-                    if ((m >> dd) & 1) dsh[dd] += sc * dl[dd];
-            }
         }
+    }
+    if (GROUP == kCurv && valid) {
+        const float inv2r = 1.0f / __fsub_rn(r, -r);
+#pragma unroll
+        for (int dd = 0; dd < 3; ++dd)
+            if (dsh[dd] != 0.f) atomicAdd(P.bstate + s * kBState + dd, dsh[dd] * inv2r);
     }
     if (dt) {
         const bool coarse = P.lay.resolutions[l] <= kAggregateRes;
@@ -1084,12 +1094,6 @@ __global__ void __launch_bounds__(kEncThreads) stencil_scatter_kernel(const __gr
             if (coarse) aggregated_add2<1>(dt, ent, acc[cc].x, acc[cc].y, nz);
             else if (nz) atomicAdd(dt + ent, acc[cc]);
         }
-    }
-    if (GROUP == kCurv && valid) {
-        const float inv2r = 1.0f / __fsub_rn(r, -r);
-#pragma unroll
-        for (int dd = 0; dd < 3; ++dd)
-            if (dsh[dd] != 0.f) atomicAdd(P.bstate + s * kBState + dd, dsh[dd] * inv2r);
     }
 }
 
@@ -1250,7 +1254,8 @@ extern "C" int64_t angelo_sdf_workspace_floats(const angelo_hashgrid_layout_t *l
                                                int32_t backward) {
     if (lay == nullptr || n < 0 || lay->n_levels < 1 || lay->n_levels > ANGELO_MAX_LEVELS) return -1;
     const int64_t x = 2 * n_evals(with_grad, with_laplace) * lay->n_levels * n;
-    return x + (backward ? kBState : kState) * n;
+    const int64_t j = (with_laplace && !backward) ? 2 * 6 * 3 * (int64_t)lay->n_levels * n : 0;
+    return x + (backward ? kBState : kState) * n + j;
 }
 
 extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32_t active_levels,
@@ -1296,6 +1301,7 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
     P.laplace = laplace;
     P.X = reinterpret_cast<float2 *>(workspace);
     P.state = workspace + 2 * n_evals(with_grad, with_laplace) * lay->n_levels * n;
+    P.J = with_laplace ? reinterpret_cast<float2 *>(P.state + kState * n) : nullptr;
     cudaStream_t s = as_stream(stream);
     if (shape_full(*nl)) return run_fwd<kFullKH, kFullNH, kFullNT3>(P, s);
     if (shape_small(*nl)) return run_fwd<kSmallKH, kSmallNH, kSmallNT3>(P, s);
@@ -1362,6 +1368,7 @@ extern "C" int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32
     const int64_t x = 2 * n_evals(with_grad, with_laplace) * lay->n_levels * n;
     P.X = reinterpret_cast<float2 *>(const_cast<float *>(workspace));
     P.state = const_cast<float *>(workspace) + x;
+    P.J = with_laplace ? reinterpret_cast<float2 *>(P.state + kState * n) : nullptr;
     P.dX = reinterpret_cast<float2 *>(bwd_workspace);
     P.bstate = bwd_workspace + x;
     P.g_sdf = g_sdf;

@@ -115,7 +115,59 @@ int operand_region(int rows, int K, int mn_major) {
     return (r + 1023) / 1024 * 1024;
 }
 
+// n back-to-back products M x N x 16 from one thread (operands zero, K-major,
+// 16 K columns: LBO 128, SBO 256), timed with the SM clock
+__global__ void __launch_bounds__(128, 1) tc_mma_rate_kernel(int M, int N, int n, long long *cycles, int *status) {
+    extern __shared__ __align__(1024) char smem[];
+    constexpr int kOperandBytes = 4096 + 8192;   // A: 128 x 16 bf16, B: 256 x 16 bf16
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + kOperandBytes);
+    uint32_t *slot = reinterpret_cast<uint32_t *>(mbar + 1);
+    for (int i = threadIdx.x * 16; i < kOperandBytes; i += 128 * 16)
+        *reinterpret_cast<uint4 *>(smem + i) = make_uint4(0u, 0u, 0u, 0u);
+    if (threadIdx.x < 32) {
+        tc::tmem_alloc(slot, 512);
+        tc::tmem_relinquish();
+    }
+    if (threadIdx.x == 0) tc::mbar_init(mbar, 1);
+    tc::fence_proxy_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *slot;
+    if (threadIdx.x == 0) {
+        const uint64_t ad = tc::smem_desc(tc::smem_addr(smem), 128, 256);
+        const uint64_t bd = tc::smem_desc(tc::smem_addr(smem + 4096), 128, 256);
+        const uint32_t id = tc::idesc_bf16_f32(M, N);
+        const long long t0 = clock64();
+        for (int i = 0; i < n; ++i) tc::mma_bf16(tmem, ad, bd, id, i > 0 ? 1u : 0u);
+        const long long t1 = clock64();
+        tc::commit(mbar);
+        const bool done = tc::mbar_wait(mbar, 0, kWaitPolls);
+        cycles[0] = t1 - t0;
+        cycles[1] = clock64() - t0;
+        if (!done) atomicExch(status, 1);
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (threadIdx.x < 32) tc::tmem_dealloc(tmem, 512);
+}
+
 }  // namespace
+
+extern "C" int angelo_tc_mma_rate(int32_t M, int32_t N, int32_t n, int64_t *cycles, int32_t *status,
+                                  void *stream) {
+    ANGELO_REQUIRE(cycles && status, "tc_mma_rate: null pointer");
+    ANGELO_REQUIRE(M == 64 || M == 128, "tc_mma_rate: M %d (64 or 128)", M);
+    ANGELO_REQUIRE(N >= 16 && N <= 256 && N % 16 == 0, "tc_mma_rate: N %d", N);
+    ANGELO_REQUIRE(n >= 1 && n <= 4096, "tc_mma_rate: n %d", n);
+    const int smem = 4096 + 8192 + 64;
+    if (cudaFuncSetAttribute(tc_mma_rate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) !=
+        cudaSuccess)
+        return check_launch("tc_mma_rate(smem attribute)");
+    tc_mma_rate_kernel<<<1, 128, smem, as_stream(stream)>>>(M, N, n, reinterpret_cast<long long *>(cycles),
+                                                           status);
+    return check_launch("tc_mma_rate");
+}
 
 extern "C" int angelo_tc_gemm_x3(const float *A, const float *B, float *D, int32_t M, int32_t N,
                                  int32_t K, int32_t a_mn_major, int32_t b_mn_major, int32_t variant,

@@ -104,3 +104,22 @@ def test_tc_m64_mn_major_weight_gradient(dev, N, K):
     got = D[lanes, :N]
     err = ((got - ref).abs().max() / ref.abs().max()).item()
     assert err < 2e-5, err
+
+
+def test_tc_mma_issue_rate_report(dev):
+    """Cycles per back-to-back tcgen05.mma (bf16, K = 16) by shape: the cost
+    model behind the fused MLP kernels' round structure (printed)."""
+    from angelo_gb._lib import call
+    from angelo_gb.ops import _p, _s
+    rows = []
+    for M, N in [(128, 256), (128, 128), (128, 64), (128, 16), (64, 64), (64, 16)]:
+        cyc = torch.zeros(2, dtype=torch.int64, device=dev)
+        st = torch.zeros(1, dtype=torch.int32, device=dev)
+        call("angelo_tc_mma_rate", M, N, 1024, _p(cyc), _p(st), _s(dev))
+        torch.cuda.synchronize()
+        assert int(st.item()) == 0
+        c = cyc.cpu().tolist()
+        rows.append((M, N, round(c[0] / 1024, 1), round(c[1] / 1024, 1)))
+    print("\n(M, N, issue cycles / mma, complete cycles / mma):", rows)
+    # the largest shape runs at the dense rate: 128 x 256 x 16 MACs in >= 128 cycles
+    assert rows[0][3] >= 100
