@@ -219,6 +219,17 @@ class NeuSModel(nn.Module):
         nc = torch.sigmoid(nxt * inv_s)
         return ((pc - nc + 1e-5) / (pc + 1e-5)).view(-1).clip(0.0, 1.0)
 
+    def _samples_bound(self):
+        """Samples any ray can have: its clipped length over the step, + 2
+        (the stratified start shifts near by up to one step)."""
+        if self.near_plane is None and self.far_plane is None:
+            length = 2.0 * math.sqrt(3.0) * float(self.config.radius)   # the box diagonal
+        elif self.near_plane is not None and self.far_plane is not None:
+            length = float(self.far_plane) - float(self.near_plane)
+        else:
+            return None
+        return int(math.ceil(length / self.render_step_size)) + 2
+
     def march_rays(self, rays_o, rays_d):
         """nerfacc.ray_marching as called at models/neus.py:210-220."""
         with torch.no_grad():
@@ -240,7 +251,7 @@ class NeuSModel(nn.Module):
                 grid = dict(roi=ops.UNBOUNDED_ROI, res=(1, 1, 1), bits=None)
             ri, t0, t1, offsets, _ = ops.march(rays_o, rays_d, t_min, t_max, self.render_step_size,
                                                cone_angle=0.0, max_steps=self.max_march_steps,
-                                               **grid)
+                                               max_samples_per_ray=self._samples_bound(), **grid)
         self._last_march = (t_min, t_max)
         self.last_num_samples = int(t0.shape[0])   # host-side, no device read
         return ri, t0, t1, offsets

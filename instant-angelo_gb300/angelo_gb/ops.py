@@ -198,13 +198,21 @@ def make_grid_desc(roi, res, bits):
 UNBOUNDED_ROI = (-1e10, -1e10, -1e10, 1e10, 1e10, 1e10)
 
 
+MARCH_SCRATCH_BYTES = 1 << 28   # single-march path while its scratch stays below this
+
+
 def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), bits=None,
-          cone_angle=0.0, max_steps=1 << 20):
+          cone_angle=0.0, max_steps=1 << 20, max_samples_per_ray=None):
     """Occupancy-grid ray marching.  Returns (ray_indices int32 (S,),
     t_starts (S,), t_ends (S,), offsets int64 (R+1,), status): the sample
     count is read back to the host to size the outputs, as the reference
     does; status is a device int32 tensor (bit 0: a ray reached max_steps)
-    that is not read here, so the caller's stream keeps running."""
+    that is not read here, so the caller's stream keeps running.
+
+    With max_samples_per_ray (a bound on every ray's sample count, e.g.
+    ceil(ray length / step) + 2) each ray is marched once: its samples are
+    recorded in a scratch buffer while counting and compacted after the scan;
+    a ray over the bound falls back to the second march (same samples)."""
     rays_o = _cuda(rays_o, "rays_o", dims=2)
     rays_d = _cuda(rays_d, "rays_d", dims=2)
     t_min = _cuda(t_min, "t_min").reshape(-1)
@@ -219,16 +227,34 @@ def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), 
     offsets = torch.empty(n + 1, device=dev, dtype=torch.int64)
     ws = torch.empty(_lib.raw("angelo_scan_workspace_size")(n), device=dev, dtype=torch.uint8)
     s = _s(dev)
-    call("angelo_march_count", _p(rays_o), _p(rays_d), _p(t_min), _p(t_max), n, ctypes.byref(g),
-         float(step), float(cone_angle), int(max_steps), _p(counts), _p(status), s)
+    per_ray = int(max_samples_per_ray) if max_samples_per_ray else 0
+    single = 0 < per_ray and n * per_ray * 8 <= MARCH_SCRATCH_BYTES
+    if single:
+        scratch = torch.empty(n * per_ray * 2, device=dev)
+        call("angelo_march_record", _p(rays_o), _p(rays_d), _p(t_min), _p(t_max), n,
+             ctypes.byref(g), float(step), float(cone_angle), int(max_steps), per_ray,
+             _p(scratch), _p(counts), _p(status), s)
+    else:
+        call("angelo_march_count", _p(rays_o), _p(rays_d), _p(t_min), _p(t_max), n,
+             ctypes.byref(g), float(step), float(cone_angle), int(max_steps), _p(counts),
+             _p(status), s)
     call("angelo_scan", _p(counts), n, _p(offsets), _p(ws), s, launches=3 if n else 0)
-    total = int(offsets[n].item())
+    if single:
+        # the total and the record-overflow bit in one device read
+        head = torch.cat([offsets[n:], status.to(torch.int64)]).cpu()
+        total, overflow = int(head[0]), bool(int(head[1]) & 4)
+    else:
+        total, overflow = int(offsets[n].item()), False
     ri = torch.empty(total, device=dev, dtype=torch.int32)
     t0 = torch.empty(total, device=dev)
     t1 = torch.empty(total, device=dev)
-    call("angelo_march_fill", _p(rays_o), _p(rays_d), _p(t_min), _p(t_max), n, ctypes.byref(g),
-         float(step), float(cone_angle), int(max_steps), _p(offsets), total, _p(ri), _p(t0),
-         _p(t1), _p(status), s)
+    if single and not overflow:
+        call("angelo_march_compact", _p(scratch), per_ray, _p(counts), _p(offsets), n, total,
+             _p(ri), _p(t0), _p(t1), _p(status), s)
+    else:
+        call("angelo_march_fill", _p(rays_o), _p(rays_d), _p(t_min), _p(t_max), n,
+             ctypes.byref(g), float(step), float(cone_angle), int(max_steps), _p(offsets), total,
+             _p(ri), _p(t0), _p(t1), _p(status), s)
     # the outputs are sized by the count pass, so the fill cannot exceed them
     return ri, t0, t1, offsets, status[0]
 

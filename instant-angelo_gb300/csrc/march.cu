@@ -170,6 +170,49 @@ __global__ void march_fill_kernel(const float *__restrict__ ro, const float *__r
     if (dropped && status) atomicOr(status, 2);
 }
 
+// One march per ray: the count and the first per_ray samples into scratch.
+__global__ void march_record_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
+                                    const float *__restrict__ tmin, const float *__restrict__ tmax,
+                                    int64_t n, Grid g, float step, float cone, int64_t max_steps,
+                                    int32_t per_ray, float2 *__restrict__ scratch,
+                                    int32_t *__restrict__ counts, int32_t *status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float o[3] = {ro[i * 3], ro[i * 3 + 1], ro[i * 3 + 2]};
+    const float d[3] = {rd[i * 3], rd[i * 3 + 1], rd[i * 3 + 2]};
+    float2 *dst = scratch + i * per_ray;
+    const int64_t c = march_ray(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status,
+                                [&](int64_t j, float t0, float t1) {
+                                    if (j < per_ray) dst[j] = make_float2(t0, t1);
+                                });
+    if (c > per_ray) atomicOr(status, 4);
+    counts[i] = (int32_t)(c > 0x7fffffff ? 0x7fffffff : c);
+}
+
+// One CTA per ray copies its recorded samples to the packed outputs.
+__global__ void march_compact_kernel(const float2 *__restrict__ scratch, int32_t per_ray,
+                                     const int32_t *__restrict__ counts,
+                                     const int64_t *__restrict__ offsets, int64_t capacity,
+                                     int32_t *__restrict__ ray_idx, float *__restrict__ ts,
+                                     float *__restrict__ te, int32_t *status) {
+    const int64_t i = blockIdx.x;
+    const int c = min(counts[i], per_ray);
+    const int64_t base = offsets[i];
+    bool dropped = false;
+    for (int j = threadIdx.x; j < c; j += blockDim.x) {
+        const int64_t p = base + j;
+        if (p < capacity) {
+            const float2 t = scratch[i * per_ray + j];
+            ray_idx[p] = (int32_t)i;
+            ts[p] = t.x;
+            te[p] = t.y;
+        } else {
+            dropped = true;
+        }
+    }
+    if (dropped && status) atomicOr(status, 2);
+}
+
 // ---------------------------------------------------------------- scan
 // Three-phase exclusive scan of int32 counts into int64 offsets: per-block
 // scans of 1024 counts (256 threads x 4), one block scanning the block sums,
@@ -329,4 +372,36 @@ extern "C" int angelo_march_fill(const float *rays_o, const float *rays_d, const
         rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, offsets, capacity,
         ray_indices, t_starts, t_ends, status);
     return check_launch("march_fill");
+}
+
+extern "C" int angelo_march_record(const float *rays_o, const float *rays_d, const float *t_min,
+                                   const float *t_max, int64_t n_rays, const angelo_grid_t *grid,
+                                   float step, float cone_angle, int64_t max_steps, int32_t per_ray,
+                                   float *scratch, int32_t *counts, int32_t *status, void *stream) {
+    Grid g;
+    if (int e = make_grid(grid, &g)) return e;
+    ANGELO_REQUIRE(n_rays >= 0 && step > 0.f && max_steps > 0 && per_ray > 0, "march_record: bad arguments");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(rays_o && rays_d && t_min && t_max && counts && scratch && status,
+                   "march_record: null pointer");
+    ANGELO_REQUIRE((reinterpret_cast<uintptr_t>(scratch) & 7) == 0, "march_record: scratch alignment");
+    march_record_kernel<<<blocks_for(n_rays, 128), 128, 0, as_stream(stream)>>>(
+        rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, per_ray,
+        reinterpret_cast<float2 *>(scratch), counts, status);
+    return check_launch("march_record");
+}
+
+extern "C" int angelo_march_compact(const float *scratch, int32_t per_ray, const int32_t *counts,
+                                    const int64_t *offsets, int64_t n_rays, int64_t capacity,
+                                    int32_t *ray_indices, float *t_starts, float *t_ends, int32_t *status,
+                                    void *stream) {
+    ANGELO_REQUIRE(n_rays >= 0 && per_ray > 0 && capacity >= 0, "march_compact: bad arguments");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(scratch && counts && offsets, "march_compact: null pointer");
+    ANGELO_REQUIRE(capacity == 0 || (ray_indices && t_starts && t_ends), "march_compact: null output");
+    ANGELO_REQUIRE(n_rays < (1LL << 31), "march_compact: too many rays");
+    march_compact_kernel<<<(unsigned)n_rays, 128, 0, as_stream(stream)>>>(
+        reinterpret_cast<const float2 *>(scratch), per_ray, counts, offsets, capacity, ray_indices, t_starts,
+        t_ends, status);
+    return check_launch("march_compact");
 }

@@ -176,6 +176,37 @@ def test_march_bit_exact(dev, p_occ):
         assert off[-1].item() == 0
 
 
+@pytest.mark.parametrize("per_ray", [None, 1026, 7])
+def test_march_single_pass_matches_oracle(dev, per_ray):
+    """The single-march path (samples recorded while counting, compacted after
+    the scan) against the oracle; per_ray 7 overflows and falls back to the
+    second march, with the same samples."""
+    from angelo_gb import ops
+    r = 1.0
+    o, d = _rays(2048, 21, 2.0)
+    aabb = np.array([-r, -r, -r, r, r, r], np.float32)
+    tmin, tmax = ops.ray_aabb_intersect(torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev),
+                                        torch.from_numpy(aabb).to(dev))
+    rtmin, rtmax = cref.ray_aabb(o, d, aabb)
+    jit = np.random.default_rng(22).random(2048, dtype=np.float32)
+    step = 1.732 * 2 * r / 1024
+    tmin_j = (rtmin + jit * np.float32(step)).astype(np.float32)
+    binary, words = _random_bits(128, 0.3, 23)
+    ri, t0, t1, off, st = ops.march(torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev),
+                                    torch.from_numpy(tmin_j).to(dev), tmax, step, roi=aabb,
+                                    res=(128, 128, 128),
+                                    bits=torch.from_numpy(words.view(np.int32)).to(dev),
+                                    max_samples_per_ray=per_ray)
+    _, roff, rri, rt0, rt1, _ = cref.march(o, d, tmin_j, rtmax, aabb, binary, step)
+    np.testing.assert_array_equal(off.cpu().numpy(), roff)
+    np.testing.assert_array_equal(ri.cpu().numpy(), rri)
+    np.testing.assert_array_equal(t0.cpu().numpy(), rt0)
+    np.testing.assert_array_equal(t1.cpu().numpy(), rt1)
+    assert (int(st) & 3) == 0
+    if per_ray == 7:
+        assert int(st) & 4   # the bound was exceeded: second march used
+
+
 def test_march_without_grid_between_planes(dev):
     """Config-1 style: no grid, samples between near 0.5 and far 4.5, dt 1/32."""
     from angelo_gb import ops
