@@ -589,25 +589,29 @@ template <int KH, int NH, int NT3>
 struct TcBwdShape {
     static constexpr int K1 = 16 * (KH + 1);
     static constexpr int N3 = 16 * ((NT3 + 1) / 2);
-    // bytes of one (hi or lo) half of each operand
+    // weights: bytes of one (hi or lo) half
     static constexpr uint32_t w1 = 64 * K1 * 2, w2 = NH == 2 ? 64 * 64 * 2 : 0, w3 = N3 * 64 * 2;
-    static constexpr uint32_t x = 128 * K1 * 2, h = 128 * 64 * 2, y = 128 * N3 * 2, ones = 128 * 16 * 2;
+    // activation stagings, hi and lo side by side in a row: X [hi | lo] (the
+    // hi column 16 KH + 3, a zero-weight pad, holds 1 for the bias sum),
+    // H1 [hi | lo | 1-block] (column 128 = 1), H2 and Z [hi | lo], Y [hi | lo]
+    static constexpr int CX = 2 * K1, CH1 = 144, CH = 128, CY = 2 * N3;
+    static constexpr uint32_t x = 128 * CX * 2, h1 = 128 * CH1 * 2, h = 128 * CH * 2, y = 128 * CY * 2;
     static constexpr uint32_t off_w1 = 0, off_w2 = off_w1 + 2 * w1, off_w3 = off_w2 + 2 * w2,
                               off_x = off_w3 + 2 * w3,
-                              off_h1 = off_x + 2 * x,                        // H1, then dZ1 (two layers)
-                              off_h2 = off_h1 + 2 * h,                       // H2 (two layers)
-                              off_z = off_h2 + (NH == 2 ? 2 * h : 0),        // dZ of the last layer
-                              off_y = off_z + 2 * h,                         // dY
-                              off_ones = off_y + 2 * y,                      // column 0 = 1, hi only
-                              off_vec = off_ones + ones,                     // b1, b2, W3 row 0
+                              off_h1 = off_x + x,                            // H1, then dZ1 (two layers)
+                              off_h2 = off_h1 + h1,                          // H2 (two layers)
+                              off_z = off_h2 + (NH == 2 ? h : 0),            // dZ of the last layer
+                              off_y = off_z + h,                             // dY
+                              off_vec = off_y + y,                           // b1, b2, W3 row 0
                               off_ds = off_vec + 3 * 64 * 4,                 // dL/dsdf [7][128]
                               off_db3 = off_ds + 7 * 128 * 4,
                               off_w3g = off_db3 + N3 * 4,                    // taps' dW3 row 0
                               off_bar = off_w3g + 64 * 4, bytes = off_bar + 32;
-    // tensor-memory columns: per evaluation A, B; CTA-resident gradients
-    static constexpr uint32_t tA = 0, tB = 64, tW1 = 128, tW2 = tW1 + K1, tW3 = tW2 + (NH == 2 ? 64 : 0),
-                              tb1 = tW3 + N3, tb2 = tb1 + 16, used = tb2 + (NH == 2 ? 16 : 0),
-                              tmem_cols = used <= 256 ? 256 : 512;
+    // tensor-memory columns: per evaluation A, B; CTA-resident gradients: dW1
+    // and dW2 (+ bias sums) as M = 128 products, rows hi then lo units, columns
+    // the operand's hi then lo (four blocks summed at the end); dW3^T (M = 64)
+    static constexpr uint32_t tA = 0, tB = 64, tW1 = 128, tW2 = tW1 + CX, tW3 = tW2 + (NH == 2 ? CH1 : 0),
+                              used = tW3 + N3, tmem_cols = used <= 256 ? 256 : 512;
 };
 
 // dL/dsdf of the evaluations of GROUP of sample s (ds[e - e0]), from the
@@ -707,8 +711,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
         else v = reinterpret_cast<const float *>(P.net + nl.off_w3row0)[i - 128];
         vec[i] = v;
     }
-    uint16_t *ones = reinterpret_cast<uint16_t *>(smem + Sh::off_ones);
-    fill_ones_operand(ones, tid, kTcThreads);
+    char *xs = smem + Sh::off_x, *h1s = smem + Sh::off_h1, *h2s = smem + Sh::off_h2, *zs = smem + Sh::off_z,
+         *ys = smem + Sh::off_y;
+    // the constant block of H1's staging: column 128 = 1, 129 .. 143 = 0
+    for (int i = tid; i < 128 * 16; i += kTcThreads)
+        *reinterpret_cast<uint16_t *>(h1s + tc::kmajor_offset(i >> 4, 128 + (i & 15), Sh::CH1)) =
+            (i & 15) == 0 ? (uint16_t)0x3F80u : (uint16_t)0u;
     float *ds = reinterpret_cast<float *>(smem + Sh::off_ds);
     float *db3 = reinterpret_cast<float *>(smem + Sh::off_db3);
     for (int i = tid; i < N3; i += kTcThreads) db3[i] = 0.f;
@@ -716,9 +724,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
     for (int i = tid; i < 64; i += kTcThreads) w3g[i] = 0.f;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + Sh::off_bar);   // [0] epilogue, [1] round
     uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 2);
-    char *xh = smem + Sh::off_x, *xl = xh + Sh::x, *h1h = smem + Sh::off_h1, *h1l = h1h + Sh::h;
-    char *h2h = smem + Sh::off_h2, *h2l = h2h + Sh::h, *zh = smem + Sh::off_z, *zl = zh + Sh::h;
-    char *yh = smem + Sh::off_y, *yl = yh + Sh::y;
     if (warp == 0) {
         tc::tmem_alloc(slot, Sh::tmem_cols);
         tc::tmem_relinquish();
@@ -735,21 +740,22 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
     tc_publish();
 
     const uint32_t sW1 = tc::smem_addr(smem + Sh::off_w1), sW2 = tc::smem_addr(smem + Sh::off_w2),
-                   sW3 = tc::smem_addr(smem + Sh::off_w3), sX = tc::smem_addr(xh), sH1 = tc::smem_addr(h1h),
-                   sH2 = tc::smem_addr(h2h), sZ = tc::smem_addr(zh), sY = tc::smem_addr(yh),
-                   sOnes = tc::smem_addr(ones);
+                   sW3 = tc::smem_addr(smem + Sh::off_w3), sX = tc::smem_addr(xs), sH1 = tc::smem_addr(h1s),
+                   sH2 = tc::smem_addr(h2s), sZ = tc::smem_addr(zs), sY = tc::smem_addr(ys);
     const TcOp W1k = op_k(sW1, Sh::w1, K1), W1t = op_t(sW1, Sh::w1, K1);
     const TcOp W2k = op_k(sW2, Sh::w2, 64), W2t = op_t(sW2, Sh::w2, 64), W3t = op_t(sW3, Sh::w3, 64);
-    const TcOp Xk = op_k(sX, Sh::x, K1), Xt = op_t(sX, Sh::x, K1);
-    const TcOp H1k = op_k(sH1, Sh::h, 64), H1t = op_t(sH1, Sh::h, 64), H2t = op_t(sH2, Sh::h, 64);
-    const TcOp Zk = op_k(sZ, Sh::h, 64), Zt = op_t(sZ, Sh::h, 64);
-    const TcOp Yk = op_k(sY, Sh::y, N3), Yt = op_t(sY, Sh::y, N3), Ones = op_t(sOnes, 0u, 16);
+    // per-row products read hi / lo (op_k2); weight gradients read the whole
+    // staging row, hi and lo stacked (op_t): one product per K step
+    const TcOp Xk = op_k2(sX, K1, Sh::CX), Xs = op_t(sX, 0u, Sh::CX);
+    const TcOp H1k = op_k2(sH1, 64, Sh::CH1), H1s = op_t(sH1, 0u, Sh::CH1), H1t = op_t2(sH1, 64, Sh::CH1);
+    const TcOp H2t = op_t2(sH2, 64, Sh::CH), Zk = op_k2(sZ, 64, Sh::CH), Zs = op_t(sZ, 0u, Sh::CH);
+    const TcOp Yk = op_k2(sY, N3, Sh::CY), Yt = op_t2(sY, N3, Sh::CY);
     // dZ1 lives in the H1 staging with two hidden layers, in the dZ staging with one
-    const TcOp D1k = NH == 2 ? H1k : Zk, D1t = NH == 2 ? H1t : Zt, HLt = NH == 2 ? H2t : H1t;
+    const TcOp D1k = NH == 2 ? H1k : Zk, D1s = NH == 2 ? H1s : Zs, HLt = NH == 2 ? H2t : H1t;
     constexpr uint32_t id_fwd = tc::idesc_bf16_f32(128, 64);
     constexpr uint32_t id_dh = tc::idesc_bf16_f32(128, 64, 0, 1), id_dx = tc::idesc_bf16_f32(128, K1, 0, 1);
-    constexpr uint32_t id_w1 = tc::idesc_bf16_f32(64, K1, 1, 1), id_w2 = tc::idesc_bf16_f32(64, 64, 1, 1);
-    constexpr uint32_t id_w3 = tc::idesc_bf16_f32(64, N3, 1, 1), id_16 = tc::idesc_bf16_f32(64, 16, 1, 1);
+    constexpr uint32_t id_w1 = tc::idesc_bf16_f32(128, Sh::CX, 1, 1), id_w2 = tc::idesc_bf16_f32(128, Sh::CH1, 1, 1);
+    constexpr uint32_t id_w3 = tc::idesc_bf16_f32(64, N3, 1, 1);
 
     constexpr int e0 = GROUP == kCurv ? 7 : 0;
     constexpr int ne = GROUP == kPoint ? 1 : (GROUP == kFD ? 7 : 6);
@@ -789,6 +795,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             tap_point(r_, eps, b, e, xc, &m);
 #pragma unroll
             for (int d = 0; d < 3; ++d) xv[d] = x2m1(xc[d]);
+            xv[3] = 1.f;   // zero-weight pad column: dW1 gathers the bias sum there
         }
     };
     float xv[16];
@@ -811,7 +818,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             if (!(alive = tc_wait_all(&bar[1], ph1))) break;
             ph1 ^= 1;
         }
-        if (slice <= KH) stage16(xh, xl, row, 16 * slice, K1, xv);
+        if (slice <= KH) stage16_2(xs, row, 16 * slice, K1, Sh::CX, xv);
         if (i == 0) {
             if (slice == kDsSlice) {
                 float d7[7];
@@ -835,7 +842,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
                     if (col == 0) g += d0;
                     yv[j] = g;
                 }
-                stage16(yh, yl, row, 16 * q, N3, yv);
+                stage16_2(ys, row, 16 * q, N3, Sh::CY, yv);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     float a = yv[j];
@@ -860,7 +867,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             tc::ld16(tmem + lane_off + Sh::tA + 16 * slice, z);
 #pragma unroll
             for (int j = 0; j < 16; ++j) softplus100_both(z[j] + vec[16 * slice + j], &hl[j], &g1[j]);
-            stage16(h1h, h1l, row, 16 * slice, 64, hl);
+            stage16_2(h1s, row, 16 * slice, 64, Sh::CH1, hl);
         }
         if (NH == 2) {
             tc_publish();
@@ -881,7 +888,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
                 tc::ld16(tmem + lane_off + Sh::tB + 16 * slice, z);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) softplus100_both(z[j] + vec[64 + 16 * slice + j], &hl[j], &gl[j]);
-                if (point) stage16(h2h, h2l, row, 16 * slice, 64, hl);
+                if (point) stage16_2(h2s, row, 16 * slice, 64, Sh::CH, hl);
             } else {
 #pragma unroll
                 for (int j = 0; j < 16; ++j) gl[j] = g1[j];
@@ -902,7 +909,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             }
 #pragma unroll
             for (int j = 0; j < 16; ++j) dh[j] *= gl[j];
-            stage16(zh, zl, row, 16 * slice, 64, dh);
+            stage16_2(zs, row, 16 * slice, 64, Sh::CH, dh);
         }
         // the next item's encodings, in flight during this item's last rounds
         if (k + 1 < n_items) load_x(k + 1, xv);
@@ -912,8 +919,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             if (tid == 0) {
                 tc_mma<4>(tmem + Sh::tA, Zk, W2t, id_dh, false);
                 tc::commit(&bar[0]);
-                tc_mma<8>(tmem + Sh::tW2, Zt, H1t, id_w2, true);
-                tc_mma<8>(tmem + Sh::tb2, Zt, Ones, id_16, true, true);
+                tc_mma1<8>(tmem + Sh::tW2, Zs, H1s, id_w2, true);   // dW2 and db2
                 if (point) tc_mma<8>(tmem + Sh::tW3, HLt, Yt, id_w3, true);
                 tc::commit(&bar[1]);
             }
@@ -926,15 +932,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             // H1 is read by dW2: rewrite it as dZ1 after the round completed
             if (!(alive = tc_wait_all(&bar[1], ph1))) break;
             ph1 ^= 1;
-            stage16(h1h, h1l, row, 16 * slice, 64, dz);
+            stage16_2(h1s, row, 16 * slice, 64, Sh::CH1, dz);
             tc_publish();
         }
         // last round: dX (epilogue), then dW1, db1 (one hidden layer: dW3)
         if (tid == 0) {
             tc_mma<4>(tmem + Sh::tB, D1k, W1t, id_dx, false);
             tc::commit(&bar[0]);
-            tc_mma<8>(tmem + Sh::tW1, D1t, Xt, id_w1, true);
-            tc_mma<8>(tmem + Sh::tb1, D1t, Ones, id_16, true, true);
+            tc_mma1<8>(tmem + Sh::tW1, D1s, Xs, id_w1, true);   // dW1 and db1
             if (NH == 1 && point) tc_mma<8>(tmem + Sh::tW3, HLt, Yt, id_w3, true);
             tc::commit(&bar[1]);
         }
@@ -967,8 +972,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
     }
     if (alive && n_items > 0) alive = tc_wait_all(&bar[1], ph1);
     if (alive) {
-        // add the CTA's gradients: tensor-memory rows 16 (warp % 4) + lane
-        const int unit = 16 * (warp & 3) + lane;
+        // add the CTA's gradients.  dW1, dW2: lane r = row r of an M = 128
+        // product (unit r % 64, hi rows then lo rows), column = operand column
+        // (hi then lo part; X's pad column 16 KH + 3 and H1's column 128 carry
+        // the bias sums).  dW3^T: M = 64, row 16 (warp % 4) + lane, lanes < 16.
+        const int r128 = 32 * (warp & 3) + lane, u128 = r128 & 63, u64 = 16 * (warp & 3) + lane;
         float *dW2 = P.d_net + 64 * K1, *dW3 = dW2 + 64 * 64, *db1 = dW3 + N3 * 64, *db2 = db1 + 64,
               *dB3 = db2 + 64;
         for (uint32_t b = slice; b < (Sh::used - Sh::tW1) / 16; b += 4) {
@@ -977,14 +985,18 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             __syncwarp();
             tc::ld16(tmem + lane_off + c0, w);
 #pragma unroll
-            for (int j = 0; j < 16 && lane < 16; ++j) {
+            for (int j = 0; j < 16; ++j) {
                 const uint32_t c = c0 + j;
                 float *dst = nullptr;
-                if (c < Sh::tW2) dst = P.d_net + unit * K1 + (c - Sh::tW1);
-                else if (c < Sh::tW3) dst = dW2 + unit * 64 + (c - Sh::tW2);
-                else if (c < Sh::tb1) dst = dW3 + (c - Sh::tW3) * 64 + unit;
-                else if (c == Sh::tb1) dst = db1 + unit;
-                else if (NH == 2 && c == Sh::tb2) dst = db2 + unit;
+                if (c < Sh::tW2) {
+                    const int k = (int)(c - Sh::tW1) % K1;
+                    dst = k == 16 * KH + 3 ? db1 + u128 : P.d_net + u128 * K1 + k;
+                } else if (c < Sh::tW3) {
+                    const int k = (int)(c - Sh::tW2);
+                    dst = k < 128 ? dW2 + u128 * 64 + (k & 63) : (k == 128 ? db2 + u128 : nullptr);
+                } else if (lane < 16) {
+                    dst = dW3 + (c - Sh::tW3) * 64 + u64;
+                }
                 if (dst && w[j] != 0.f) atomicAdd(dst, w[j]);
             }
         }

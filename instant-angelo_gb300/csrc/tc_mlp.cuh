@@ -70,6 +70,42 @@ __device__ __forceinline__ TcOp op_t(uint32_t hi, uint32_t half, int C) {
     return TcOp{hi, hi + half, 16u * (uint32_t)C, 128u, 32u * (uint32_t)C};
 }
 
+// hi and lo side by side in one [rows][C] staging: the hi part in columns
+// [0, w), the lo part in [w, 2 w) (a weight-gradient product then reads both
+// as one operand of 2 w rows: op_t(base, 0, C) with M or N = 2 w)
+__device__ __forceinline__ TcOp op_k2(uint32_t base, int w, int C) {
+    return TcOp{base, base + (uint32_t)(w / 8) * 128u, 128u, 16u * (uint32_t)C, 256u};
+}
+__device__ __forceinline__ TcOp op_t2(uint32_t base, int w, int C) {
+    return TcOp{base, base + (uint32_t)(w / 8) * 128u, 16u * (uint32_t)C, 128u, 32u * (uint32_t)C};
+}
+
+// 16 columns c0 .. c0 + 15 of row r, hi part at column c0 and lo part at
+// column w + c0 of a staging with C columns
+__device__ __forceinline__ void stage16_2(char *base, int r, int c0, int w, int C, const float (&v)[16]) {
+    uint32_t h[8], l[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const Split sp = split2(v[2 * i], v[2 * i + 1]);
+        h[i] = sp.hi;
+        l[i] = sp.lo;
+    }
+    *reinterpret_cast<uint4 *>(base + tc::kmajor_offset(r, c0, C)) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(base + tc::kmajor_offset(r, c0 + 8, C)) = make_uint4(h[4], h[5], h[6], h[7]);
+    *reinterpret_cast<uint4 *>(base + tc::kmajor_offset(r, w + c0, C)) = make_uint4(l[0], l[1], l[2], l[3]);
+    *reinterpret_cast<uint4 *>(base + tc::kmajor_offset(r, w + c0 + 8, C)) = make_uint4(l[4], l[5], l[6], l[7]);
+}
+
+// D (+)= A B^T over KSTEPS steps of 16, one product per step (operands
+// whose rows already stack the hi and lo parts).  One thread.
+template <int KSTEPS>
+__device__ __forceinline__ void tc_mma1(uint32_t d, const TcOp &a, const TcOp &b, uint32_t idesc, bool acc) {
+#pragma unroll
+    for (int ks = 0; ks < KSTEPS; ++ks)
+        tc::mma_bf16(d, tc::smem_desc(a.hi + ks * a.step, a.lbo, a.sbo),
+                     tc::smem_desc(b.hi + ks * b.step, b.lbo, b.sbo), idesc, (acc || ks > 0) ? 1u : 0u);
+}
+
 // D (+)= A B^T over KSTEPS steps of 16 in bf16x3 (lo*hi + hi*lo + hi*hi); with
 // b_exact, B is exact in bf16 and its lo product is left out.  One thread.
 template <int KSTEPS>
