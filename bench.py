@@ -15,7 +15,9 @@ e2e   : rays/s through NeuSModel / NeuSTrainer with each step's rays and
         colours sampled on the host and copied from pinned memory, the loss
         read back.
 Both forms of the path are run: "plain" (the reference's structure with the
-library's encode / march / composite kernels) and, when built, "fused".
+library's encode / march / composite kernels) and, when built, "fused"; and
+"fused_bg", the fused step with the sparse configs' learned NeRF++ background
+added (a wider workload than the headline, reported under "forms").
 
 --impl reference times the oracle's CPU restatement of the same step on the
 host cores (the reference itself is Python over tcnn/nerfacc CUDA kernels,
@@ -52,7 +54,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--forms", default="auto", help="comma list of plain,fused (auto: all built)")
+    ap.add_argument("--forms", default="auto",
+                    help="comma list of plain,fused,fused_bg (auto: all built)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--sdf-case", type=int, default=0, metavar="N",
@@ -137,7 +140,8 @@ def make_trainer(form, dev, seed=0):
     from angelo_gb import models, scenes, workloads
     from angelo_gb.system import NeuSTrainer
     torch.manual_seed(seed)
-    cfg = workloads.model_config("full", fused=(form == "fused"))
+    extra = workloads.background() if form == "fused_bg" else {}
+    cfg = workloads.model_config("full", fused=form in ("fused", "fused_bg"), **extra)
     model = models.make("neus", cfg).to(dev)
     model.train()
     with torch.no_grad():
@@ -149,6 +153,10 @@ def make_trainer(form, dev, seed=0):
         bits[: occ.numel()] = occ.long()
         w = (bits.view(-1, 32) << torch.arange(32, device=dev)).sum(-1)
         g.bits.copy_(w.to(torch.int64).bitwise_and(0xFFFFFFFF).to(torch.int32))
+        if form == "fused_bg":
+            # the background grid starts with every cell occupied
+            model.occupancy_grid_bg.occs.fill_(1.0)
+            model.occupancy_grid_bg.bits.fill_(-1)
     tr = NeuSTrainer(model, workloads.SYSTEM, train_num_rays=8192, max_train_num_rays=8192,
                      train_num_samples=1 << 18)
     tr.global_step = GLOBAL_STEP
@@ -377,7 +385,7 @@ def available_forms():
     try:
         from angelo_gb import fused  # noqa: F401
         if fused.available():
-            forms.append("fused")
+            forms += ["fused", "fused_bg"]
     except ImportError:
         pass
     return forms
@@ -397,6 +405,19 @@ def run_ours(args):
     hbm_peak, _, peak_kind = measured_peaks()
     for form in forms:
         model, tr = make_trainer(form, dev)
+        # every measured pass starts from the same state: the analytic
+        # occupancy grid and the initial ray count (the grid update every 16
+        # steps re-derives the grid from the untrained field, which changes
+        # the samples per ray), then its own warm-up steps
+        grids = [model.occupancy_grid] + ([model.occupancy_grid_bg] if model.learned_background else [])
+        start = ([(g.occs.clone(), g.bits.clone()) for g in grids], tr.train_num_rays, tr.global_step)
+
+        def reset():
+            for g, (occs, bits) in zip(grids, start[0]):
+                g.occs.copy_(occs)
+                g.bits.copy_(bits)
+            tr.train_num_rays, tr.global_step = start[1], start[2]
+
         gen = torch.Generator(device=dev).manual_seed(1234 + rank)
         for _ in range(args.warmup):
             step_device(tr, views, gen)
@@ -412,6 +433,9 @@ def run_ours(args):
         # per-call CUDA events (roofline, kernel shares, launch count) over a
         # second timed pass of as many steps: recording them costs host time,
         # so they stay out of the pass that gives `value`
+        reset()
+        for _ in range(args.warmup):
+            step_device(tr, views, gen)
         _lib.PROFILER.start()
         timed(lambda: step_device(tr, views, gen), args.steps, dev, world)
         _lib.PROFILER.stop()
@@ -423,7 +447,8 @@ def run_ours(args):
         rl, shares = roofline(summ, hbm_peak, peak_kind)
         # host-fed end-to-end through the public API
         feed = HostFeed(views, seed=77 + rank)
-        for _ in range(max(1, args.warmup // 2)):
+        reset()
+        for _ in range(args.warmup):
             step_host(tr, feed, dev)
         feed.read_result()
         ms_e2e, acc_e = timed(lambda: step_host(tr, feed, dev), args.steps, dev, world)
@@ -461,10 +486,13 @@ def run_ours(args):
                    "global_step": GLOBAL_STEP, "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (hash table 0.43 GB + AdamW state)",
                    "per_call_events": "roofline, kernel_ms and gpu_launches from a second "
-                   "timed pass of the same number of steps"},
+                   "timed pass of the same number of steps",
+                   "passes": "each pass (value, per-call events, e2e) starts from the analytic "
+                   "occupancy grid, 8192 rays and the same global step, then W warm-up steps"},
         "e2e": R["e2e"], "roofline": R["roofline"], "clocks": R["clocks"],
         "gpu_launches": R["gpu_launches"], "kernel_ms": R["kernel_ms"],
         "forms": {f: {"value": round(v["value"], 1), "ms_per_step": round(v["ms_per_step"], 3),
+                      "samples_per_step": round(v["samples_per_step"], 1),
                       "e2e": v["e2e"]["value"]} for f, v in results.items()},
     }
     if "fused" in results and "plain" in results:

@@ -113,11 +113,20 @@ int angelo_ray_aabb(const float *rays_o, const float *rays_d, int64_t n, const f
 
 /* Occupancy grid as seen by the marcher: res^3 cells over roi, one bit per
  * cell, cell index = ix*res_y*res_z + iy*res_z + iz, bit (c & 31) of word
- * c >> 5.  A NULL bits pointer means "every cell occupied". */
+ * c >> 5.  A NULL bits pointer means "every cell occupied".  contraction
+ * (nerfacc 0.3.3 ContractionType): ANGELO_CONTRACT_AABB, cells over roi and
+ * nothing outside it, empty cells skipped to the next cell boundary; or
+ * ANGELO_CONTRACT_UNBOUNDED_SPHERE (the learned background's grid,
+ * models/neus.py:69-74), roi mapped to [-1,1]^3, points beyond the unit
+ * sphere contracted to radius 2 - 1/|x|, the radius-2 ball to [0,1]^3, no
+ * skipping. */
+#define ANGELO_CONTRACT_AABB 0
+#define ANGELO_CONTRACT_UNBOUNDED_SPHERE 1
 typedef struct {
     float roi[6];
     int32_t res[3];
     const uint32_t *bits;
+    int32_t contraction;
 } angelo_grid_t;
 
 /* nerfacc.ray_marching (models/neus.py:210-220), pass 1: samples per ray.
@@ -195,6 +204,16 @@ int angelo_weights_fwd(const float *alpha, const int64_t *offsets, int64_t n_ray
 int angelo_weights_bwd(const float *alpha, const float *trans, const int64_t *offsets,
                        int64_t n_rays, float early_stop_eps, const float *dweights,
                        float *dalpha, void *stream);
+
+/* nerfacc.render_weight_from_density (the learned background,
+ * models/neus.py:171): per ray in sample order, tau_j = sigma_j (t_end_j -
+ * t_start_j), w_j = (1 - exp(-tau_j)) exp(-(tau_0 + .. + tau_{j-1})). */
+int angelo_density_weights_fwd(const float *t_starts, const float *t_ends, const float *sigmas,
+                               const int64_t *offsets, int64_t n_rays, float *weights, void *stream);
+/* dsigmas (written) from dweights, with the forward's weights. */
+int angelo_density_weights_bwd(const float *t_starts, const float *t_ends, const float *sigmas,
+                               const float *weights, const int64_t *offsets, int64_t n_rays,
+                               const float *dweights, float *dsigmas, void *stream);
 
 /* nerfacc.accumulate_along_rays (models/neus.py:235-240): out[r, c] =
  * sum_j w_j * v[j, c] over the samples of ray r (v == NULL: v = 1, C = 1). */

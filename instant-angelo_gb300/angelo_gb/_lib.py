@@ -36,7 +36,10 @@ class HashGridLayout(ctypes.Structure):
 
 
 class GridDesc(ctypes.Structure):
-    _fields_ = [("roi", c_f32 * 6), ("res", c_i32 * 3), ("bits", c_vp)]
+    _fields_ = [("roi", c_f32 * 6), ("res", c_i32 * 3), ("bits", c_vp), ("contraction", c_i32)]
+
+
+CONTRACT_AABB, CONTRACT_UNBOUNDED_SPHERE = 0, 1
 
 
 class SdfNetLayout(ctypes.Structure):
@@ -81,6 +84,8 @@ SIGNATURES = {
     "angelo_occ_workspace_size": (c_i64, [c_i64]),
     "angelo_occ_update": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_i64, c_f32, c_f32, c_vp, c_vp,
                                   c_vp]),
+    "angelo_density_weights_fwd": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp]),
+    "angelo_density_weights_bwd": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "angelo_weights_fwd": (c_i32, [c_vp, c_vp, c_i64, c_f32, c_vp, c_vp, c_vp]),
     "angelo_weights_bwd": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_f32, c_vp, c_vp, c_vp]),
     "angelo_accumulate_fwd": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp]),

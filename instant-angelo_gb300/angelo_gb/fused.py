@@ -377,9 +377,9 @@ def neus_forward(model, rays_o, rays_d, ri, t0, t1, offsets, n_rays):
         out.update({"sdf_samples": sdf, "sdf_grad_samples": sdf_grad, "weights": weights,
                     "points": mid, "intervals": t1 - t0, "ray_indices": ray_indices,
                     "sdf_laplace_samples": sdf_laplace})
-    out_bg = {"comp_rgb": bg[None, :].expand(*comp_rgb.shape),
-              "num_samples": torch.zeros_like(out["num_samples"]),
-              "rays_valid": torch.zeros_like(out["rays_valid"])}
+    out_bg = model.background(out, comp_rgb, rays_o, rays_d)
+    if model.learned_background:
+        comp_full = comp_rgb + out_bg["comp_rgb"] * (1.0 - opacity)
     out_full = {"comp_rgb": comp_full,
                 "num_samples": out["num_samples"] + out_bg["num_samples"],
                 "rays_valid": out["rays_valid"] | out_bg["rays_valid"]}
@@ -414,4 +414,4 @@ def _plain_render(model, rays_o, rays_d, ray_indices, t0, t1, offsets, sdf, sdf_
                     "weights": weights.view(-1), "points": mid.view(-1),
                     "intervals": dists.view(-1), "ray_indices": ray_indices.view(-1),
                     "sdf_laplace_samples": sdf_laplace})
-    return model._with_background(out, comp_rgb)
+    return model._with_background(out, comp_rgb, rays_o, rays_d)

@@ -30,6 +30,108 @@ def contract_to_unisphere(x, radius):
     return (x - (-radius)) / (radius - (-radius)) * (1 - 0) + 0
 
 
+def contract_unbounded_sphere(x, radius):
+    """UN_BOUNDED_SPHERE contraction (models/geometry.py:22-28): [-r, r]^3 to
+    [-1, 1]^3, points beyond the unit sphere to radius 2 - 1/|x|, then
+    [-2, 2]^3 to [0, 1]^3 (a select instead of the masked assignment, so that
+    no device read is needed)."""
+    x = (x - (-radius)) / (radius - (-radius)) * (1 - 0) + 0
+    x = x * 2 - 1
+    mag = x.norm(dim=-1, keepdim=True)
+    x = torch.where(mag > 1, (2 - 1 / mag) * (x / mag), x)
+    return x / 4 + 0.5
+
+
+class _TruncExp(torch.autograd.Function):
+    """exp with the backward's argument clamped at 15 (models/utils.py:53-69)."""
+
+    @staticmethod
+    def forward(ctx, x):
+        x = x.float()
+        ctx.save_for_backward(x)
+        return torch.exp(x)
+
+    @staticmethod
+    def backward(ctx, g):
+        (x,) = ctx.saved_tensors
+        return g * torch.exp(torch.clamp(x, max=15))
+
+
+def get_activation(name):
+    """models/utils.py:72-98 for the activations the NeuS configs use."""
+    if name is None or str(name).lower() == "none":
+        return lambda x: x
+    name = str(name).lower()
+    if name == "trunc_exp":
+        return _TruncExp.apply
+    if name == "sigmoid":
+        return torch.sigmoid
+    if name == "tanh":
+        return torch.tanh
+    if name.startswith("+") or name.startswith("-"):
+        return lambda x: x + float(name)
+    return getattr(F, name)
+
+
+class EncodingWithNetwork(nn.Module):
+    """models/network_utils.py:188-198."""
+
+    def __init__(self, encoding, network):
+        super().__init__()
+        self.encoding, self.network = encoding, network
+
+    def forward(self, x):
+        return self.network(self.encoding(x))
+
+    def update_step(self, epoch, global_step):
+        for m in (self.encoding, self.network):
+            if hasattr(m, "update_step"):
+                m.update_step(epoch, global_step)
+
+
+@models.register("volume-density")
+class VolumeDensity(nn.Module):
+    """The learned background's density field (models/geometry.py:152-177):
+    unbounded-sphere contraction -> hash grid (+ x*2-1) -> MLP; density =
+    activation(out[..., 0] + density_bias), feature = out."""
+
+    def __init__(self, config):
+        super().__init__()
+        self.config = config = to_config(config)
+        self.radius = config.radius
+        self.n_input_dims = config.get("n_input_dims", 3)
+        self.n_output_dims = config.feature_dim
+        encoding = get_encoding(self.n_input_dims, config.xyz_encoding_config)
+        network = get_mlp(encoding.n_output_dims, self.n_output_dims, config.mlp_network_config)
+        self.encoding_with_network = EncodingWithNetwork(encoding, network)
+        self.contraction_type = "unbounded_sphere"
+
+    def _density(self, out):
+        density = out[..., 0]
+        if "density_activation" in self.config:
+            density = get_activation(self.config.density_activation)(
+                density + float(self.config.density_bias))
+        return density
+
+    def forward(self, points):
+        pts = contract_unbounded_sphere(points, self.radius)
+        out = self.encoding_with_network(pts.view(-1, self.n_input_dims)).view(
+            *pts.shape[:-1], self.n_output_dims).float()
+        feature = out
+        if "feature_activation" in self.config:
+            feature = get_activation(self.config.feature_activation)(feature)
+        return self._density(out), feature
+
+    def forward_level(self, points):
+        pts = contract_unbounded_sphere(points, self.radius)
+        out = self.encoding_with_network(pts.reshape(-1, self.n_input_dims)).reshape(
+            *pts.shape[:-1], self.n_output_dims)
+        return -self._density(out)
+
+    def update_step(self, epoch, global_step):
+        self.encoding_with_network.update_step(epoch, global_step)
+
+
 _FD_DIRS = [[1.0, 0.0, 0.0], [-1.0, 0.0, 0.0], [0.0, 1.0, 0.0], [0.0, -1.0, 0.0],
             [0.0, 0.0, 1.0], [0.0, 0.0, -1.0]]
 

@@ -13,7 +13,7 @@ import torch
 import torch.nn as nn
 import torch.nn.functional as F
 
-from . import models, ops
+from . import _lib, models, ops
 from .config import to_config
 
 
@@ -98,12 +98,26 @@ class OccupancyGrid(nn.Module):
             occ_idx = occ_idx[torch.randint(len(occ_idx), (n,), device=dev)]
         return torch.cat([uni, occ_idx])
 
+    @property
+    def contraction(self):
+        return (_lib.CONTRACT_UNBOUNDED_SPHERE if self.contraction_type == "unbounded_sphere"
+                else _lib.CONTRACT_AABB)
+
     @torch.no_grad()
     def update(self, step, occ_eval_fn, occ_thre=0.01, ema_decay=0.95, warmup_steps=256):
         idx = self.sample_cells(step, warmup_steps)
         coords = self.cell_coords(idx).float()
         x = (coords + self.jitter_fn(coords)) / self.res
         lo, hi = self.roi_aabb[:3], self.roi_aabb[3:]
+        if self.contraction_type == "unbounded_sphere":
+            # only the cells inside the contracted ball are valid; [0,1]^3 ->
+            # [-2,2]^3 -> inverse sphere contraction -> [-1,1]^3 -> roi
+            keep = (x - 0.5).norm(dim=-1) < 0.5
+            x, idx = x[keep], idx[keep]
+            u = x * 4.0 - 2.0
+            nrm = u.norm(dim=-1, keepdim=True)
+            u = torch.where(nrm > 1.0, u / (nrm * (2.0 - nrm)), u)
+            x = u * 0.5 + 0.5
         x = x * (hi - lo) + lo
         occ = occ_eval_fn(x).reshape(-1).float()
         ops.occ_update(self.occs, idx, occ, ema_decay, occ_thre, self.bits)
@@ -151,8 +165,6 @@ class NeuSModel(nn.Module):
     def __init__(self, config):
         super().__init__()
         self.config = config = to_config(config)
-        if config.get("learned_background", False):
-            raise NotImplementedError("the learned NeRF++ background is not part of this build")
         fused = bool(config.get("fused", False))
         config.geometry["fused"] = fused
         config.texture["fused"] = fused
@@ -162,12 +174,25 @@ class NeuSModel(nn.Module):
         self.geometry = models.make(config.geometry.name, config.geometry)
         self.texture = models.make(config.texture.name, config.texture)
         self.geometry.contraction_type = "aabb"
+        self.learned_background = bool(config.get("learned_background", False))
+        if self.learned_background:
+            # models/neus.py:51-56: density field and radiance outside the box,
+            # marched from the box exit (or 0.1) to 1e3 with exponential steps
+            self.geometry_bg = models.make(config.geometry_bg.name, config.geometry_bg)
+            self.texture_bg = models.make(config.texture_bg.name, config.texture_bg)
+            self.geometry_bg.contraction_type = "unbounded_sphere"
+            self.near_plane_bg, self.far_plane_bg = 0.1, 1e3
+            self.cone_angle_bg = 10 ** (math.log10(self.far_plane_bg) / config.num_samples_per_ray_bg) - 1.0
+            self.render_step_size_bg = 0.01
         self.variance = VarianceNetwork(config.variance)
         r = config.radius
         self.register_buffer("scene_aabb", torch.as_tensor([-r, -r, -r, r, r, r],
                                                            dtype=torch.float32))
         if config.grid_prune:
             self.occupancy_grid = OccupancyGrid(self.scene_aabb, resolution=128)
+            if self.learned_background:
+                self.occupancy_grid_bg = OccupancyGrid(self.scene_aabb, resolution=256,
+                                                       contraction_type="unbounded_sphere")
         self.randomized = config.randomized
         self.background_color = None
         self.render_step_size = config.get("render_step_size",
@@ -184,6 +209,9 @@ class NeuSModel(nn.Module):
     def update_step(self, epoch, global_step):
         self.geometry.update_step(epoch, global_step)
         self.texture.update_step(epoch, global_step)
+        if self.learned_background:
+            self.geometry_bg.update_step(epoch, global_step)
+            self.texture_bg.update_step(epoch, global_step)
         self.variance.update_step(epoch, global_step)
         cae = self.config.get("cos_anneal_end", 0)
         self.cos_anneal_ratio = 1.0 if cae == 0 else min(1.0, global_step / cae)
@@ -198,9 +226,18 @@ class NeuSModel(nn.Module):
             nc = torch.sigmoid(nxt * inv_s)
             return ((pc - nc + 1e-5) / (pc + 1e-5)).view(-1, 1).clip(0.0, 1.0)
 
+        def occ_eval_fn_bg(x):
+            # density * step: the first-order 1 - exp(-density * step) (models/neus.py:103-106)
+            density, _ = self.geometry_bg(x)
+            return density[..., None] * self.render_step_size_bg
+
         if self.training and self.config.grid_prune:
             self.occupancy_grid.every_n_step(step=global_step, occ_eval_fn=occ_eval_fn,
                                              occ_thre=self.config.get("grid_prune_occ_thre", 0.01))
+            if self.learned_background:
+                self.occupancy_grid_bg.every_n_step(
+                    step=global_step, occ_eval_fn=occ_eval_fn_bg,
+                    occ_thre=self.config.get("grid_prune_occ_thre_bg", 0.01))
 
     def isosurface(self):
         return self.geometry.isosurface()
@@ -292,16 +329,90 @@ class NeuSModel(nn.Module):
                         "weights": weights.view(-1), "points": midpoints.view(-1),
                         "intervals": dists.view(-1), "ray_indices": ray_indices.view(-1),
                         "sdf_laplace_samples": sdf_laplace})
-        return self._with_background(out, comp_rgb)
+        return self._with_background(out, comp_rgb, rays_o, rays_d)
 
-    def _with_background(self, out, comp_rgb):
+    def _bg_samples_bound(self):
+        """Samples a background ray can have: the steps of the march
+        recurrence from t = 0 to the far plane, + 4."""
+        key = (self.render_step_size_bg, self.cone_angle_bg, self.far_plane_bg)
+        if getattr(self, "_bg_bound", (None, 0))[0] == key:
+            return self._bg_bound[1]
+        t0, n = 0.0, 0
+        step, cone = self.render_step_size_bg, self.cone_angle_bg
+        t1 = t0 + max(t0 * cone, step)
+        while (t0 + t1) * 0.5 < self.far_plane_bg:
+            t0, t1 = t1, t1 + max(t1 * cone, step)
+            n += 1
+        self._bg_bound = (key, n + 4)
+        return n + 4
+
+    def forward_bg_(self, rays_o, rays_d):
+        """The learned background (models/neus.py:141-203): marched from the
+        box exit (0.1 when the ray misses the box) to 1e3 through the
+        unbounded-sphere grid, samples of transmittance < 1e-4 dropped
+        (nerfacc's sigma_fn visibility test), weights from density."""
+        n_rays = rays_o.shape[0]
+        with torch.no_grad():
+            _, t_exit = ops.ray_aabb_intersect(rays_o, rays_d, self.scene_aabb)
+            near = torch.where(t_exit > 1e9, torch.full_like(t_exit, self.near_plane_bg), t_exit)
+            # nerfacc.ray_marching without scene_aabb: t in [0, 1e10], clamped by the planes
+            t_min = torch.maximum(torch.zeros_like(near), near)
+            t_max = torch.full_like(near, 1e10).clamp(max=self.far_plane_bg)
+            if self.randomized:
+                t_min = t_min + self.stratified_fn(t_min) * self.render_step_size_bg
+            if self.config.grid_prune:
+                g = self.occupancy_grid_bg
+                grid = dict(roi=g.roi, res=(g.res,) * 3, bits=g.bits, contraction=g.contraction)
+            else:
+                grid = dict(roi=ops.UNBOUNDED_ROI, res=(1, 1, 1), bits=None)
+            ri, t0, t1, offsets, _ = ops.march(rays_o, rays_d, t_min, t_max, self.render_step_size_bg,
+                                               cone_angle=self.cone_angle_bg,
+                                               max_steps=self.max_march_steps,
+                                               max_samples_per_ray=self._bg_samples_bound(), **grid)
+            rl = ri.long()
+            pos = rays_o[rl] + rays_d[rl] * ((t0 + t1) * 0.5)[:, None]
+            sigma, _ = self.geometry_bg(pos)
+            alpha = 1.0 - torch.exp(-sigma * (t1 - t0))
+            keep = ops.transmittance_from_alpha(alpha, offsets) >= 1e-4
+            self._last_march_bg_full = (offsets, ri, t0, t1)
+            ri, t0, t1 = ri[keep], t0[keep], t1[keep]
+            offsets = ops.offsets_from_ray_indices(ri, n_rays)
+            self._last_march_bg = (offsets, ri, t0, t1)
+        ray_indices = ri.long()
+        t_dirs = rays_d[ray_indices]
+        midpoints = ((t0 + t1) * 0.5)[:, None]
+        positions = rays_o[ray_indices] + t_dirs * midpoints
+        intervals = (t1 - t0)[:, None]
+        density, feature = self.geometry_bg(positions)
+        rgb = self.texture_bg(feature, t_dirs)
+        weights = ops.render_weight_from_density(t0[:, None], t1[:, None], density[:, None], offsets)
+        opacity = ops.accumulate_along_rays(weights, offsets)
+        depth = ops.accumulate_along_rays(weights, offsets, midpoints)
+        comp_rgb = ops.accumulate_along_rays(weights, offsets, rgb)
+        comp_rgb = comp_rgb + self.background_color * (1.0 - opacity)
+        out = {"comp_rgb": comp_rgb, "opacity": opacity, "depth": depth, "rays_valid": opacity > 0,
+               "num_samples": torch.full((1,), len(t0), dtype=torch.int32, device=rays_o.device)}
+        if self.training:
+            out.update({"weights": weights.view(-1), "points": midpoints.view(-1),
+                        "intervals": intervals.view(-1), "ray_indices": ray_indices.view(-1)})
+        return out
+
+    def background(self, out, comp_rgb, rays_o, rays_d):
+        """The background outputs: the learned background, or the constant
+        colour (models/neus.py:265-272)."""
+        if self.learned_background:
+            return self.forward_bg_(rays_o, rays_d)
+        bg = self.background_color
+        return {"comp_rgb": bg[None, :].expand(*comp_rgb.shape),
+                "num_samples": torch.zeros_like(out["num_samples"]),
+                "rays_valid": torch.zeros_like(out["rays_valid"])}
+
+    def _with_background(self, out, comp_rgb, rays_o=None, rays_d=None):
         bg = self.background_color
         if bg is None:
             raise RuntimeError("set model.background_color before rendering "
                                "(the reference's system sets it per batch)")
-        out_bg = {"comp_rgb": bg[None, :].expand(*comp_rgb.shape),
-                  "num_samples": torch.zeros_like(out["num_samples"]),
-                  "rays_valid": torch.zeros_like(out["rays_valid"])}
+        out_bg = self.background(out, comp_rgb, rays_o, rays_d)
         out_full = {"comp_rgb": out["comp_rgb"] + out_bg["comp_rgb"] * (1.0 - out["opacity"]),
                     "num_samples": out["num_samples"] + out_bg["num_samples"],
                     "rays_valid": out["rays_valid"] | out_bg["rays_valid"]}

@@ -185,13 +185,14 @@ def ray_aabb_intersect(rays_o, rays_d, aabb):
     return t_min, t_max
 
 
-def make_grid_desc(roi, res, bits):
+def make_grid_desc(roi, res, bits, contraction=_lib.CONTRACT_AABB):
     g = _lib.GridDesc()
     for i in range(6):
         g.roi[i] = float(roi[i])
     for i in range(3):
         g.res[i] = int(res[i])
     g.bits = bits.data_ptr() if bits is not None else None
+    g.contraction = int(contraction)
     return g
 
 
@@ -202,7 +203,8 @@ MARCH_SCRATCH_BYTES = 1 << 28   # single-march path while its scratch stays belo
 
 
 def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), bits=None,
-          cone_angle=0.0, max_steps=1 << 20, max_samples_per_ray=None):
+          cone_angle=0.0, max_steps=1 << 20, max_samples_per_ray=None,
+          contraction=_lib.CONTRACT_AABB):
     """Occupancy-grid ray marching.  Returns (ray_indices int32 (S,),
     t_starts (S,), t_ends (S,), offsets int64 (R+1,), status): the sample
     count is read back to the host to size the outputs, as the reference
@@ -221,7 +223,7 @@ def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), 
         bits = _cuda(bits, "bits", dtype=torch.int32)
     dev = rays_o.device
     n = rays_o.shape[0]
-    g = make_grid_desc(roi, res, bits)
+    g = make_grid_desc(roi, res, bits, contraction)
     counts = torch.empty(n, device=dev, dtype=torch.int32)
     status = torch.zeros(1, device=dev, dtype=torch.int32)
     offsets = torch.empty(n + 1, device=dev, dtype=torch.int64)
@@ -313,6 +315,56 @@ class _WeightsFromAlpha(torch.autograd.Function):
 
 def render_weight_from_alpha(alpha, offsets, early_stop_eps=1e-4):
     return _WeightsFromAlpha.apply(alpha, offsets, early_stop_eps)
+
+
+@torch.no_grad()
+def transmittance_from_alpha(alpha, offsets):
+    """T_j = prod_{k<j} (1 - alpha_k) per ray (held once below 1e-4, where
+    every later sample is invisible anyway): nerfacc's
+    render_transmittance_from_alpha as used by its visibility test."""
+    alpha = _cuda(alpha, "alpha").reshape(-1)
+    offsets = _cuda(offsets, "offsets", dtype=torch.int64)
+    w = torch.empty_like(alpha)
+    trans = torch.empty_like(alpha)
+    call("angelo_weights_fwd", _p(alpha), _p(offsets), offsets.numel() - 1, 1e-4, _p(w), _p(trans),
+         _s(alpha.device))
+    return trans
+
+
+def offsets_from_ray_indices(ray_indices, n_rays):
+    """int64 offsets (n_rays + 1) of packed samples sorted by ray."""
+    counts = torch.bincount(ray_indices.long(), minlength=n_rays)
+    return torch.cat([counts.new_zeros(1), torch.cumsum(counts, 0)])
+
+
+class _WeightsFromDensity(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, t_starts, t_ends, sigmas, offsets):
+        ctx.in_shape = sigmas.shape
+        t0 = _cuda(t_starts, "t_starts").reshape(-1)
+        t1 = _cuda(t_ends, "t_ends").reshape(-1)
+        sg = _cuda(sigmas, "sigmas").reshape(-1)
+        offsets = _cuda(offsets, "offsets", dtype=torch.int64)
+        w = torch.empty_like(sg)
+        call("angelo_density_weights_fwd", _p(t0), _p(t1), _p(sg), _p(offsets), offsets.numel() - 1,
+             _p(w), _s(sg.device))
+        ctx.save_for_backward(t0, t1, sg, w, offsets)
+        return w.view(ctx.in_shape)
+
+    @staticmethod
+    def backward(ctx, dw):
+        t0, t1, sg, w, offsets = ctx.saved_tensors
+        dw = dw.contiguous().float().reshape(-1)
+        ds = torch.empty_like(sg)
+        call("angelo_density_weights_bwd", _p(t0), _p(t1), _p(sg), _p(w), _p(offsets),
+             offsets.numel() - 1, _p(dw), _p(ds), _s(sg.device))
+        return None, None, ds.view(ctx.in_shape), None
+
+
+def render_weight_from_density(t_starts, t_ends, sigmas, offsets):
+    """nerfacc.render_weight_from_density (models/neus.py:171) over packed
+    samples with int64 ray offsets; differentiable in sigmas."""
+    return _WeightsFromDensity.apply(t_starts, t_ends, sigmas, offsets)
 
 
 class _Accumulate(torch.autograd.Function):

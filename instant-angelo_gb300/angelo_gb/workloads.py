@@ -9,6 +9,8 @@ system configuration keys (configs/neuralangelo-colmap_sparse.yaml:16-147).
            occupancy grid, step sqrt(3)*2*0.5/512; rays resized toward 2^18
            samples, at most 8192; FD eps annealed 1/32 -> 1/2048; eikonal 0.1,
            curvature 5e-4; 1600x1200 views of a torus/box/sphere union).
+* background(): the sparse configs' learned NeRF++ background, merged into
+           either model's keys.
 """
 from __future__ import annotations
 
@@ -59,10 +61,36 @@ FULL_MODEL = dict(
                  mlp_network_config=_mlp(2), color_activation="sigmoid"),
 )
 
+def background(n_levels=16, log2_hashmap_size=19, base_resolution=32,
+               per_level_scale=1.3195079107728942, start_level=4, update_steps=1000,
+               radius=0.5):
+    """The learned background of the sparse configs
+    (configs/neuralangelo-colmap_sparse.yaml:29,80-117): volume-density with
+    trunc_exp(x - 1) density and 8 features, volume-radiance on (feature,
+    SH4(dir)), 256 samples per ray, 256^3 unbounded-sphere grid."""
+    return dict(
+        learned_background=True, num_samples_per_ray_bg=256,
+        geometry_bg=dict(name="volume-density", radius=radius, feature_dim=8,
+                         density_activation="trunc_exp", density_bias=-1, isosurface=None,
+                         xyz_encoding_config=dict(otype="ProgressiveBandHashGrid", n_levels=n_levels,
+                                                  n_features_per_level=2,
+                                                  log2_hashmap_size=log2_hashmap_size,
+                                                  base_resolution=base_resolution,
+                                                  per_level_scale=per_level_scale, include_xyz=True,
+                                                  start_level=start_level, start_step=0,
+                                                  update_steps=update_steps),
+                         mlp_network_config=_mlp(1)),
+        texture_bg=dict(name="volume-radiance", input_feature_dim=8,
+                        dir_encoding_config=dict(otype="SphericalHarmonics", degree=4),
+                        mlp_network_config=_mlp(2), color_activation="sigmoid"),
+    )
+
+
 SYSTEM = dict(
     loss=dict(lambda_rgb_mse=10.0, lambda_eikonal=0.1, lambda_curvature=5e-4),
     optimizer=dict(name="AdamW", args=dict(lr=0.01, betas=[0.9, 0.99], eps=1e-15),
                    params=dict(geometry=dict(lr=0.01), texture=dict(lr=0.01),
+                               geometry_bg=dict(lr=0.01), texture_bg=dict(lr=0.01),
                                variance=dict(lr=0.001))),
 )
 

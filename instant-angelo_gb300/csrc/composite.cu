@@ -85,7 +85,66 @@ __global__ void accumulate_bwd_kernel(const float *__restrict__ w, const float *
     }
 }
 
+// nerfacc 0.3.3 render_weight_from_density (the learned background,
+// models/neus.py:171): per ray in sample order, with tau_j = sigma_j (t1_j -
+// t0_j), w_j = (1 - e^-tau_j) e^-(tau_0 + .. + tau_{j-1}).
+__global__ void density_weights_fwd_kernel(const float *__restrict__ t0, const float *__restrict__ t1,
+                                           const float *__restrict__ sigma, const int64_t *__restrict__ off,
+                                           int64_t n_rays, float *__restrict__ w) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rays) return;
+    float depth = 0.0f;
+    for (int64_t j = off[r]; j < off[r + 1]; ++j) {
+        const float tau = __fmul_rn(sigma[j], __fsub_rn(t1[j], t0[j]));
+        w[j] = __fmul_rn(__fsub_rn(1.0f, expf(-tau)), expf(-depth));
+        depth = __fadd_rn(depth, tau);
+    }
+}
+
+// dL/dsigma_j = dt_j (g_j e^-(tau_0 + .. + tau_j) - sum_{k>j} g_k w_k),
+// the suffix sum taken back to front.
+__global__ void density_weights_bwd_kernel(const float *__restrict__ t0, const float *__restrict__ t1,
+                                           const float *__restrict__ sigma, const float *__restrict__ w,
+                                           const int64_t *__restrict__ off, int64_t n_rays,
+                                           const float *__restrict__ gw, float *__restrict__ gs) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rays) return;
+    float total = 0.0f;
+    for (int64_t j = off[r]; j < off[r + 1]; ++j) total += sigma[j] * (t1[j] - t0[j]);
+    float after = 0.0f;   // sum_{k>j} g_k w_k
+    float depth = total;  // tau_0 + .. + tau_j, walking back
+    for (int64_t j = off[r + 1] - 1; j >= off[r]; --j) {
+        const float dt = t1[j] - t0[j];
+        gs[j] = dt * (gw[j] * expf(-depth) - after);
+        after += gw[j] * w[j];
+        depth -= sigma[j] * dt;
+    }
+}
+
 }  // namespace
+
+extern "C" int angelo_density_weights_fwd(const float *t_starts, const float *t_ends, const float *sigmas,
+                                          const int64_t *offsets, int64_t n_rays, float *weights,
+                                          void *stream) {
+    ANGELO_REQUIRE(n_rays >= 0, "density_weights_fwd: negative n_rays");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(t_starts && t_ends && sigmas && offsets && weights, "density_weights_fwd: null pointer");
+    density_weights_fwd_kernel<<<blocks_for(n_rays, 128), 128, 0, as_stream(stream)>>>(
+        t_starts, t_ends, sigmas, offsets, n_rays, weights);
+    return check_launch("density_weights_fwd");
+}
+
+extern "C" int angelo_density_weights_bwd(const float *t_starts, const float *t_ends, const float *sigmas,
+                                          const float *weights, const int64_t *offsets, int64_t n_rays,
+                                          const float *dweights, float *dsigmas, void *stream) {
+    ANGELO_REQUIRE(n_rays >= 0, "density_weights_bwd: negative n_rays");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(t_starts && t_ends && sigmas && weights && offsets && dweights && dsigmas,
+                   "density_weights_bwd: null pointer");
+    density_weights_bwd_kernel<<<blocks_for(n_rays, 128), 128, 0, as_stream(stream)>>>(
+        t_starts, t_ends, sigmas, weights, offsets, n_rays, dweights, dsigmas);
+    return check_launch("density_weights_bwd");
+}
 
 extern "C" int angelo_weights_fwd(const float *alpha, const int64_t *offsets, int64_t n_rays,
                                   float early_stop_eps, float *weights, float *trans,

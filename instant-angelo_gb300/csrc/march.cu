@@ -16,18 +16,39 @@ struct Grid {
     float lo[3], hi[3];
     int res[3];
     const uint32_t *bits;
+    int contraction;   // ANGELO_CONTRACT_*
 };
 
 __device__ __forceinline__ bool occupied(const Grid &g, const float xyz[3]) {
+    float u[3];
+    if (g.contraction == ANGELO_CONTRACT_AABB) {
 #pragma unroll
-    for (int d = 0; d < 3; ++d)
-        if (xyz[d] < g.lo[d] || xyz[d] > g.hi[d]) return false;
-    if (g.bits == nullptr) return true;
+        for (int d = 0; d < 3; ++d)
+            if (xyz[d] < g.lo[d] || xyz[d] > g.hi[d]) return false;
+        if (g.bits == nullptr) return true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) u[d] = __fdiv_rn(__fsub_rn(xyz[d], g.lo[d]), __fsub_rn(g.hi[d], g.lo[d]));
+    } else {
+        // unbounded sphere: roi -> [-1,1]^3; beyond the unit sphere
+        // x <- (2 - 1/|x|) x/|x|; the radius-2 ball -> [0,1]^3
+        if (g.bits == nullptr) return true;
+#pragma unroll
+        for (int d = 0; d < 3; ++d)
+            u[d] = __fsub_rn(__fmul_rn(__fdiv_rn(__fsub_rn(xyz[d], g.lo[d]), __fsub_rn(g.hi[d], g.lo[d])), 2.0f),
+                             1.0f);
+        const float nrm = __fsqrt_rn(__fmaf_rn(u[2], u[2], __fmaf_rn(u[1], u[1], __fmul_rn(u[0], u[0]))));
+        if (nrm > 1.0f) {
+            const float sc = __fsub_rn(2.0f, __fdiv_rn(1.0f, nrm));
+#pragma unroll
+            for (int d = 0; d < 3; ++d) u[d] = __fmul_rn(sc, __fdiv_rn(u[d], nrm));
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) u[d] = __fadd_rn(__fmul_rn(u[d], 0.25f), 0.5f);
+    }
     int ix[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
-        const float u = __fdiv_rn(__fsub_rn(xyz[d], g.lo[d]), __fsub_rn(g.hi[d], g.lo[d]));
-        int v = (int)__fmul_rn(u, (float)g.res[d]);
+        int v = (int)__fmul_rn(u[d], (float)g.res[d]);
         v = v < 0 ? 0 : (v > g.res[d] - 1 ? g.res[d] - 1 : v);
         ix[d] = v;
     }
@@ -81,6 +102,11 @@ __device__ __forceinline__ int64_t march_ray(const Grid &g, const float o[3], co
         if (occupied(g, xyz)) {
             emit(j, t0, t1);
             ++j;
+            t0 = t1;
+            t1 = __fadd_rn(t0, calc_dt(t0, cone, step));
+            tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
+        } else if (g.contraction != ANGELO_CONTRACT_AABB) {
+            // contracted grids are not skipped: the next step
             t0 = t1;
             t1 = __fadd_rn(t0, calc_dt(t0, cone, step));
             tm = __fmul_rn(__fadd_rn(t0, t1), 0.5f);
@@ -304,6 +330,9 @@ int make_grid(const angelo_grid_t *in, Grid *g) {
                        in->res[d]);
     }
     g->bits = in->bits;
+    ANGELO_REQUIRE(in->contraction == ANGELO_CONTRACT_AABB || in->contraction == ANGELO_CONTRACT_UNBOUNDED_SPHERE,
+                   "march: contraction %d", in->contraction);
+    g->contraction = in->contraction;
     return ANGELO_OK;
 }
 

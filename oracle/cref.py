@@ -58,7 +58,7 @@ def lib():
             L.or_ray_aabb.argtypes = [_f32p, _f32p, ctypes.c_int64, _f32p, _f32p, _f32p]
             L.or_march.restype = None
             L.or_march.argtypes = [_f32p, _f32p, _f32p, _f32p, ctypes.c_int64, _f32p, _u8p,
-                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                   ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
                                    ctypes.c_float, ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
             L.or_weights.restype = None
@@ -130,7 +130,8 @@ def ray_aabb(rays_o, rays_d, aabb):
     return tmin, tmax
 
 
-def march(rays_o, rays_d, t_min, t_max, roi, binary, step, cone=0.0, max_steps=1 << 20):
+def march(rays_o, rays_d, t_min, t_max, roi, binary, step, cone=0.0, max_steps=1 << 20,
+          contraction=0):
     """nerfacc.ray_marching core (models/neus.py:210-220): returns
     (counts[int32], offsets[int64, n+1], ray_indices[int32], t_starts, t_ends, overflow)."""
     o = _c(rays_o, np.float32).reshape(-1, 3)
@@ -145,17 +146,17 @@ def march(rays_o, rays_d, t_min, t_max, roi, binary, step, cone=0.0, max_steps=1
     counts = np.zeros(n, np.int32)
     ovf = np.zeros(1, np.int32)
     L = lib()
-    L.or_march(o, d, tmin, tmax, n, roi, b, rx, ry, rz, float(step), float(cone), int(max_steps),
-               counts.ctypes.data, None, None, None, None, ovf.ctypes.data)
+    L.or_march(o, d, tmin, tmax, n, roi, b, rx, ry, rz, int(contraction), float(step), float(cone),
+               int(max_steps), counts.ctypes.data, None, None, None, None, ovf.ctypes.data)
     offsets = np.zeros(n + 1, np.int64)
     np.cumsum(counts, out=offsets[1:])
     tot = int(offsets[-1])
     ri = np.zeros(max(tot, 1), np.int32)
     t0 = np.zeros(max(tot, 1), np.float32)
     t1 = np.zeros(max(tot, 1), np.float32)
-    L.or_march(o, d, tmin, tmax, n, roi, b, rx, ry, rz, float(step), float(cone), int(max_steps),
-               None, offsets.ctypes.data, ri.ctypes.data, t0.ctypes.data, t1.ctypes.data,
-               ovf.ctypes.data)
+    L.or_march(o, d, tmin, tmax, n, roi, b, rx, ry, rz, int(contraction), float(step), float(cone),
+               int(max_steps), None, offsets.ctypes.data, ri.ctypes.data, t0.ctypes.data,
+               t1.ctypes.data, ovf.ctypes.data)
     return counts, offsets, ri[:tot], t0[:tot], t1[:tot], bool(ovf[0])
 
 

@@ -362,6 +362,73 @@ def neus_render(rays, P, G, T, march, rand_dirs, cos_anneal_ratio, background_co
     return out
 
 
+# ---------------------------------------------------------- learned background
+
+
+def contract_unbounded(x, r):
+    """UN_BOUNDED_SPHERE contraction (models/geometry.py:22-28)."""
+    x = contract(x, r) * 2 - 1
+    mag = x.norm(dim=-1, keepdim=True)
+    x = torch.where(mag > 1, (2 - 1 / mag) * (x / mag), x)
+    return x / 4 + 0.5
+
+
+def volume_density(points, P, B):
+    """VolumeDensity.forward (models/geometry.py:162-170) with the sparse
+    configs' trunc_exp density: B holds radius, lay, active_levels, n_layers,
+    density_bias.  Returns (density, feature)."""
+    x = contract_unbounded(points, B["radius"])
+    pre = "geometry_bg.encoding_with_network"
+    enc = composite_encode(x, P[pre + ".encoding.encoding.encoding.params"], B["lay"],
+                           B["active_levels"])
+    out = mlp(enc, mlp_layers(P, pre + ".network", B["n_layers"], False), False)
+    return torch.exp(out[:, 0] + B["density_bias"]), out
+
+
+def texture_bg(features, dirs, P, n_layers):
+    """VolumeRadiance without normals (models/texture.py:23-30, the
+    background's texture): sigmoid(MLP(cat(feature, SH4((d+1)/2))))."""
+    inp = torch.cat([features, sh4((dirs + 1.0) / 2.0)], dim=-1)
+    return torch.sigmoid(mlp(inp, mlp_layers(P, "texture_bg.network", n_layers, False), False))
+
+
+def density_weights(t0, t1, sigma, offsets):
+    """render_weight_from_density (nerfacc 0.3.3, models/neus.py:171): per ray
+    w_j = (1 - exp(-tau_j)) exp(-sum_{k<j} tau_k), tau = sigma (t1 - t0)."""
+    tau = sigma * (t1 - t0)
+    ws = []
+    for r in range(len(offsets) - 1):
+        t = tau[offsets[r]:offsets[r + 1]]
+        if t.numel() == 0:
+            continue
+        before = torch.cat([torch.zeros(1, dtype=t.dtype, device=t.device), torch.cumsum(t, 0)[:-1]])
+        ws.append((1 - torch.exp(-t)) * torch.exp(-before))
+    return torch.cat(ws) if ws else torch.zeros_like(tau)
+
+
+def render_bg(rays, P, B, n_layers_tex, march, background_color):
+    """NeuSModel.forward_bg_ (models/neus.py:141-203) on given samples
+    ``march`` = (offsets, ray_indices, t_starts, t_ends) after the visibility
+    test; float64.  Returns comp_rgb (background colour blended), opacity,
+    depth."""
+    n_rays = rays.shape[0]
+    offsets, ray_idx, t0, t1 = march
+    ray_idx = torch.as_tensor(ray_idx, dtype=torch.int64, device=rays.device)
+    t0 = torch.as_tensor(t0, dtype=rays.dtype, device=rays.device)
+    t1 = torch.as_tensor(t1, dtype=rays.dtype, device=rays.device)
+    o, d = rays[:, 0:3], rays[:, 3:6]
+    mid = (t0 + t1) / 2.0
+    pos = o[ray_idx] + d[ray_idx] * mid[:, None]
+    density, feat = volume_density(pos, P, B)
+    rgb = texture_bg(feat, d[ray_idx], P, n_layers_tex)
+    w = density_weights(t0, t1, density, list(np.asarray(offsets)))
+    opacity = accumulate(w, ray_idx, None, n_rays)
+    depth = accumulate(w, ray_idx, mid[:, None], n_rays)
+    comp = accumulate(w, ray_idx, rgb, n_rays)
+    comp = comp + background_color.to(comp.dtype)[None, :] * (1.0 - opacity)
+    return {"comp_rgb": comp, "opacity": opacity, "depth": depth, "weights": w}
+
+
 def neus_loss_terms(out, rgb_target, lam_rgb_mse=10.0, lam_eikonal=0.1, lam_curvature=5e-4):
     """The hot-path loss seeds of NeuSSystem.training_step
     (systems/neus.py:130-159), weighted: (rgb MSE on valid rays + eikonal,

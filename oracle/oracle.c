@@ -222,13 +222,28 @@ void or_ray_aabb(const float *o, const float *d, int64_t n, const float *aabb, f
     }
 }
 
-static int or_occupied(const float xyz[3], const float *roi, const uint8_t *binary, const int res[3]) {
-    for (int d = 0; d < 3; ++d)
-        if (xyz[d] < roi[d] || xyz[d] > roi[3 + d]) return 0;
+/* nerfacc 0.3.3 grid_occupied_at: contraction 0 = AABB (nothing outside
+ * roi), 1 = UN_BOUNDED_SPHERE (roi -> [-1,1]^3, |x| > 1 -> (2 - 1/|x|) x/|x|,
+ * then x/4 + 1/2; models/neus.py:69-74 builds the background grid this way). */
+static int or_occupied(const float xyz[3], const float *roi, const uint8_t *binary, const int res[3],
+                       int contraction) {
+    float u[3];
+    if (contraction == 0) {
+        for (int d = 0; d < 3; ++d)
+            if (xyz[d] < roi[d] || xyz[d] > roi[3 + d]) return 0;
+        for (int d = 0; d < 3; ++d) u[d] = (xyz[d] - roi[d]) / (roi[3 + d] - roi[d]);
+    } else {
+        for (int d = 0; d < 3; ++d) u[d] = ((xyz[d] - roi[d]) / (roi[3 + d] - roi[d])) * 2.0f - 1.0f;
+        const float nrm = sqrtf(fmaf(u[2], u[2], fmaf(u[1], u[1], u[0] * u[0])));
+        if (nrm > 1.0f) {
+            const float sc = 2.0f - 1.0f / nrm;
+            for (int d = 0; d < 3; ++d) u[d] = sc * (u[d] / nrm);
+        }
+        for (int d = 0; d < 3; ++d) u[d] = u[d] * 0.25f + 0.5f;
+    }
     int ix[3];
     for (int d = 0; d < 3; ++d) {
-        float u = (xyz[d] - roi[d]) / (roi[3 + d] - roi[d]);
-        int v = (int)(u * (float)res[d]);
+        int v = (int)(u[d] * (float)res[d]);
         if (v < 0) v = 0;
         if (v > res[d] - 1) v = res[d] - 1;
         ix[d] = v;
@@ -261,15 +276,17 @@ static float or_dist_next_voxel(const float xyz[3], const float dir[3], const fl
     return t > 0.0f ? t : 0.0f;
 }
 
-/* Ray marching with grid skipping (contraction AABB, cone_angle >= 0).
+/* Ray marching with grid skipping (contraction AABB) or stepping (contracted
+ * grids), cone_angle >= 0.
  * Pass 1 (offsets == NULL): counts[i] = number of samples of ray i.
  * Pass 2: writes ray index, t0, t1 of every sample at offsets[i] + j.
  * The sample point is xyz = fmaf(t_mid, dir, origin).  max_steps bounds the
  * loop; a ray that reaches it is cut there and flagged in *overflow. */
 void or_march(const float *rays_o, const float *rays_d, const float *t_min, const float *t_max,
               int64_t n_rays, const float *roi, const uint8_t *binary, int rx, int ry, int rz,
-              float step, float cone, int64_t max_steps, int32_t *counts, const int64_t *offsets,
-              int32_t *ray_indices, float *t_starts, float *t_ends, int32_t *overflow) {
+              int contraction, float step, float cone, int64_t max_steps, int32_t *counts,
+              const int64_t *offsets, int32_t *ray_indices, float *t_starts, float *t_ends,
+              int32_t *overflow) {
     const int res[3] = {rx, ry, rz};
     for (int64_t i = 0; i < n_rays; ++i) {
         const float *o = rays_o + i * 3, *d = rays_d + i * 3;
@@ -286,7 +303,7 @@ void or_march(const float *rays_o, const float *rays_d, const float *t_min, cons
             if (++it > max_steps) { if (overflow) *overflow = 1; break; }
             float xyz[3];
             for (int k = 0; k < 3; ++k) xyz[k] = fmaf(tm, d[k], o[k]);
-            if (or_occupied(xyz, roi, binary, res)) {
+            if (or_occupied(xyz, roi, binary, res, contraction)) {
                 if (offsets) {
                     const int64_t p = offsets[i] + j;
                     ray_indices[p] = (int32_t)i;
@@ -294,6 +311,11 @@ void or_march(const float *rays_o, const float *rays_d, const float *t_min, cons
                     t_ends[p] = t1;
                 }
                 ++j;
+                t0 = t1;
+                t1 = t0 + or_calc_dt(t0, cone, dt_min, dt_max);
+                tm = (t0 + t1) * 0.5f;
+            } else if (contraction != 0) {
+                /* a contracted grid is not skipped: the next step */
                 t0 = t1;
                 t1 = t0 + or_calc_dt(t0, cone, dt_min, dt_max);
                 tm = (t0 + t1) * 0.5f;
