@@ -181,6 +181,30 @@ int angelo_march_compact(const float *scratch, int32_t per_ray, const int32_t *c
                          int32_t *ray_indices, float *t_starts, float *t_ends, int32_t *status,
                          void *stream);
 
+/* ------------------------------------------------------- marching cubes */
+
+/* Isosurface of an nx x ny x nz float32 lattice (x-major: value (i,j,k) at
+ * (i*ny + j)*nz + k) at `level`, replacing PyMCubes in MarchingCubeHelper
+ * (models/geometry.py:79-113; isosurface() triangulates the SDF at 0.001).
+ * One vertex per lattice edge whose ends straddle the level (value >= level
+ * on one end), linearly interpolated; triangles per cube from a 256-case
+ * table built by a face-walk rule that cuts off the corners at or above the
+ * level (the mesh is closed where the surface stays inside the lattice;
+ * triangles face the higher values).  No counterpart table in the reference
+ * (it calls PyMCubes): the vertex set is the same, the triangulation of
+ * ambiguous faces may differ.
+ * angelo_mc_count fills the workspace (angelo_mc_workspace_size bytes) and
+ * writes the vertex and face totals to totals (device int64[2]);
+ * angelo_mc_extract then writes vertices (totals[0] x 3 floats, origin +
+ * index * spacing) and faces (totals[1] x 3 int64 vertex indices); either
+ * output may be NULL. */
+int64_t angelo_mc_workspace_size(int32_t nx, int32_t ny, int32_t nz);
+int angelo_mc_count(const float *grid, int32_t nx, int32_t ny, int32_t nz, float level,
+                    void *workspace, int64_t *totals, void *stream);
+int angelo_mc_extract(const float *grid, int32_t nx, int32_t ny, int32_t nz, float level,
+                      const float *origin3, const float *spacing3, const void *workspace,
+                      float *vertices, int64_t *faces, void *stream);
+
 /* ------------------------------------------------------- occupancy update */
 
 /* OccupancyGrid._update's EMA + threshold (models/neus.py:108-109 through

@@ -86,6 +86,10 @@ SIGNATURES = {
                                   c_vp]),
     "angelo_density_weights_fwd": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp]),
     "angelo_density_weights_bwd": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "angelo_mc_workspace_size": (c_i64, [c_i32, c_i32, c_i32]),
+    "angelo_mc_count": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_f32, c_vp, c_vp, c_vp]),
+    "angelo_mc_extract": (c_i32, [c_vp, c_i32, c_i32, c_i32, c_f32, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                  c_vp]),
     "angelo_weights_fwd": (c_i32, [c_vp, c_vp, c_i64, c_f32, c_vp, c_vp, c_vp]),
     "angelo_weights_bwd": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_f32, c_vp, c_vp, c_vp]),
     "angelo_accumulate_fwd": (c_i32, [c_vp, c_vp, c_i32, c_vp, c_i64, c_vp, c_vp]),

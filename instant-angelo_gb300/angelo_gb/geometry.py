@@ -255,13 +255,13 @@ class VolumeSDF(nn.Module):
         """The SDF query lattice of MarchingCubeHelper (models/geometry.py:60-113):
         points x_min + i * (2/resolution) per axis over the bounds, evaluated in
         blocks of (block_res+1)^3 lattice points.  Returns the (nx,ny,nz)
-        float32 SDF grid and the axes; the reference triangulates -(-sdf) =
-        sdf at the 0.001 level (models/geometry.py:84,101,119,148)."""
+        float32 SDF grid on `device` and the axes; the reference triangulates
+        -(-sdf) = sdf at the 0.001 level (models/geometry.py:84,101,119,148)."""
         r = self.radius
         bounds = bounds or ((-r, r), (-r, r), (-r, r))
         intv = 2.0 / resolution
         axes = [torch.arange(lo, hi, intv) for lo, hi in bounds]
-        grid = torch.empty(*[len(a) for a in axes], dtype=torch.float32)
+        grid = torch.empty(*[len(a) for a in axes], dtype=torch.float32, device=device)
         for xi in range(0, len(axes[0]), block_res):
             for yi in range(0, len(axes[1]), block_res):
                 for zi in range(0, len(axes[2]), block_res):
@@ -271,16 +271,20 @@ class VolumeSDF(nn.Module):
                     X, Y, Z = torch.meshgrid(xs, ys, zs, indexing="ij")
                     xyz = torch.stack([X, Y, Z], -1).to(device)
                     sdf = self.forward_level(xyz.reshape(-1, 3)).reshape(X.shape)
-                    grid[xi:xi + len(xs), yi:yi + len(ys), zi:zi + len(zs)] = sdf.float().cpu()
+                    grid[xi:xi + len(xs), yi:yi + len(ys), zi:zi + len(zs)] = sdf.float()
         return grid, axes
 
     @torch.no_grad()
     def isosurface(self):
+        """MarchingCubeHelper.forward at threshold 0.001 (models/geometry.py:
+        88-113, 144-149): the lattice on the device, triangulated there (one
+        mesh, vertices shared across the reference's blocks)."""
         iso = self.config.get("isosurface")
         if iso is None:
             raise NotImplementedError
         from . import mesh
         sdf, axes = self.sdf_grid(int(iso.resolution))
-        v, f = mesh.marching_cubes(sdf.numpy(), 0.001)
-        v = v * (2.0 / int(iso.resolution)) + np.array([a[0].item() for a in axes], np.float32)
-        return {"v_pos": torch.from_numpy(v), "t_pos_idx": torch.from_numpy(f.astype(np.int64))}
+        intv = 2.0 / int(iso.resolution)
+        v, f = mesh.marching_cubes(sdf, 0.001, origin=[float(a[0]) for a in axes],
+                                   spacing=(intv, intv, intv))
+        return {"v_pos": v.cpu(), "t_pos_idx": f.cpu()}
