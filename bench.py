@@ -51,7 +51,7 @@ N_VIEWS, W, H, FOV, CAM_R = 8, 1600, 1200, 40.0, 1.5
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--forms", default="auto",
@@ -75,49 +75,78 @@ def dist_env():
 
 
 class Clocks:
-    """nvidia-smi sampling of SM clock and throttle reasons during a region."""
+    """nvidia-smi sampling of SM clock and throttle reasons.  The sampler starts
+    before the warm-up steps (its own start-up then falls outside the timed
+    region) and the summary keeps the samples stamped inside the window that
+    `mark()` opened and closed; with fewer than three there, every sample of
+    the sampler's run (warm-up and timed steps, all under load)."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 100
 
     def __init__(self, index):
         self.index = index
         self.proc = None
+        self.window = [None, None]
 
     def __enter__(self):
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                 "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)], stdout=self.f,
                 stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+        # wait (up to 5 s) for the first sample: the sampler is then running
+        # when the warm-up steps start
+        t_end = time.time() + 5.0
+        while self.proc is not None and self.proc.poll() is None and time.time() < t_end:
+            if os.path.getsize(self.f.name) > 0:
+                break
+            time.sleep(0.02)
         return self
+
+    def mark(self, i):
+        """i = 0: the timed region starts now; i = 1: it ended."""
+        self.window[i] = time.time()
 
     def __exit__(self, *a):
         if self.proc is not None:
             self.proc.terminate()
             self.proc.wait(timeout=10)
 
+    @staticmethod
+    def _stamp(s):
+        import datetime
+        try:
+            return datetime.datetime.strptime(s.strip(), "%Y/%m/%d %H:%M:%S.%f").timestamp()
+        except ValueError:
+            return None
+
     def summary(self):
         self.f.flush()
         rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
         os.unlink(self.f.name)
-        sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        parsed = []
         for r in rows:
             try:
-                sm.append(float(r[1]))
-                mx = float(r[2])
-                for nm, v in zip(names, r[5:9]):
-                    if v.strip().lower() == "active":
-                        reasons.add(nm)
+                parsed.append((self._stamp(r[0]), float(r[2]), float(r[3]),
+                               {nm for nm, v in zip(names, r[6:10]) if v.strip().lower() == "active"}))
             except (ValueError, IndexError):
                 continue
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "samples": len(sm), "reasons": sorted(reasons)}
+        t0, t1 = self.window
+        inside = [p for p in parsed if p[0] is not None and t0 is not None and t1 is not None
+                  and t0 - 0.05 <= p[0] <= t1 + 0.05]
+        use, where = (inside, "timed steps") if len(inside) >= 3 else (parsed, "warm-up and timed steps")
+        sm = [p[1] for p in use]
+        reasons = set().union(*[p[3] for p in use]) if use else set()
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": use[-1][2] if use else None, "samples": len(sm),
+                "period_ms": self.PERIOD_MS, "window": where, "reasons": sorted(reasons)}
 
 
 def measured_peaks():
@@ -233,16 +262,20 @@ def step_host(tr, feed, dev):
     return rays.shape[0], n_samples, h2d, loss_h.numel() * loss_h.element_size()
 
 
-def timed(fn, steps, dev, world):
+def timed(fn, steps, dev, world, clk=None):
     torch.cuda.synchronize(dev)
     if world > 1:
         torch.distributed.barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
+    if clk is not None:
+        clk.mark(0)
     e0.record()
     acc = [fn() for _ in range(steps)]
     e1.record()
     torch.cuda.synchronize(dev)
+    if clk is not None:
+        clk.mark(1)
     if world > 1:
         torch.distributed.barrier()
     ms = e0.elapsed_time(e1)
@@ -405,29 +438,33 @@ def run_ours(args):
     hbm_peak, _, peak_kind = measured_peaks()
     for form in forms:
         model, tr = make_trainer(form, dev)
-        # every measured pass starts from the same state: the analytic
-        # occupancy grid and the initial ray count (the grid update every 16
-        # steps re-derives the grid from the untrained field, which changes
-        # the samples per ray), then its own warm-up steps
-        grids = [model.occupancy_grid] + ([model.occupancy_grid_bg] if model.learned_background else [])
-        start = ([(g.occs.clone(), g.bits.clone()) for g in grids], tr.train_num_rays, tr.global_step)
+        # every measured pass starts from the same state: the model's
+        # parameters and buffers (the analytic occupancy grid among them) as
+        # initialised, empty optimizer moments, the initial ray count and the
+        # same global step, then its own warm-up steps.  Without this, each
+        # pass would train the field further, and the grid refresh every 16
+        # steps (re-derived from the field) would change the samples per ray
+        # from one pass to the next.
+        snap = {k: v.detach().clone() for k, v in model.state_dict().items()}
+        start = (tr.train_num_rays, tr.global_step)
 
         def reset():
-            for g, (occs, bits) in zip(grids, start[0]):
-                g.occs.copy_(occs)
-                g.bits.copy_(bits)
-            tr.train_num_rays, tr.global_step = start[1], start[2]
+            with torch.no_grad():
+                for k, v in model.state_dict().items():
+                    v.copy_(snap[k])
+            tr.optimizer.state.clear()
+            tr.train_num_rays, tr.global_step = start
 
         gen = torch.Generator(device=dev).manual_seed(1234 + rank)
-        for _ in range(args.warmup):
-            step_device(tr, views, gen)
         with Clocks(local) as clk:
+            for _ in range(args.warmup):
+                step_device(tr, views, gen)
             # profiler range (cudaProfilerStart/Stop) marks the timed steps
             # for a capture started with --profile-from-start off; the
             # backward kernels launch from autograd's own thread, which an
             # NVTX range of this thread would not cover
             torch.cuda.profiler.start()
-            ms, acc = timed(lambda: step_device(tr, views, gen), args.steps, dev, world)
+            ms, acc = timed(lambda: step_device(tr, views, gen), args.steps, dev, world, clk)
             torch.cuda.profiler.stop()
         torch.cuda.synchronize(dev)
         # per-call CUDA events (roofline, kernel shares, launch count) over a
@@ -487,8 +524,9 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (hash table 0.43 GB + AdamW state)",
                    "per_call_events": "roofline, kernel_ms and gpu_launches from a second "
                    "timed pass of the same number of steps",
-                   "passes": "each pass (value, per-call events, e2e) starts from the analytic "
-                   "occupancy grid, 8192 rays and the same global step, then W warm-up steps"},
+                   "passes": "each pass (value, per-call events, e2e) starts from the same "
+                   "initial model, empty optimizer moments, the analytic occupancy grid, 8192 "
+                   "rays and the same global step, then W warm-up steps"},
         "e2e": R["e2e"], "roofline": R["roofline"], "clocks": R["clocks"],
         "gpu_launches": R["gpu_launches"], "kernel_ms": R["kernel_ms"],
         "forms": {f: {"value": round(v["value"], 1), "ms_per_step": round(v["ms_per_step"], 3),
