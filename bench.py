@@ -58,6 +58,7 @@ def parse():
                     help="comma list of plain,fused,fused_bg (auto: all built)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-mesh", action="store_true")
     ap.add_argument("--sdf-case", type=int, default=0, metavar="N",
                     help="profiling case: 3 fused VolumeSDF training passes (16 levels x 2^22, "
                          "FD + curvature) on N points of the full model, then exit")
@@ -319,6 +320,13 @@ def algorithmic_bytes(name, u):
     return None
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per processed
+# sample of a call, from one ncu capture of its kernels on a step of this
+# workload (the four kernels of one angelo_sdf_stencil_bwd call: 2.479 GB
+# for 284,088 samples); `traffic` scales it to the launch's samples.
+TRAFFIC_BYTES_PER_SAMPLE = {"angelo_sdf_stencil_bwd": 2.479e9 / 284088}
+
+
 def roofline(summary, hbm_peak, peak_kind):
     best = None
     for name, (calls, ms, units) in summary.items():
@@ -340,8 +348,13 @@ def roofline(summary, hbm_peak, peak_kind):
                 "unit": "GB/s", "frac": None, "traffic": None,
                 "peak_source": peak_kind}, shares
     gbs = total_bytes / (ms * 1e-3) / 1e9
+    traffic = None
+    if name in TRAFFIC_BYTES_PER_SAMPLE:
+        traffic = int(TRAFFIC_BYTES_PER_SAMPLE[name] * sum(u["n"] for u in units) / calls)
     return {"kernel": name, "bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_peak,
-            "unit": "GB/s", "frac": round(gbs / hbm_peak, 4), "traffic": None,
+            "unit": "GB/s", "frac": round(gbs / hbm_peak, 4), "traffic": traffic,
+            "traffic_source": "ncu DRAM bytes per sample of this call on the full step, "
+            "times the launch's samples" if traffic else None,
             "bytes_per_launch": int(total_bytes / calls), "launches": calls,
             "ms_per_launch": round(ms / calls, 4), "peak_source": peak_kind}, shares
 
@@ -537,6 +550,8 @@ def run_ours(args):
         line["fused_vs_plain"] = round(results["fused"]["value"] / results["plain"]["value"], 3)
     if rank == 0 and not args.no_serving and "fused" in forms:
         line["serving"] = run_serving(dev, seed=1000 + rank)
+    if rank == 0 and not args.no_mesh:
+        line["mesh"] = run_mesh(dev, hbm_peak)
     if rank == 0 and not args.no_cpu_baseline:
         model, tr = make_trainer("plain", dev)
         model.update_step(0, GLOBAL_STEP)
@@ -644,6 +659,91 @@ def run_serving(dev, seed, n_render=16, n_grid=4, rate=50.0):
     out["served_vs_plain"] = round(out["served_mrays_per_s"] / out["plain_sequential"]["mrays_per_s"], 2)
     del plain
     torch.cuda.empty_cache()
+    return out
+
+
+MESH_RES = 512
+
+
+def run_mesh(dev, hbm_peak, res=MESH_RES):
+    """Mesh extraction (models/geometry.py:79-113, export.py:57-78), measured
+    three ways: marching cubes on a resident res^3 lattice of the union
+    scene's analytic SDF (device time, CUDA events, the lattice larger than
+    L2); the same from a pinned host lattice with the mesh read back (wall
+    clock); and the full model's export at isosurface resolution 512 (field
+    lattice + triangulation + vertex colours and normals, to host tensors).
+    The CPU figure is the oracle's restatement on a 64^3 block of the same
+    lattice that the torus tube's inner wall crosses."""
+    from angelo_gb import mesh, models, scenes, workloads
+    from angelo_gb.config import to_config
+    ax = torch.linspace(-0.5, 0.5, res, device=dev)
+    X, Y, Z = torch.meshgrid(ax, ax, ax, indexing="ij")
+    lat = scenes.UnionScene().sdf(torch.stack([X, Y, Z], -1)).contiguous()
+    del X, Y, Z
+    sp = 1.0 / (res - 1)
+    org, spc = (-0.5, -0.5, -0.5), (sp, sp, sp)
+    for _ in range(3):
+        v, f = mesh.marching_cubes(lat, 0.0, org, spc)
+    times = []
+    for _ in range(10):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        e0.record()
+        v, f = mesh.marching_cubes(lat, 0.0, org, spc)
+        e1.record()
+        torch.cuda.synchronize(dev)
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    cells = (res - 1) ** 3
+    nbytes = lat.numel() * 4 + v.shape[0] * 12 + f.shape[0] * 24
+    out = {"workload": f"marching cubes, {res}^3 lattice of the torus/box/sphere union SDF at "
+                       "level 0", "vertices": int(v.shape[0]), "triangles": int(f.shape[0]),
+           "ms": round(ms, 3), "gcells_per_s": round(cells / ms / 1e6, 3),
+           "roofline": {"bound": "hbm", "achieved": round(nbytes / ms / 1e6, 1),
+                        "peak": hbm_peak, "unit": "GB/s",
+                        "frac": round(nbytes / ms / 1e6 / hbm_peak, 4),
+                        "bytes": int(nbytes), "note": "lattice read once + mesh written once"}}
+    lat_h = lat.cpu().pin_memory()
+    walls = []
+    for i in range(4):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        v2, f2 = mesh.marching_cubes(lat_h.to(dev, non_blocking=True), 0.0, org, spc)
+        v2, f2 = v2.cpu(), f2.cpu()
+        walls.append(time.perf_counter() - t0)
+    out["e2e"] = {"ms": round(1e3 * statistics.median(walls[1:]), 2),
+                  "h2d_bytes": lat_h.numel() * 4, "d2h_bytes": v2.numel() * 4 + f2.numel() * 8}
+    del lat, v, f, v2, f2
+    torch.cuda.empty_cache()
+    # the reference's export path on the full model (isosurface resolution 512)
+    torch.manual_seed(0)
+    m = models.make("neus", workloads.model_config("full", fused=True)).to(dev).eval()
+    m.update_step(0, GLOBAL_STEP)
+    ecfg = to_config({"chunk_size": 2097152, "export_vertex_color": True})
+    m.export(ecfg)
+    walls = []
+    for _ in range(2):
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        msh = m.export(ecfg)
+        walls.append(time.perf_counter() - t0)
+    out["export"] = {"ms": round(1e3 * min(walls), 1), "resolution": 512,
+                     "vertices": int(msh["v_pos"].shape[0]), "triangles": int(msh["t_pos_idx"].shape[0]),
+                     "what": "full model (16 lv x 2^22, untrained: the geometric-init sphere): SDF "
+                             "lattice, triangulation, vertex colours and normals, to host tensors"}
+    del m, msh
+    torch.cuda.empty_cache()
+    # oracle on a bounded block
+    from oracle import mcubes as mc_oracle
+    i0 = int(round((0.2 + 0.5) / sp)) - 32   # the torus tube's inner wall at x = 0.2
+    j0 = k0 = res // 2 - 32
+    blk = lat_h[i0:i0 + 64, j0:j0 + 64, k0:k0 + 64].numpy()
+    t0 = time.perf_counter()
+    vb, fb = mc_oracle.marching_cubes(blk, 0.0)
+    dt = time.perf_counter() - t0
+    out["cpu_baseline"] = {"value": round(63 ** 3 / dt / 1e6, 4), "unit": "Mcells/s", "cores": 1,
+                           "kind": "port", "sample": f"64^3 block of the lattice ({len(fb)} "
+                           "triangles), the oracle's Python restatement"}
     return out
 
 

@@ -261,15 +261,17 @@ class VolumeSDF(nn.Module):
         bounds = bounds or ((-r, r), (-r, r), (-r, r))
         intv = 2.0 / resolution
         axes = [torch.arange(lo, hi, intv) for lo, hi in bounds]
+        # the 1-D axes go to the device once; each block's points are formed there
+        axes_d = [a.to(device) for a in axes]
         grid = torch.empty(*[len(a) for a in axes], dtype=torch.float32, device=device)
         for xi in range(0, len(axes[0]), block_res):
             for yi in range(0, len(axes[1]), block_res):
                 for zi in range(0, len(axes[2]), block_res):
-                    xs = axes[0][xi:xi + block_res + 1]
-                    ys = axes[1][yi:yi + block_res + 1]
-                    zs = axes[2][zi:zi + block_res + 1]
+                    xs = axes_d[0][xi:xi + block_res + 1]
+                    ys = axes_d[1][yi:yi + block_res + 1]
+                    zs = axes_d[2][zi:zi + block_res + 1]
                     X, Y, Z = torch.meshgrid(xs, ys, zs, indexing="ij")
-                    xyz = torch.stack([X, Y, Z], -1).to(device)
+                    xyz = torch.stack([X, Y, Z], -1)
                     sdf = self.forward_level(xyz.reshape(-1, 3)).reshape(X.shape)
                     grid[xi:xi + len(xs), yi:yi + len(ys), zi:zi + len(zs)] = sdf.float()
         return grid, axes

@@ -20,7 +20,9 @@ def dev():
     return torch.device("cuda:0")
 
 
-@pytest.mark.parametrize("shape,level", [((2, 2, 2), 0.0), ((9, 13, 7), 0.1), ((23, 17, 20), -0.3)])
+@pytest.mark.parametrize("shape,level", [((2, 2, 2), 0.0), ((9, 13, 7), 0.1), ((23, 17, 20), -0.3),
+                                         ((3, 4, 33), 0.1), ((4, 3, 64), -0.2), ((5, 6, 70), 0.0),
+                                         ((2, 5, 31), 0.3)])
 def test_random_lattice_matches_oracle(dev, shape, level):
     from angelo_gb import mesh
     g = np.random.default_rng(sum(shape)).normal(size=shape).astype(np.float32)
