@@ -365,6 +365,44 @@ int angelo_adamw_step(float *param, const float *grad, float *exp_avg, float *ex
                       float lr, float beta1, float beta2, float eps, float weight_decay,
                       float bias_correction1, float bias_correction2, void *stream);
 
+/* ----------------------------------------------------- weight norm and loss */
+
+/* nn.utils.weight_norm (dim 0) of n_layers <= 8 layers at once, as VanillaMLP
+ * applies it to the geometry MLP (models/network_utils.py:132-133): layer i
+ * has rows[i] x cols[i] row-major v[i], g[i] (rows[i] values) and output
+ * w[i] = g * v / ||v||_row.  The backward writes (not accumulates)
+ * dg = (dW . v) / n and dv = (g / n) dW - (g (dW . v) / n^3) v, n = ||v||_row.
+ * Pointer arrays are host arrays of device pointers. */
+int angelo_weight_norm_fwd(int32_t n_layers, const int32_t *rows, const int32_t *cols,
+                           const float *const *v, const float *const *g, float *const *w,
+                           void *stream);
+int angelo_weight_norm_bwd(int32_t n_layers, const int32_t *rows, const int32_t *cols,
+                           const float *const *v, const float *const *g, const float *const *dw,
+                           float *const *dv, float *const *dg, void *stream);
+
+/* The loss the NeuS training step seeds (systems/neus.py:130-159): rgb MSE
+ * over the valid rays (valid: n_rays bytes, nonzero = valid), eikonal
+ * mean((||grad|| - 1)^2) over n_samples, curvature mean(|laplace|) (laplace
+ * may be NULL: term 0).  out (device float[5]) = total = w_rgb rgb +
+ * w_eikonal eikonal + w_curvature curvature (the curvature term only when
+ * w_curvature > 0), rgb, eikonal, curvature, n_valid.  No valid ray gives a
+ * NaN rgb term, as the reference's mse over an empty selection does.
+ * workspace: angelo_loss_workspace_size() bytes, zeroed once before the
+ * first call (the call leaves it zeroed).  Sums reduce in a fixed order.
+ * The backward writes dL/d(rgb_pred), dL/d(sdf_grad) and (when d_laplace is
+ * not NULL) dL/d(laplace) for dL/dtotal = *d_total, from the forward's out
+ * (stats). */
+int64_t angelo_loss_workspace_size(void);
+int angelo_neus_loss_fwd(const float *rgb_pred, const float *rgb_true, const uint8_t *valid,
+                         int64_t n_rays, const float *sdf_grad, const float *laplace,
+                         int64_t n_samples, float w_rgb, float w_eikonal, float w_curvature,
+                         void *workspace, float *out, void *stream);
+int angelo_neus_loss_bwd(const float *rgb_pred, const float *rgb_true, const uint8_t *valid,
+                         int64_t n_rays, const float *sdf_grad, const float *laplace,
+                         int64_t n_samples, float w_rgb, float w_eikonal, float w_curvature,
+                         const float *stats, const float *d_total, float *d_rgb, float *d_grad,
+                         float *d_laplace, void *stream);
+
 /* ----------------------------------------------------- fused radiance network */
 
 /* Bytes of the prepared radiance-MLP buffer for a feature input of feat_dim

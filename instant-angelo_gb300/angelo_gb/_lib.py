@@ -111,6 +111,13 @@ SIGNATURES = {
     "angelo_tc_mma_rate": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "angelo_adamw_step": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_f32, c_f32, c_f32,
                                   c_f32, c_f32, c_vp]),
+    "angelo_weight_norm_fwd": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_weight_norm_bwd": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_loss_workspace_size": (c_i64, []),
+    "angelo_neus_loss_fwd": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64, c_f32, c_f32, c_f32,
+                                     c_vp, c_vp, c_vp]),
+    "angelo_neus_loss_bwd": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_i64, c_f32, c_f32, c_f32,
+                                     c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "angelo_radiance_net_bytes": (c_i64, [c_i32]),
     "angelo_radiance_grad_size": (c_i64, [c_i32]),
     "angelo_radiance_prep": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),

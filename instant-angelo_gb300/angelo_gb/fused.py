@@ -158,6 +158,57 @@ class _FusedSdf(torch.autograd.Function):
         return (None, None, d_table, None, *flat)
 
 
+class _WeightNorm(torch.autograd.Function):
+    """W_i = g_i * v_i / ||v_i||_row for every layer in one launch, and the
+    backward in one launch (angelo_weight_norm_fwd/bwd)."""
+
+    @staticmethod
+    def forward(ctx, *vg):
+        vs = [t.detach().float().contiguous() for t in vg[0::2]]
+        gs = [t.detach().float().contiguous() for t in vg[1::2]]
+        n = len(vs)
+        ws = [torch.empty_like(v) for v in vs]
+        rows = (ctypes.c_int32 * n)(*[v.shape[0] for v in vs])
+        cols = (ctypes.c_int32 * n)(*[v.shape[1] for v in vs])
+        ptrs = lambda ts: (ctypes.c_void_p * n)(*[t.data_ptr() for t in ts])
+        call("angelo_weight_norm_fwd", n, rows, cols, ptrs(vs), ptrs(gs), ptrs(ws), _s(vs[0].device))
+        ctx.save_for_backward(*vs, *gs)
+        ctx.n = n
+        return tuple(ws)
+
+    @staticmethod
+    def backward(ctx, *dws):
+        n = ctx.n
+        vs, gs = ctx.saved_tensors[:n], ctx.saved_tensors[n:]
+        dws = [d.float().contiguous() if d is not None else torch.zeros_like(v) for d, v in zip(dws, vs)]
+        dvs = [torch.empty_like(v) for v in vs]
+        dgs = [torch.empty_like(g) for g in gs]
+        rows = (ctypes.c_int32 * n)(*[v.shape[0] for v in vs])
+        cols = (ctypes.c_int32 * n)(*[v.shape[1] for v in vs])
+        ptrs = lambda ts: (ctypes.c_void_p * n)(*[t.data_ptr() for t in ts])
+        call("angelo_weight_norm_bwd", n, rows, cols, ptrs(vs), ptrs(gs), ptrs(dws), ptrs(dvs),
+             ptrs(dgs), _s(vs[0].device))
+        out = []
+        for dv, dg in zip(dvs, dgs):
+            out += [dv, dg]
+        return tuple(out)
+
+
+def effective_weights(mlp):
+    """[(W, b)] of a VanillaMLP: weight-normalised layers through the native
+    weight norm (one launch forward, one backward), plain layers as they are."""
+    from .network_utils import WNLinear
+    lins = mlp.linears()
+    wn = [m for m in lins if isinstance(m, WNLinear)]
+    if not wn or len(wn) > 8 or not wn[0].weight_v.is_cuda:
+        return mlp.effective_weights()
+    vg = []
+    for m in wn:
+        vg += [m.weight_v, m.weight_g]
+    ws = iter(_WeightNorm.apply(*vg))
+    return [(next(ws) if isinstance(m, WNLinear) else m.weight, m.bias) for m in lins]
+
+
 def _net_for(geom):
     net = getattr(geom, "_fused_net", None)
     mlp = geom.network
@@ -179,7 +230,7 @@ def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
         pts_c = (pos - (-geom.radius)) / (geom.radius - (-geom.radius))
         rd = geom.curvature_dirs_fn(pts_c).float().contiguous()
     weights = []
-    for W, b in geom.network.effective_weights():
+    for W, b in effective_weights(geom.network):
         weights += [W, b]
     table = geom.hashgrid.encoding.params
     meta = dict(geom=geom, net=net, flags=(bool(with_grad), bool(with_laplace),

@@ -28,6 +28,67 @@ def loss_terms(out, rgb, eikonal_weight=0.1, curvature_weight=5e-4, rgb_mse_weig
     return total, terms
 
 
+class _NeusLoss(torch.autograd.Function):
+    """loss_terms in two launches (angelo_neus_loss_fwd/bwd): returns (total,
+    rgb_mse, eikonal, curvature); only the total carries a gradient."""
+
+    _ws = {}
+
+    @staticmethod
+    def forward(ctx, rgb_pred, rgb_true, valid, sdf_grad, laplace, w_rgb, w_eik, w_curv):
+        from . import _lib
+        from .ops import _p, _s
+        dev = rgb_pred.device
+        ws = _NeusLoss._ws.get(dev)
+        if ws is None:
+            ws = torch.zeros(_lib.raw("angelo_loss_workspace_size")(), dtype=torch.uint8, device=dev)
+            _NeusLoss._ws[dev] = ws
+        c = rgb_pred.detach().float().contiguous()
+        t = rgb_true.detach().float().contiguous()
+        v = valid.reshape(-1).to(torch.bool).contiguous()
+        g = sdf_grad.detach().float().contiguous()
+        lap = laplace.detach().float().contiguous().reshape(-1) if laplace is not None else None
+        out = torch.empty(5, device=dev)
+        _lib.call("angelo_neus_loss_fwd", _p(c), _p(t), _p(v), c.shape[0], _p(g),
+                  _p(lap) if lap is not None else None, g.shape[0], float(w_rgb), float(w_eik),
+                  float(w_curv), _p(ws), _p(out), _s(dev))
+        ctx.save_for_backward(c, t, v, g, lap if lap is not None else torch.empty(0, device=dev), out)
+        ctx.has_lap = lap is not None
+        ctx.w = (float(w_rgb), float(w_eik), float(w_curv))
+        ctx.lap_shape = laplace.shape if laplace is not None else None
+        terms = out[1:4].clone()
+        ctx.mark_non_differentiable(terms)
+        return out[0].clone(), terms
+
+    @staticmethod
+    def backward(ctx, d_total, d_terms):
+        from . import _lib
+        from .ops import _p, _s
+        c, t, v, g, lap, stats = ctx.saved_tensors
+        dev = c.device
+        dt = (d_total if d_total is not None else torch.zeros((), device=dev)).float().reshape(1).contiguous()
+        d_c = torch.empty_like(c)
+        d_g = torch.empty_like(g)
+        d_lap = torch.empty_like(lap) if ctx.has_lap else None
+        _lib.call("angelo_neus_loss_bwd", _p(c), _p(t), _p(v), c.shape[0], _p(g),
+                  _p(lap) if ctx.has_lap else None, g.shape[0], *ctx.w, _p(stats), _p(dt), _p(d_c),
+                  _p(d_g), _p(d_lap) if d_lap is not None else None, _s(dev))
+        return (d_c, None, None, d_g, d_lap.view(ctx.lap_shape) if d_lap is not None else None,
+                None, None, None)
+
+
+def fused_loss_terms(out, rgb, eikonal_weight=0.1, curvature_weight=5e-4, rgb_mse_weight=10.0):
+    """loss_terms through the native loss (same terms and weights)."""
+    lap = out["sdf_laplace_samples"] if curvature_weight > 0 else None
+    total, t = _NeusLoss.apply(out["comp_rgb_full"], rgb, out["rays_valid_full"][..., 0],
+                               out["sdf_grad_samples"], lap, rgb_mse_weight, eikonal_weight,
+                               curvature_weight)
+    terms = {"rgb_mse": t[0], "eikonal": t[1]}
+    if curvature_weight > 0:
+        terms["curvature"] = t[2]
+    return total, terms
+
+
 class NeuSTrainer:
     """One training step = update_step (band mask, FD eps, cosine anneal,
     occupancy refresh every 16 steps) -> forward -> losses -> backward ->
@@ -76,10 +137,11 @@ class NeuSTrainer:
             self.train_num_rays = min(int(self.train_num_rays * 0.9 + new * 0.1),
                                       self.max_train_num_rays)
         lc = self.loss_cfg
-        loss, terms = loss_terms(out, rgb,
-                                 eikonal_weight=self.C(lc.get("lambda_eikonal", 0.1)),
-                                 curvature_weight=self.C(lc.get("lambda_curvature", 5e-4)),
-                                 rgb_mse_weight=self.C(lc.get("lambda_rgb_mse", 10.0)))
+        fn = fused_loss_terms if getattr(m, "fused", False) else loss_terms
+        loss, terms = fn(out, rgb,
+                         eikonal_weight=self.C(lc.get("lambda_eikonal", 0.1)),
+                         curvature_weight=self.C(lc.get("lambda_curvature", 5e-4)),
+                         rgb_mse_weight=self.C(lc.get("lambda_rgb_mse", 10.0)))
         self.optimizer.zero_grad(set_to_none=True)
         loss.backward()
         self.optimizer.step()
