@@ -366,6 +366,9 @@ class _FusedComposite(torch.autograd.Function):
                               acc_n, weights, trans)
         ctx.meta = meta
         ctx.mark_non_differentiable(weights)
+        # outputs the loss does not use (opacity, depth, normals) arrive as
+        # None, which the kernel reads as zero: no zero-filled gradients
+        ctx.set_materialize_grads(False)
         return opacity, depth, comp_rgb, comp_normal, comp_full, weights
 
     @staticmethod
