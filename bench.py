@@ -467,6 +467,7 @@ def run_ours(args):
                     v.copy_(snap[k])
             tr.optimizer.state.clear()
             tr.train_num_rays, tr.global_step = start
+            gen.manual_seed(1234 + rank)   # the same ray batches as the first pass
 
         gen = torch.Generator(device=dev).manual_seed(1234 + rank)
         with Clocks(local) as clk:
@@ -539,7 +540,8 @@ def run_ours(args):
                    "timed pass of the same number of steps",
                    "passes": "each pass (value, per-call events, e2e) starts from the same "
                    "initial model, empty optimizer moments, the analytic occupancy grid, 8192 "
-                   "rays and the same global step, then W warm-up steps"},
+                   "rays and the same global step, then W warm-up steps; the per-call pass "
+                   "replays the value pass's ray batches, e2e draws its own on the host"},
         "e2e": R["e2e"], "roofline": R["roofline"], "clocks": R["clocks"],
         "gpu_launches": R["gpu_launches"], "kernel_ms": R["kernel_ms"],
         "forms": {f: {"value": round(v["value"], 1), "ms_per_step": round(v["ms_per_step"], 3),

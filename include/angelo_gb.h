@@ -364,6 +364,15 @@ int angelo_tc_mma_rate(int32_t M, int32_t N, int32_t n, int64_t *cycles, int32_t
 int angelo_adamw_step(float *param, const float *grad, float *exp_avg, float *exp_avg_sq, int64_t n,
                       float lr, float beta1, float beta2, float eps, float weight_decay,
                       float bias_correction1, float bias_correction2, void *stream);
+/* The same update for n_tensors tensors in one launch per 32 (host arrays of
+ * device pointers, sizes and per-tensor hyper-parameters); bit-identical to
+ * angelo_adamw_step on each tensor.  For the many small MLP tensors. */
+int angelo_adamw_step_multi(int32_t n_tensors, float *const *params, const float *const *grads,
+                            float *const *exp_avg, float *const *exp_avg_sq, const int64_t *sizes,
+                            const float *lr, const float *beta1, const float *beta2,
+                            const float *eps, const float *weight_decay,
+                            const float *bias_correction1, const float *bias_correction2,
+                            void *stream);
 
 /* ----------------------------------------------------- weight norm and loss */
 

@@ -111,6 +111,8 @@ SIGNATURES = {
     "angelo_tc_mma_rate": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "angelo_adamw_step": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_f32, c_f32, c_f32,
                                   c_f32, c_f32, c_vp]),
+    "angelo_adamw_step_multi": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                        c_vp, c_vp, c_vp, c_vp]),
     "angelo_weight_norm_fwd": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "angelo_weight_norm_bwd": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "angelo_loss_workspace_size": (c_i64, []),

@@ -1,11 +1,13 @@
 """AdamW of the reference's optimizer config (systems/utils.py:314-325:
 torch.optim.AdamW(lr, betas, eps), default weight decay 0.01, per-group lr)
-with the update as one libangelo_gb streaming pass per parameter
-(angelo_adamw_step).  Same parameter groups, hyper-parameters and state
+with the update as one libangelo_gb streaming pass per large parameter
+(angelo_adamw_step) and one launch for all small ones (angelo_adamw_step_multi).  Same parameter groups, hyper-parameters and state
 names (step, exp_avg, exp_avg_sq) as torch.optim.AdamW, so state dicts load
 either way.  Parameters must be float32 CUDA tensors; there is no other
 path."""
 from __future__ import annotations
+
+import ctypes
 
 import torch
 
@@ -20,12 +22,16 @@ class AdamW(torch.optim.Optimizer):
         super().__init__(params, dict(lr=lr, betas=tuple(betas), eps=eps,
                                       weight_decay=weight_decay))
 
+    # tensors below this size share one multi-tensor launch per step
+    SMALL = 1 << 16
+
     @torch.no_grad()
     def step(self, closure=None):
         loss = None
         if closure is not None:
             with torch.enable_grad():
                 loss = closure()
+        small = []
         for group in self.param_groups:
             b1, b2 = group["betas"]
             for p in group["params"]:
@@ -43,8 +49,24 @@ class AdamW(torch.optim.Optimizer):
                 st["step"] += 1
                 t = float(st["step"])
                 g = p.grad if p.grad.is_contiguous() else p.grad.contiguous()
+                hp = (float(group["lr"]), float(b1), float(b2), float(group["eps"]),
+                      float(group["weight_decay"]), 1.0 - b1 ** t, 1.0 - b2 ** t)
+                if p.numel() < self.SMALL:
+                    small.append((p, g, st, hp))
+                    continue
                 call("angelo_adamw_step", _p(p), _p(g), _p(st["exp_avg"]), _p(st["exp_avg_sq"]),
-                     p.numel(), float(group["lr"]), float(b1), float(b2), float(group["eps"]),
-                     float(group["weight_decay"]), 1.0 - b1 ** t, 1.0 - b2 ** t, _s(p.device),
+                     p.numel(), *hp, _s(p.device),
                      launches=1 if p.numel() % 4 == 0 else 2, units=dict(n=p.numel()))
+        by_dev = {}
+        for item in small:
+            by_dev.setdefault(item[0].device, []).append(item)
+        for dev, items in by_dev.items():
+            n = len(items)
+            ptrs = lambda ts: (ctypes.c_void_p * n)(*[x.data_ptr() for x in ts])
+            f32 = lambda j: (ctypes.c_float * n)(*[it[3][j] for it in items])
+            call("angelo_adamw_step_multi", n, ptrs([it[0] for it in items]),
+                 ptrs([it[1] for it in items]), ptrs([it[2]["exp_avg"] for it in items]),
+                 ptrs([it[2]["exp_avg_sq"] for it in items]),
+                 (ctypes.c_int64 * n)(*[it[0].numel() for it in items]), *[f32(j) for j in range(7)],
+                 _s(dev), launches=(n + 31) // 32, units=dict(n=sum(it[0].numel() for it in items)))
         return loss

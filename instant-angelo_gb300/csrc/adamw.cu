@@ -66,6 +66,38 @@ __global__ void adamw_scalar_kernel(float *__restrict__ p, const float *__restri
 
 bool aligned16(const void *x) { return (reinterpret_cast<uintptr_t>(x) & 15) == 0; }
 
+// Many small tensors in one launch: block b of the grid takes chunk
+// b - blk0[k] (kMultiChunk elements) of tensor k, each tensor with its own
+// hyper-parameters; the per-element update is adamw_one, as above.
+constexpr int kMultiMax = 32, kMultiChunk = 2048;
+
+struct MultiAdam {
+    int n;
+    int64_t blk0[kMultiMax + 1];
+    float *p[kMultiMax];
+    const float *g[kMultiMax];
+    float *m[kMultiMax];
+    float *v[kMultiMax];
+    int64_t size[kMultiMax];
+    AdamArgs a[kMultiMax];
+};
+
+__global__ void adamw_multi_kernel(const __grid_constant__ MultiAdam M) {
+    int k = 0;
+    for (int i = 1; i < M.n; ++i)
+        if ((int64_t)blockIdx.x >= M.blk0[i]) k = i;
+    const int64_t base = ((int64_t)blockIdx.x - M.blk0[k]) * kMultiChunk;
+    const int64_t end = base + kMultiChunk < M.size[k] ? base + kMultiChunk : M.size[k];
+    const AdamArgs a = M.a[k];
+    for (int64_t i = base + threadIdx.x; i < end; i += blockDim.x) {
+        float pp = M.p[k][i], mm = M.m[k][i], vv = M.v[k][i];
+        adamw_one(pp, M.g[k][i], mm, vv, a);
+        M.p[k][i] = pp;
+        M.m[k][i] = mm;
+        M.v[k][i] = vv;
+    }
+}
+
 }  // namespace
 
 extern "C" int angelo_adamw_step(float *param, const float *grad, float *exp_avg, float *exp_avg_sq,
@@ -108,4 +140,52 @@ extern "C" int angelo_adamw_step(float *param, const float *grad, float *exp_avg
                                                                 exp_avg_sq + head, rest, a);
     }
     return check_launch("adamw_step");
+}
+
+extern "C" int angelo_adamw_step_multi(int32_t n_tensors, float *const *params, const float *const *grads,
+                                       float *const *exp_avg, float *const *exp_avg_sq, const int64_t *sizes,
+                                       const float *lr, const float *beta1, const float *beta2, const float *eps,
+                                       const float *weight_decay, const float *bias_correction1,
+                                       const float *bias_correction2, void *stream) {
+    ANGELO_REQUIRE(n_tensors >= 0, "adamw_step_multi: negative count");
+    if (n_tensors == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(params && grads && exp_avg && exp_avg_sq && sizes && lr && beta1 && beta2 && eps &&
+                       weight_decay && bias_correction1 && bias_correction2,
+                   "adamw_step_multi: null array");
+    cudaStream_t s = as_stream(stream);
+    for (int32_t t0 = 0; t0 < n_tensors; t0 += kMultiMax) {
+        MultiAdam M{};
+        M.n = 0;
+        int64_t blocks = 0;
+        for (int32_t t = t0; t < n_tensors && t < t0 + kMultiMax; ++t) {
+            ANGELO_REQUIRE(sizes[t] >= 0, "adamw_step_multi: tensor %d has negative size", t);
+            if (sizes[t] == 0) continue;
+            ANGELO_REQUIRE(params[t] && grads[t] && exp_avg[t] && exp_avg_sq[t],
+                           "adamw_step_multi: tensor %d has a null pointer", t);
+            ANGELO_REQUIRE(bias_correction1[t] > 0.f && bias_correction2[t] > 0.f,
+                           "adamw_step_multi: tensor %d bias corrections", t);
+            const int k = M.n++;
+            M.blk0[k] = blocks;
+            blocks += (sizes[t] + kMultiChunk - 1) / kMultiChunk;
+            M.p[k] = params[t];
+            M.g[k] = grads[t];
+            M.m[k] = exp_avg[t];
+            M.v[k] = exp_avg_sq[t];
+            M.size[k] = sizes[t];
+            AdamArgs &a = M.a[k];
+            a.lr = lr[t];
+            a.beta1 = beta1[t];
+            a.beta2 = beta2[t];
+            a.eps = eps[t];
+            a.wd = weight_decay[t];
+            a.step_size = lr[t] / bias_correction1[t];
+            a.bc2_sqrt = sqrtf(bias_correction2[t]);
+        }
+        if (M.n == 0) continue;
+        M.blk0[M.n] = blocks;
+        ANGELO_REQUIRE(blocks < (1ll << 31), "adamw_step_multi: %lld blocks", (long long)blocks);
+        adamw_multi_kernel<<<(unsigned)blocks, 256, 0, s>>>(M);
+        if (int rc = check_launch("adamw_step_multi")) return rc;
+    }
+    return ANGELO_OK;
 }

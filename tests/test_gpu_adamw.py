@@ -75,3 +75,29 @@ def test_adamw_param_groups_and_unaligned(dev):
     o3.step()
     o4.step()
     np.testing.assert_allclose(u.detach().cpu().numpy(), u2.detach().cpu().numpy(), rtol=2e-5, atol=1e-7)
+
+
+def test_multi_tensor_launch_is_bit_identical(dev):
+    """Small tensors go through one angelo_adamw_step_multi launch; the update
+    equals angelo_adamw_step on each tensor bit for bit."""
+    import ctypes
+    from angelo_gb._lib import call
+    from angelo_gb.ops import _p, _s
+    g = torch.Generator(device="cpu").manual_seed(5)
+    sizes = [1, 3, 64 * 35, 4096, 2049, 65]
+    ps = [torch.randn(n, generator=g).to(dev) for n in sizes]
+    gs = [torch.randn(n, generator=g).to(dev) for n in sizes]
+    ms = [torch.rand(n, generator=g).to(dev) * 0.1 for n in sizes]
+    vs = [torch.rand(n, generator=g).to(dev) * 0.01 for n in sizes]
+    single = [[t.clone() for t in ts] for ts in (ps, ms, vs)]
+    hp = [(0.01 * (i + 1), 0.9, 0.99, 1e-15, 0.01, 1 - 0.9 ** 3, 1 - 0.99 ** 3) for i in range(len(sizes))]
+    for i in range(len(sizes)):
+        call("angelo_adamw_step", _p(single[0][i]), _p(gs[i]), _p(single[1][i]), _p(single[2][i]),
+             sizes[i], *hp[i], _s(dev))
+    n = len(sizes)
+    ptr = lambda ts: (ctypes.c_void_p * n)(*[t.data_ptr() for t in ts])
+    f32 = lambda j: (ctypes.c_float * n)(*[h[j] for h in hp])
+    call("angelo_adamw_step_multi", n, ptr(ps), ptr(gs), ptr(ms), ptr(vs), (ctypes.c_int64 * n)(*sizes),
+         *[f32(j) for j in range(7)], _s(dev))
+    for a, b in zip(ps + ms + vs, single[0] + single[1] + single[2]):
+        assert torch.equal(a, b)
