@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-mesh", action="store_true")
+    ap.add_argument("--max-rays", type=int, default=8192,
+                    help="ray budget per step (profiling case: fewer rays, same model and views)")
     ap.add_argument("--sdf-case", type=int, default=0, metavar="N",
                     help="profiling case: 3 fused VolumeSDF training passes (16 levels x 2^22, "
                          "FD + curvature) on N points of the full model, then exit")
@@ -166,6 +168,9 @@ def make_views(dev):
     return scenes.TargetViews(scenes.UnionScene(), N_VIEWS, W, H, FOV, CAM_R, seed=0, device=dev)
 
 
+MAX_RAYS = 8192   # the full workload's ray budget (--max-rays shrinks it for kernel captures)
+
+
 def make_trainer(form, dev, seed=0):
     from angelo_gb import models, scenes, workloads
     from angelo_gb.system import NeuSTrainer
@@ -187,7 +192,7 @@ def make_trainer(form, dev, seed=0):
             # the background grid starts with every cell occupied
             model.occupancy_grid_bg.occs.fill_(1.0)
             model.occupancy_grid_bg.bits.fill_(-1)
-    tr = NeuSTrainer(model, workloads.SYSTEM, train_num_rays=8192, max_train_num_rays=8192,
+    tr = NeuSTrainer(model, workloads.SYSTEM, train_num_rays=MAX_RAYS, max_train_num_rays=MAX_RAYS,
                      train_num_samples=1 << 18)
     tr.global_step = GLOBAL_STEP
     return model, tr
@@ -815,7 +820,9 @@ def run_sdf_case(n):
 
 
 def main():
+    global MAX_RAYS
     args = parse()
+    MAX_RAYS = args.max_rays
     if args.sdf_case:
         run_sdf_case(args.sdf_case)
         return
