@@ -6,6 +6,8 @@
 // each ray is marched by one thread exactly in the reference's order; the
 // occupancy bitfield (res^3 bits, 256 KiB at 128^3) stays L1/L2 resident.
 // Count, scan and fill are three launches, as in the reference.
+#include <cmath>
+
 #include "common.cuh"
 
 using namespace angelo;
@@ -15,9 +17,22 @@ namespace {
 struct Grid {
     float lo[3], hi[3];
     int res[3];
+    // bit d set: the extent hi - lo (pow2_ext) or the resolution (pow2_res)
+    // of axis d is a power of two, and a division by it is the exact
+    // multiplication by its reciprocal: RN(x / 2^k) = RN(x * 2^-k), both the
+    // correctly rounded value of the same real number
+    int pow2_ext, pow2_res;
+    float inv_ext[3], inv_res[3];
     const uint32_t *bits;
     int contraction;   // ANGELO_CONTRACT_*
 };
+
+__device__ __forceinline__ float div_ext(const Grid &g, int d, float x) {
+    return ((g.pow2_ext >> d) & 1) ? __fmul_rn(x, g.inv_ext[d]) : __fdiv_rn(x, __fsub_rn(g.hi[d], g.lo[d]));
+}
+__device__ __forceinline__ float div_res(const Grid &g, int d, float x) {
+    return ((g.pow2_res >> d) & 1) ? __fmul_rn(x, g.inv_res[d]) : __fdiv_rn(x, (float)g.res[d]);
+}
 
 __device__ __forceinline__ bool occupied(const Grid &g, const float xyz[3]) {
     float u[3];
@@ -27,15 +42,14 @@ __device__ __forceinline__ bool occupied(const Grid &g, const float xyz[3]) {
             if (xyz[d] < g.lo[d] || xyz[d] > g.hi[d]) return false;
         if (g.bits == nullptr) return true;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) u[d] = __fdiv_rn(__fsub_rn(xyz[d], g.lo[d]), __fsub_rn(g.hi[d], g.lo[d]));
+        for (int d = 0; d < 3; ++d) u[d] = div_ext(g, d, __fsub_rn(xyz[d], g.lo[d]));
     } else {
         // unbounded sphere: roi -> [-1,1]^3; beyond the unit sphere
         // x <- (2 - 1/|x|) x/|x|; the radius-2 ball -> [0,1]^3
         if (g.bits == nullptr) return true;
 #pragma unroll
         for (int d = 0; d < 3; ++d)
-            u[d] = __fsub_rn(__fmul_rn(__fdiv_rn(__fsub_rn(xyz[d], g.lo[d]), __fsub_rn(g.hi[d], g.lo[d])), 2.0f),
-                             1.0f);
+            u[d] = __fsub_rn(__fmul_rn(div_ext(g, d, __fsub_rn(xyz[d], g.lo[d])), 2.0f), 1.0f);
         const float nrm = __fsqrt_rn(__fmaf_rn(u[2], u[2], __fmaf_rn(u[1], u[1], __fmul_rn(u[0], u[0]))));
         if (nrm > 1.0f) {
             const float sc = __fsub_rn(2.0f, __fdiv_rn(1.0f, nrm));
@@ -71,9 +85,9 @@ __device__ __forceinline__ float dist_next_voxel(const Grid &g, const float xyz[
     for (int d = 0; d < 3; ++d) {
         const float ext = __fsub_rn(g.hi[d], g.lo[d]);
         const float r = (float)g.res[d];
-        const float u = __fmul_rn(__fdiv_rn(__fsub_rn(xyz[d], g.lo[d]), ext), r);
+        const float u = __fmul_rn(div_ext(g, d, __fsub_rn(xyz[d], g.lo[d])), r);
         const float tgt = floorf(__fadd_rn(__fadd_rn(u, 0.5f), __fmul_rn(0.5f, sgn(dir[d]))));
-        const float td = __fmul_rn(__fdiv_rn(__fmul_rn(__fsub_rn(tgt, u), inv[d]), r), ext);
+        const float td = __fmul_rn(div_res(g, d, __fmul_rn(__fsub_rn(tgt, u), inv[d])), ext);
         t = d == 0 ? td : fminf(t, td);
     }
     return t > 0.f ? t : 0.f;
@@ -330,6 +344,23 @@ int make_grid(const angelo_grid_t *in, Grid *g) {
                        in->res[d]);
     }
     g->bits = in->bits;
+    g->pow2_ext = g->pow2_res = 0;
+    for (int d = 0; d < 3; ++d) {
+        // the same float32 subtraction as the device's; a power of two has
+        // mantissa 0.5 under frexpf
+        const float ext = g->hi[d] - g->lo[d];
+        int e = 0;
+        g->inv_ext[d] = g->inv_res[d] = 0.f;
+        if (std::isfinite(ext) && ext > 0.f && std::frexp(ext, &e) == 0.5f && e - 1 >= -126 && e - 1 <= 126) {
+            g->pow2_ext |= 1 << d;
+            g->inv_ext[d] = std::ldexp(1.0f, 1 - e);
+        }
+        const float r = (float)g->res[d];
+        if (std::frexp(r, &e) == 0.5f) {
+            g->pow2_res |= 1 << d;
+            g->inv_res[d] = std::ldexp(1.0f, 1 - e);
+        }
+    }
     ANGELO_REQUIRE(in->contraction == ANGELO_CONTRACT_AABB || in->contraction == ANGELO_CONTRACT_UNBOUNDED_SPHERE,
                    "march: contraction %d", in->contraction);
     g->contraction = in->contraction;

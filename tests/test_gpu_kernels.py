@@ -145,10 +145,12 @@ def _random_bits(res, p, seed):
     return b.reshape(res, res, res), words
 
 
-@pytest.mark.parametrize("p_occ", [1.0, 0.3, 0.02, 0.0])
-def test_march_bit_exact(dev, p_occ):
+@pytest.mark.parametrize("p_occ,r,res", [(1.0, 0.5, 128), (0.3, 0.5, 128), (0.02, 0.5, 128),
+                                         (0.0, 0.5, 128), (0.3, 0.7, 96), (0.02, 0.7, 96)])
+def test_march_bit_exact(dev, p_occ, r, res):
+    """Power-of-two extents and resolutions (0.5 box, 128^3) take the kernel's
+    exact multiplication form of the divisions; 1.4 and 96 keep the divisions."""
     from angelo_gb import ops
-    r = 0.5
     o, d = _rays(4096, 8, r)
     o[0] = [3, 3, 3]  # misses the box
     d[0] = [1, 0, 0]
@@ -161,10 +163,10 @@ def test_march_bit_exact(dev, p_occ):
     jit = np.random.default_rng(9).random(4096, dtype=np.float32)
     step = 1.732 * 2 * r / 1024
     tmin_j = (rtmin + jit * np.float32(step)).astype(np.float32)
-    binary, words = _random_bits(128, p_occ, 10)
+    binary, words = _random_bits(res, p_occ, 10)
     ri, t0, t1, off, st = ops.march(torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev),
                                     torch.from_numpy(tmin_j).to(dev), tmax, step, roi=aabb,
-                                    res=(128, 128, 128),
+                                    res=(res, res, res),
                                     bits=torch.from_numpy(words.view(np.int32)).to(dev))
     cnt, roff, rri, rt0, rt1, ovf = cref.march(o, d, tmin_j, rtmax, aabb, binary, step)
     np.testing.assert_array_equal(off.cpu().numpy(), roff)
