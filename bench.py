@@ -540,7 +540,7 @@ def run_ours(args):
                    "rays_per_step": round(R["rays_per_step"], 1),
                    "samples_per_step": round(R["samples_per_step"], 1),
                    "global_step": GLOBAL_STEP, "parallelism": f"replicas x{world}",
-                   "l2": "inputs larger than L2 (hash table 0.43 GB + AdamW state)",
+                   "l2": "inputs larger than L2 (hash table 0.37 GB + AdamW state 0.73 GB)",
                    "per_call_events": "roofline, kernel_ms and gpu_launches from a second "
                    "timed pass of the same number of steps",
                    "passes": "each pass (value, per-call events, e2e) starts from the same "
