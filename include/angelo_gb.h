@@ -259,6 +259,11 @@ typedef struct {
      * W3 (16*k_tiles3b x 64) in the K-major core-matrix layout, bf16 hi then lo */
     int64_t off_tcw1, off_tcw2, off_tcw3;
     int64_t bytes;
+    /* tensor-core products per layer in the forward kernels: 3 (bf16x3, the
+     * default the query sets: hi*hi + lo*hi + hi*lo, ~16 mantissa bits per
+     * operand) or 1 (a single bf16 pass, the precision form); the backward
+     * recompute is always bf16x3 */
+    int32_t mma_passes;
 } angelo_sdf_net_layout;
 
 int angelo_sdf_net_layout_query(int32_t n_levels, int32_t n_hidden, int32_t out_dim,
@@ -428,11 +433,12 @@ int angelo_radiance_prep(int32_t feat_dim, const float *W1, const float *b1, con
                          void *stream);
 /* VolumeRadiance / VolumeDualColor forward (models/texture.py:23-30,50-58):
  * rgb = sigmoid(MLP([feature, SH4((d+1)/2), normalize(grad)])) (+ sigmoid of
- * feature[1:4] when dual), d = rays_d[ray_idx].  precision 0: bf16x3, 1:
- * single-pass bf16. */
+ * feature[1:4] when dual), d = rays_d[ray_idx].  flags bit 0: dual colour;
+ * bit 1: the MLP in a single bf16 pass (the precision form) instead of
+ * bf16x3. */
 int angelo_radiance_fwd(int32_t feat_dim, const void *net, const float *feature,
                         int64_t feat_stride, const float *grad, const int32_t *ray_idx,
-                        const float *rays_d, int64_t n, int32_t dual, float *rgb, void *stream);
+                        const float *rays_d, int64_t n, int32_t flags, float *rgb, void *stream);
 /* Backward: d_feature (written, n x feat_stride), d_grad (written, n x 3),
  * d_net (accumulated). */
 int angelo_radiance_bwd(int32_t feat_dim, const void *net, const float *feature,

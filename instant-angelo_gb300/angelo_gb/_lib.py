@@ -47,7 +47,7 @@ class SdfNetLayout(ctypes.Structure):
                 ("k_tiles3b", c_i32), ("out_dim", c_i32),
                 ("off_b1", c_i64), ("off_b2", c_i64), ("off_b3", c_i64),
                 ("off_w3row0", c_i64), ("off_tcw1", c_i64), ("off_tcw2", c_i64),
-                ("off_tcw3", c_i64), ("bytes", c_i64)]
+                ("off_tcw3", c_i64), ("bytes", c_i64), ("mma_passes", c_i32)]
 
 
 class AngeloError(RuntimeError):

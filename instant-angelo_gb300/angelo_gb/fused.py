@@ -233,6 +233,7 @@ def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
     for W, b in effective_weights(geom.network):
         weights += [W, b]
     table = geom.hashgrid.encoding.params
+    net.layout.mma_passes = 1 if getattr(geom, "fused_precision", "fp32") == "bf16" else 3
     meta = dict(geom=geom, net=net, flags=(bool(with_grad), bool(with_laplace),
                                            bool(with_feature)))
     with torch.set_grad_enabled(geom.training and torch.is_grad_enabled()):
@@ -296,8 +297,9 @@ class _FusedRadiance(torch.autograd.Function):
         grad = grad.contiguous()
         S = feature.shape[0]
         rgb = torch.empty(S, 3, device=feature.device)
+        flags = int(dual) | (2 if meta.get("one_pass") else 0)
         call("angelo_radiance_fwd", net.feat_dim, _p(net.buf), _p(feature), feature.stride(0),
-             _p(grad), _p(ray_idx), _p(rays_d), S, int(dual), _p(rgb), _s(feature.device),
+             _p(grad), _p(ray_idx), _p(rays_d), S, flags, _p(rgb), _s(feature.device),
              units=dict(n=S, F=net.feat_dim, bwd=False))
         ctx.save_for_backward(feature, grad, ray_idx, rays_d)
         ctx.meta = meta
@@ -331,7 +333,8 @@ def radiance_forward(texture, feature, grad, ray_idx, rays_d):
     weights = []
     for W, b in texture.network.effective_weights():
         weights += [W, b]
-    meta = dict(net=net, dual=bool(getattr(texture, "dual", False)))
+    meta = dict(net=net, dual=bool(getattr(texture, "dual", False)),
+                one_pass=getattr(texture, "fused_precision", "fp32") == "bf16")
     return _FusedRadiance.apply(feature, grad, ray_idx, rays_d, meta, *weights)
 
 

@@ -173,6 +173,9 @@ class NeuSModel(nn.Module):
         self.fused = fused
         self.geometry = models.make(config.geometry.name, config.geometry)
         self.texture = models.make(config.texture.name, config.texture)
+        # "bf16": the forward MLPs of the fused kernels in one bf16 pass (the
+        # precision form); "fp32" (default): bf16x3
+        self.texture.fused_precision = config.get("fused_precision", "fp32")
         self.geometry.contraction_type = "aabb"
         self.learned_background = bool(config.get("learned_background", False))
         if self.learned_background:

@@ -109,6 +109,7 @@ struct RadParams {
     const float *rays_d;
     int64_t S;
     int dual;
+    int passes;   // forward tensor-core products per layer: 3 (bf16x3) or 1 (one bf16 pass)
     float *rgb;
     const float *g_rgb;
     float *d_feature;
@@ -229,7 +230,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) rad_fwd_tc_kernel(const __grid_
         const bool v = s < P.S;
         tc_publish();
         if (tid == 0) {
-            tc_mma<KT1>(tmem, Xk, W1k, id64, false);
+            tc_mma_p<KT1>(tmem, Xk, W1k, id64, false, P.passes);
             tc::commit(bar);
         }
         if (!(alive = tc_wait_all(bar, phase))) break;
@@ -246,8 +247,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) rad_fwd_tc_kernel(const __grid_
             stage16(hh, hl, row, 16 * slice, 64, z);
             tc_publish();
             if (tid == 0) {
-                if (layer == 0) tc_mma<4>(tmem + 64, Hk, W2k, id64, false);
-                else tc_mma<4>(tmem, Hk, W3k, id16, false);
+                if (layer == 0) tc_mma_p<4>(tmem + 64, Hk, W2k, id64, false, P.passes);
+                else tc_mma_p<4>(tmem, Hk, W3k, id16, false, P.passes);
                 tc::commit(bar);
             }
             if (!(alive = tc_wait_all(bar, phase))) break;
@@ -859,8 +860,9 @@ int dispatch_rad(const RadParams &P, cudaStream_t st) {
 
 extern "C" int angelo_radiance_fwd(int32_t feat_dim, const void *net, const float *feature,
                                    int64_t feat_stride, const float *grad, const int32_t *ray_idx,
-                                   const float *rays_d, int64_t n, int32_t dual, float *rgb,
+                                   const float *rays_d, int64_t n, int32_t flags, float *rgb,
                                    void *stream) {
+    ANGELO_REQUIRE((flags & ~3) == 0, "radiance_fwd: flags %d", flags);
     ANGELO_REQUIRE(feat_dim >= 1 && feat_dim + 19 <= kXCols, "radiance_fwd: feature width");
     ANGELO_REQUIRE(n >= 0, "radiance_fwd: negative n");
     if (n == 0) return ANGELO_OK;
@@ -875,7 +877,8 @@ extern "C" int angelo_radiance_fwd(int32_t feat_dim, const void *net, const floa
     P.ray_idx = ray_idx;
     P.rays_d = rays_d;
     P.S = n;
-    P.dual = dual;
+    P.dual = flags & 1;
+    P.passes = (flags & 2) ? 1 : 3;
     P.rgb = rgb;
     return dispatch_rad<false>(P, as_stream(stream));
 }

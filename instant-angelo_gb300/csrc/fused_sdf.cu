@@ -444,7 +444,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
         {
             tc_publish();
             if (tid == 0) {
-                tc_mma<K1 / 16>(tmem, op_k(sA1h, Sh::a1, K1), op_k(sW1h, Sh::w1, K1), id_hidden, false);
+                tc_mma_p<K1 / 16>(tmem, op_k(sA1h, Sh::a1, K1), op_k(sW1h, Sh::w1, K1), id_hidden, false,
+                                  P.nl.mma_passes);
                 tc::commit(bar);
             }
             if (!(alive = tc_wait_all(bar, phase))) break;
@@ -466,11 +467,14 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
                 tc_publish();
                 if (tid == 0) {
                     if (layer + 1 < NH)
-                        tc_mma<4>(tmem + 64, op_k(sA2h, Sh::a2, 64), op_k(sW2h, Sh::w2, 64), id_hidden, false);
+                        tc_mma_p<4>(tmem + 64, op_k(sA2h, Sh::a2, 64), op_k(sW2h, Sh::w2, 64), id_hidden, false,
+                                    P.nl.mma_passes);
                     else if (GROUP != kCurv && e == 0 && P.with_feature)
-                        tc_mma<4>(tmem + 128, op_k(sA2h, Sh::a2, 64), op_k(sW3h, Sh::w3, 64), id_out_main, false);
+                        tc_mma_p<4>(tmem + 128, op_k(sA2h, Sh::a2, 64), op_k(sW3h, Sh::w3, 64), id_out_main, false,
+                                    P.nl.mma_passes);
                     else
-                        tc_mma<4>(tmem + 128, op_k(sA2h, Sh::a2, 64), op_k(sW3h, Sh::w3, 64), id_out_tap, false);
+                        tc_mma_p<4>(tmem + 128, op_k(sA2h, Sh::a2, 64), op_k(sW3h, Sh::w3, 64), id_out_tap, false,
+                                    P.nl.mma_passes);
                     tc::commit(bar);
                 }
                 if (!(alive = tc_wait_all(bar, phase))) break;
@@ -1143,6 +1147,7 @@ extern "C" int angelo_sdf_net_layout_query(int32_t n_levels, int32_t n_hidden, i
     L.off_tcw2 = take(n_hidden == 2 ? 2 * 64 * 64 * 2 : 0);
     L.off_tcw3 = take(2 * (16 * L.k_tiles3b) * 64 * 2);
     L.bytes = o;
+    L.mma_passes = 3;
     *out = L;
     return ANGELO_OK;
 }
@@ -1290,6 +1295,8 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
     ANGELO_REQUIRE(!with_feature || (feature && feat_stride >= nl->out_dim + 3),
                    "sdf_stencil_fwd: bad feature output");
     ANGELO_REQUIRE(eps > 0.f && radius > 0.f, "sdf_stencil_fwd: eps/radius");
+    ANGELO_REQUIRE(nl->mma_passes == 1 || nl->mma_passes == 3, "sdf_stencil_fwd: mma_passes %d (1 or 3)",
+                   nl->mma_passes);
     ANGELO_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 7) == 0, "sdf_stencil_fwd: workspace alignment");
     SdfParams P{};
     P.lay = *lay;

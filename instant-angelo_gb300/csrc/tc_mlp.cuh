@@ -122,6 +122,15 @@ __device__ __forceinline__ void tc_mma(uint32_t d, const TcOp &a, const TcOp &b,
     }
 }
 
+// D (+)= A B^T with `passes` products per K step: 3 = bf16x3 (tc_mma), 1 =
+// the hi parts alone (a single bf16 pass).  One thread.
+template <int KSTEPS>
+__device__ __forceinline__ void tc_mma_p(uint32_t d, const TcOp &a, const TcOp &b, uint32_t idesc, bool acc,
+                                         int passes) {
+    if (passes == 1) tc_mma1<KSTEPS>(d, a, b, idesc, acc);
+    else tc_mma<KSTEPS>(d, a, b, idesc, acc);
+}
+
 // The constant operand [rows = 128][16] with column 0 = 1 (bf16, hi only):
 // dZ^T times it is the column sum of dZ (a bias gradient) in column 0.
 __device__ __forceinline__ void fill_ones_operand(uint16_t *ones, int tid, int nthreads) {

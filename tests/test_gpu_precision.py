@@ -14,7 +14,10 @@ the FP64 oracle run on the GPU (oracle/neus_fp64.py):
 
 The report (max / mean absolute errors) goes to $ANGELO_PRECISION_REPORT when
 that is set.  Bounds: 1e-3 for every fused output with the FP32 table and for
-the gated alpha at every inv_s."""
+the gated alpha at every inv_s.  The precision form proper (FP16 table, the
+forward MLPs in one bf16 pass: fused_precision "bf16") is reported beside
+them; its SDF error must exceed the bf16x3 form's (the single pass is in
+effect) and stay below 0.1."""
 import json
 import math
 import os
@@ -39,10 +42,11 @@ def dev():
     return torch.device("cuda:0")
 
 
-def _model(dev, fused, fp16_table=False):
+def _model(dev, fused, fp16_table=False, one_pass=False):
     from angelo_gb import models, workloads
     torch.manual_seed(0)
-    m = models.make("neus", workloads.model_config("small", fused=fused)).to(dev)
+    extra = {"fused_precision": "bf16"} if one_pass else {}
+    m = models.make("neus", workloads.model_config("small", fused=fused, **extra)).to(dev)
     m.update_step(0, 5000)
     with torch.no_grad():
         g = torch.Generator(device="cpu").manual_seed(7)
@@ -91,7 +95,8 @@ def _write():
 def test_precision_sdf_and_normals(dev):
     from oracle import neus_fp64 as O
     forms = {"plain_fp32": _model(dev, False), "fused_fp32_table": _model(dev, True),
-             "fused_fp16_table": _model(dev, True, fp16_table=True)}
+             "fused_fp16_table": _model(dev, True, fp16_table=True),
+             "fused_fp16_table_bf16_mlp": _model(dev, True, fp16_table=True, one_pass=True)}
     P, G, _ = _oracle_cfg(forms["plain_fp32"])
     g = torch.Generator(device="cpu").manual_seed(11)
     pts = (torch.rand(N_POINTS, 3, generator=g) * 2.0 - 1.0).to(dev)
@@ -113,6 +118,11 @@ def test_precision_sdf_and_normals(dev):
         assert out[name]["sdf"]["max"] < 1e-3, (name, out[name])
         assert out[name]["normal"]["mean"] < 1e-3, (name, out[name])
     assert out["fused_fp16_table"]["sdf"]["max"] < 1e-2, out["fused_fp16_table"]
+    # the precision form proper (FP16 table, one bf16 pass per layer): its SDF
+    # error is bf16's (~2^-9 relative); the FD normal divides it by 2 eps
+    one = out["fused_fp16_table_bf16_mlp"]
+    assert one["sdf"]["max"] < 0.1 and math.isfinite(one["normal"]["max"]), one
+    assert one["sdf"]["max"] > out["fused_fp16_table"]["sdf"]["max"], (one, out["fused_fp16_table"])
 
 
 def _rays(dev):
@@ -146,7 +156,8 @@ def test_precision_render(dev):
                             1.0, bg.double(), training=True)
     out = {}
     for name, m in (("plain_fp32", plain), ("fused_fp32_table", _model(dev, True)),
-                    ("fused_fp16_table", _model(dev, True, fp16_table=True))):
+                    ("fused_fp16_table", _model(dev, True, fp16_table=True)),
+                    ("fused_fp16_table_bf16_mlp", _model(dev, True, fp16_table=True, one_pass=True))):
         m.background_color = bg
         m.geometry.curvature_dirs_fn = lambda t: rd
         m.train()
