@@ -177,3 +177,93 @@ def test_backward_matches_central_differences(dev):
         assert abs(fd - ag) <= 1e-2 * max(abs(ag), floor), (k, i, fd, ag)
         # the hand-written backward (fused) agrees with the float64 gradient
         assert abs(a - ag) <= 1e-2 * max(abs(ag), floor), ("fused", k, i, a, ag)
+
+
+def test_full_model_backward_matches_fp64(dev):
+    """The full model (16 levels x 2^22 table entries, two hidden layers of
+    64, 65 outputs, dual-colour radiance; FD eps 1/2048 at global step 6000)
+    through the fused training forward/backward: its gradients of the same
+    loss on the same samples against the float64 oracle's autograd gradient
+    (checked against central differences in the test above), on 64 rays
+    marched through the grid's inner cells."""
+    from angelo_gb import models, workloads
+    from angelo_gb.scenes import look_at_c2w, pixel_directions, rays_from
+    from oracle import neus_fp64 as O
+    torch.manual_seed(0)
+    m = models.make("neus", workloads.model_config("full", fused=True)).to(dev)
+    m.update_step(0, 6000)
+    with torch.no_grad():
+        # occupied: the cells whose centres lie within 0.35 of the origin on
+        # every axis, so that no stencil or curvature tap reaches the box
+        # boundary (where the reference's formulation differs from the
+        # fused backward: all taps of an outside point clamp to one point)
+        from angelo_gb.checkpoint import pack_bits
+        res = m.occupancy_grid.res
+        ctr = (torch.arange(res, dtype=torch.float32) + 0.5) / res - 0.5
+        inner = ctr.abs() < 0.35
+        occ = inner[:, None, None] & inner[None, :, None] & inner[None, None, :]
+        m.occupancy_grid.bits.copy_(pack_bits(occ.reshape(-1)).to(dev))
+        m.occupancy_grid.occs.copy_(occ.reshape(-1).float().to(dev))
+        g = torch.Generator(device="cpu").manual_seed(7)
+        p = m.geometry.hashgrid.encoding.params
+        p.copy_((torch.rand(p.shape, generator=g) * 0.1 - 0.05).to(dev))
+        wv = m.geometry.network.layers[0].weight_v
+        wv[:, 3:].copy_((torch.randn(wv[:, 3:].shape, generator=g) * 0.05).to(dev))
+        m.variance.variance.fill_(0.5)
+    m.train()
+    m.randomized = False
+    n_rays = 64
+    rng = np.random.default_rng(31)
+    dirs = pixel_directions(64, 64, 40.0, device=dev).reshape(-1, 3)
+    c2w = torch.as_tensor(look_at_c2w((0.9, 0.7, 0.9)), dtype=torch.float32, device=dev)
+    pix = torch.from_numpy(rng.integers(0, dirs.shape[0], n_rays)).to(dev)
+    rays = rays_from(dirs[pix], c2w[None].expand(n_rays, 3, 4)).float().contiguous()
+    target = torch.from_numpy(rng.uniform(0, 1, (n_rays, 3)).astype(np.float32)).to(dev)
+    bg = torch.ones(3, device=dev)
+    m.background_color = bg
+    o, d = rays[:, :3].contiguous(), rays[:, 3:].contiguous()
+    ri, t0, t1, off = m.march_rays(o, d)
+    assert ri.numel() > 5000
+    rd = torch.randn(ri.numel(), 3, generator=torch.Generator(device="cpu").manual_seed(5)).to(dev)
+    m.geometry.curvature_dirs_fn = lambda t: rd
+    valid = torch.ones(n_rays, dtype=torch.bool, device=dev)
+    m.zero_grad()
+    out = m.forward_(rays)
+    _loss(out, target, valid).backward()
+    ours = {k: p.grad.detach().double().clone() for k, p in m.named_parameters() if p.grad is not None}
+
+    c = m.config
+    h = c.geometry.xyz_encoding_config
+    lay = O.HashGridLayout(h.n_levels, h.n_features_per_level, h.log2_hashmap_size,
+                           h.base_resolution, h.per_level_scale)
+    G = dict(radius=float(c.radius), eps=float(m.geometry._finite_difference_eps), lay=lay,
+             active_levels=int(m.geometry.hashgrid.mask_levels),
+             n_layers=c.geometry.mlp_network_config.n_hidden_layers + 1,
+             feature_dim=c.geometry.feature_dim)
+    T = dict(kind="dual", n_layers=c.texture.mlp_network_config.n_hidden_layers + 1)
+    Pg = {k: v.detach().double().clone().requires_grad_(v.is_floating_point())
+          for k, v in m.state_dict().items()}
+    march = (off.cpu().numpy(), ri.long(), t0, t1)
+    # the cosine annealing ratio of global step 6000 (cos_anneal_end 20000)
+    r = O.neus_render(rays.double(), Pg, G, T, march, rd.double(), float(m.cos_anneal_ratio),
+                      bg.double(), training=True)
+    _loss(r, target.double(), valid).backward()
+
+    checks = []
+    tk = "geometry.encoding.encoding.encoding.params"
+    checks += [(tk, i) for i in torch.topk(ours[tk].abs(), 16).indices.tolist()]
+    for k in ("geometry.network.layers.0.weight_v", "geometry.network.layers.0.weight_g",
+              "geometry.network.layers.2.weight_v", "geometry.network.layers.4.weight_v",
+              "geometry.network.layers.4.bias", "texture.network.layers.0.weight",
+              "texture.network.layers.2.weight", "texture.network.layers.4.weight",
+              "texture.network.layers.4.bias"):
+        n = ours[k].numel()
+        checks += [(k, i) for i in torch.topk(ours[k].abs().view(-1), min(4, n)).indices.tolist()]
+    checks.append(("variance.variance", 0))
+    rows = [(k, i, float(ours[k].view(-1)[i]), float(Pg[k].grad.view(-1)[i])) for k, i in checks]
+    print("\n(param, index, fused, autograd fp64)")
+    for row in rows:
+        print(row)
+    scale = max(abs(r_[3]) for r_ in rows)
+    for k, i, a, ag in rows:
+        assert abs(a - ag) <= 1e-2 * max(abs(ag), 1e-2 * scale), ("fused", k, i, a, ag)
