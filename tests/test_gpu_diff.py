@@ -41,9 +41,10 @@ def dev():
     return torch.device("cuda:0")
 
 
-def _model(dev, fused=True):
+def _model(dev, fused=True, log2_table=16):
     from angelo_gb import models, workloads
     cfg = workloads.model_config("small", fused=fused)
+    cfg["geometry"]["xyz_encoding_config"]["log2_hashmap_size"] = log2_table
     cfg["render_step_size"] = 4.0 / 64          # 64 samples between near 0.5 and far 4.5
     cfg["texture"] = dict(
         name="volume-dual-colorV3", input_feature_dim=13 + 6, use_ide=True, ide_degree=4,
@@ -91,10 +92,13 @@ def _loss(out, target, valid_ray):
     return l_rgb + l_eik + l_curv
 
 
-def test_backward_matches_central_differences(dev):
+@pytest.mark.parametrize("log2_table", [16, 22])
+def test_backward_matches_central_differences(dev, log2_table):
+    """log2_table 22: the differentiation configuration's 2^22-entry table
+    (the finest levels hashed), the stencil recomputed in the backward."""
     from angelo_gb.scenes import look_at_c2w, pixel_directions, rays_from
     from oracle import neus_fp64 as O
-    m = _model(dev)
+    m = _model(dev, log2_table=log2_table)
     G, T = _oracle_cfg(m)
     g = np.random.default_rng(23)
     dirs = pixel_directions(128, 128, 50.0, device=dev).reshape(-1, 3)
@@ -117,7 +121,7 @@ def test_backward_matches_central_differences(dev):
     out = m.forward_(rays)
     _loss(out, target, valid).backward()
     ours = {k: p.grad.detach().double().clone() for k, p in m.named_parameters() if p.grad is not None}
-    mp = _model(dev, fused=False)
+    mp = _model(dev, fused=False, log2_table=log2_table)
     mp.load_state_dict(m.state_dict())
     mp.background_color = bg
     mp.geometry.curvature_dirs_fn = lambda t: rd
