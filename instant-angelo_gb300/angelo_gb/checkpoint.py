@@ -81,9 +81,21 @@ def to_reference(model):
     return out
 
 
-def load_reference_checkpoint(model, ckpt, strict=True):
+def load_reference_checkpoint(model, ckpt, strict=True, trusted=False):
     """Load a reference checkpoint (a path or an already loaded dict) into
-    ``model``; returns load_state_dict's (missing, unexpected) keys."""
+    ``model``; returns load_state_dict's (missing, unexpected) keys.
+
+    A path is read with torch.load(weights_only=True): tensors and plain
+    containers only.  A Lightning checkpoint that also pickles objects (its
+    hyper-parameters) needs trusted=True, which unpickles everything in it:
+    pass it only for files from a source you trust."""
     if isinstance(ckpt, (str, bytes)) or hasattr(ckpt, "__fspath__"):
-        ckpt = torch.load(ckpt, map_location="cpu", weights_only=False)
+        try:
+            ckpt = torch.load(ckpt, map_location="cpu", weights_only=True)
+        except Exception as e:   # noqa: BLE001 - the unpickler's refusal
+            if not trusted:
+                raise RuntimeError(
+                    f"{ckpt}: holds objects other than tensors ({type(e).__name__}); "
+                    "pass trusted=True to unpickle a checkpoint from a trusted source") from e
+            ckpt = torch.load(ckpt, map_location="cpu", weights_only=False)
     return model.load_state_dict(from_reference(ckpt), strict=strict)

@@ -72,3 +72,24 @@ def test_binary_cell_order():
     assert int(bits[c0 // 32]) == 1 << (c0 % 32)
     assert int(bits.ne(0).sum()) == 2
     assert torch.equal(m.occupancy_grid.binary, b)
+
+
+class _Hyper:
+    """Stands for the pickled hyper-parameter object of a Lightning checkpoint."""
+
+    def __init__(self):
+        self.lr = 0.01
+
+
+def test_pickled_objects_need_trusted(tmp_path):
+    """A checkpoint that pickles an object is refused unless trusted=True."""
+    import pytest
+    m = _model(5)
+    ref = checkpoint.to_reference(m)
+    path = tmp_path / "with_object.ckpt"
+    torch.save({"state_dict": ref, "hyper_parameters": _Hyper()}, path)
+    m2 = _model(6)
+    with pytest.raises(RuntimeError, match="trusted=True"):
+        checkpoint.load_reference_checkpoint(m2, str(path))
+    checkpoint.load_reference_checkpoint(m2, str(path), trusted=True)
+    _assert_same(m, m2)
