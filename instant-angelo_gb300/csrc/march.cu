@@ -5,7 +5,9 @@
 // dt, DDA skips over empty cells) whose rounding fixes which samples exist, so
 // each ray is marched by one thread exactly in the reference's order; the
 // occupancy bitfield (res^3 bits, 256 KiB at 128^3) stays L1/L2 resident.
-// Count, scan and fill are three launches, as in the reference.
+// Count, scan and fill are three launches, as in the reference; with a bound
+// on the samples per ray, record (count + the samples into a per-ray scratch),
+// scan and compact march each ray once.
 #include <cmath>
 
 #include "common.cuh"
