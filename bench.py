@@ -268,6 +268,25 @@ def step_host(tr, feed, dev):
     return rays.shape[0], n_samples, h2d, loss_h.numel() * loss_h.element_size()
 
 
+def max_over_ranks(x, dev, world):
+    """The largest value of x over the ranks (the job's time is its slowest
+    rank's); x itself with one rank."""
+    if world <= 1:
+        return float(x)
+    t = torch.tensor([float(x)], device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(values, dev, world):
+    """Element-wise sums of a list of counts over the ranks (whole-job work)."""
+    if world <= 1:
+        return [int(v) for v in values]
+    t = torch.tensor([float(v) for v in values], device=dev, dtype=torch.float64)
+    torch.distributed.all_reduce(t)
+    return [int(v) for v in t.tolist()]
+
+
 def timed(fn, steps, dev, world, clk=None):
     torch.cuda.synchronize(dev)
     if world > 1:
@@ -284,11 +303,7 @@ def timed(fn, steps, dev, world, clk=None):
         clk.mark(1)
     if world > 1:
         torch.distributed.barrier()
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(e0.elapsed_time(e1), dev, world)
     return ms, acc
 
 
@@ -512,10 +527,7 @@ def run_ours(args):
         assert len(feed.losses) >= args.steps and all(np.isfinite(feed.losses[-args.steps:]))
         rays_e = sum(a[0] for a in acc_e)
         samples_e = sum(a[1] for a in acc_e)
-        if world > 1:
-            t = torch.tensor([rays, rays_e, samples], device=dev, dtype=torch.float64)
-            torch.distributed.all_reduce(t)
-            rays, rays_e, samples = (int(v) for v in t.tolist())
+        rays, rays_e, samples = sum_over_ranks([rays, rays_e, samples], dev, world)
         results[form] = dict(
             value=rays / (ms * 1e-3), ms_per_step=ms / args.steps, rays_per_step=rays / args.steps
             / world, samples_per_step=samples / args.steps / world, roofline=rl,
