@@ -132,3 +132,60 @@ def marching_cubes(grid, level, origin=(0.0, 0.0, 0.0), spacing=(1.0, 1.0, 1.0))
                 f.append(vid[(int(p0[0]), int(p0[1]), int(p0[2]), a)])
             faces.append(f)
     return (np.array(verts, np.float32).reshape(-1, 3), np.array(faces, np.int64).reshape(-1, 3))
+
+
+# per case: triangle count and the (lower corner, axis) of each triangle edge
+_NTRI = np.array([len(t) for t in TABLE], np.int64)
+_TRI = np.zeros((256, 5, 3), np.int64)
+for _c, _tris in enumerate(TABLE):
+    for _t, _tri in enumerate(_tris):
+        _TRI[_c, _t] = _tri
+_EDGE_LO = np.array([_corner(c0) for c0, _ in EDGES], np.int64)           # (12, 3)
+_EDGE_AXIS = np.array([int(np.argmax(_corner(c1) - _corner(c0))) for c0, c1 in EDGES], np.int64)
+
+
+def marching_cubes_vec(grid, level, origin=(0.0, 0.0, 0.0), spacing=(1.0, 1.0, 1.0)):
+    """The same mesh as marching_cubes with whole-array numpy operations (the
+    CPU baseline's form; the loop form above is the definition it is tested
+    against): vertices in edge order (3 * point + axis), faces in cube order."""
+    g = np.ascontiguousarray(grid, np.float32)
+    nx, ny, nz = g.shape
+    lv = np.float32(level)
+    o = np.asarray(origin, np.float32)
+    sp = np.asarray(spacing, np.float32)
+    above = g >= lv
+    cross = np.zeros((nx, ny, nz, 3), bool)
+    cross[:-1, :, :, 0] = above[:-1] != above[1:]
+    cross[:, :-1, :, 1] = above[:, :-1] != above[:, 1:]
+    cross[:, :, :-1, 2] = above[:, :, :-1] != above[:, :, 1:]
+    flat = cross.reshape(-1)
+    eid = np.nonzero(flat)[0]
+    vid_of = np.cumsum(flat, dtype=np.int64) - 1
+    p, a = eid // 3, eid % 3
+    i, j, k = p // (ny * nz), (p // nz) % ny, p % nz
+    idx = np.stack([i, j, k], 1)
+    idx1 = idx.copy()
+    idx1[np.arange(len(a)), a] += 1
+    v0 = g[i, j, k]
+    v1 = g[idx1[:, 0], idx1[:, 1], idx1[:, 2]]
+    t = ((lv - v0).astype(np.float32) / (v1 - v0).astype(np.float32)).astype(np.float32)
+    q = idx.astype(np.float32)
+    q[np.arange(len(a)), a] = (q[np.arange(len(a)), a] + t).astype(np.float32)
+    verts = (o + (q * sp).astype(np.float32)).astype(np.float32)
+    case = np.zeros((nx - 1, ny - 1, nz - 1), np.int64)
+    for c in range(8):
+        dx, dy, dz = c & 1, (c >> 1) & 1, (c >> 2) & 1
+        case |= above[dx:nx - 1 + dx, dy:ny - 1 + dy, dz:nz - 1 + dz].astype(np.int64) << c
+    case = case.reshape(-1)
+    nt = _NTRI[case]
+    cubes = np.nonzero(nt)[0]
+    reps = nt[cubes]
+    cube_of = np.repeat(cubes, reps)
+    tri_of = np.arange(len(cube_of)) - np.repeat(np.cumsum(reps) - reps, reps)
+    ci, cj, ck = cube_of // ((ny - 1) * (nz - 1)), (cube_of // (nz - 1)) % (ny - 1), cube_of % (nz - 1)
+    e = _TRI[case[cube_of], tri_of]                                       # (F, 3) local edges
+    lo = _EDGE_LO[e]                                                      # (F, 3, 3)
+    pi, pj, pk = ci[:, None] + lo[..., 0], cj[:, None] + lo[..., 1], ck[:, None] + lo[..., 2]
+    gid = ((pi * ny + pj) * nz + pk) * 3 + _EDGE_AXIS[e]
+    faces = vid_of[gid]
+    return verts.reshape(-1, 3), faces.astype(np.int64).reshape(-1, 3)

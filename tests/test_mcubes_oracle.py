@@ -38,3 +38,23 @@ def test_sphere_is_closed_outward_and_has_the_area():
     area = 0.5 * np.linalg.norm(nrm, axis=1).sum()
     assert abs(area / (4 * np.pi * r * r) - 1) < 0.01
     assert np.abs(np.linalg.norm(v - c, axis=1) - r).max() < 0.05
+
+
+def test_array_form_equals_the_loop_form():
+    """marching_cubes_vec (the CPU baseline's form) gives the loop form's mesh
+    bit for bit: random lattices whose sizes are not multiples of anything,
+    and a sphere."""
+    rng = np.random.default_rng(4)
+    for shape, lv in [((2, 2, 2), 0.0), ((9, 13, 7), 0.1), ((5, 6, 33), -0.2)]:
+        g = rng.normal(size=shape).astype(np.float32)
+        a = M.marching_cubes(g, lv, (-0.7, 0.2, 1.5), (0.01, 0.02, 0.03))
+        b = M.marching_cubes_vec(g, lv, (-0.7, 0.2, 1.5), (0.01, 0.02, 0.03))
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[1], b[1])
+    n = 24
+    ax = np.arange(n, dtype=np.float32)
+    X, Y, Z = np.meshgrid(ax, ax, ax, indexing="ij")
+    sdf = (np.sqrt((X - 11.3) ** 2 + (Y - 12.1) ** 2 + (Z - 11.7) ** 2) - 8.4).astype(np.float32)
+    a, b = M.marching_cubes(sdf, 0.0), M.marching_cubes_vec(sdf, 0.0)
+    np.testing.assert_array_equal(a[0], b[0])
+    np.testing.assert_array_equal(a[1], b[1])
