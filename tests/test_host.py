@@ -111,3 +111,20 @@ def test_ide_matches_reference_golden():
     np.testing.assert_allclose(out.numpy(), g["ide"], rtol=1e-5, atol=1e-5)
     out32 = IntegratedDirEncoding(4)(torch.from_numpy(g["xyz"]), torch.from_numpy(g["kappa_inv"]))
     np.testing.assert_allclose(out32.numpy(), g["ide"], rtol=1e-4, atol=1e-4)
+
+
+def test_sdf_net_layout_query_and_struct(lib):
+    """angelo_sdf_net_layout (a host-only call): the shapes the fused kernels
+    are instantiated for, the forward's default of three products per layer,
+    and the Python mirror's size matching the C struct's field layout (the
+    last field sits after the 8-byte aligned block of offsets)."""
+    from angelo_gb import _lib
+    L = _lib.SdfNetLayout()
+    assert lib.angelo_sdf_net_layout_query(16, 2, 65, ctypes.byref(L)) == 0
+    assert (L.k_tiles1, L.n_hidden, L.n_tiles3, L.out_dim, L.mma_passes) == (3, 2, 9, 65, 3)
+    assert L.bytes > 0 and L.off_tcw1 < L.off_tcw2 < L.off_tcw3 < L.bytes
+    assert lib.angelo_sdf_net_layout_query(8, 1, 13, ctypes.byref(L)) == 0
+    assert (L.k_tiles1, L.n_hidden, L.n_tiles3, L.mma_passes) == (2, 1, 2, 3)
+    assert lib.angelo_sdf_net_layout_query(16, 3, 65, ctypes.byref(L)) != 0
+    assert _lib.SdfNetLayout.mma_passes.offset == 5 * 4 + 4 + 8 * 8
+    assert ctypes.sizeof(_lib.SdfNetLayout) == 5 * 4 + 4 + 8 * 8 + 8
