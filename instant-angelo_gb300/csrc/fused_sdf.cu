@@ -857,7 +857,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             }
         }
         tc_publish();
-        // round 1: Z1 (one hidden layer, point: also dH1 = dY W3)
+        // stage 1: Z1 (one hidden layer, point: also dH1 = dY W3)
         if (tid == 0) {
             tc_mma<K1 / 16>(tmem + Sh::tA, Xk, W1k, id_fwd, false);
             if (NH == 1 && point) tc_mma<N3 / 16>(tmem + Sh::tB, Yk, W3t, id_dh, false);
@@ -875,7 +875,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
         }
         if (NH == 2) {
             tc_publish();
-            // round 2: Z2 (point: also dH2 = dY W3)
+            // stage 2: Z2 (point: also dH2 = dY W3)
             if (tid == 0) {
                 tc_mma<4>(tmem + Sh::tB, H1k, W2k, id_fwd, false);
                 if (point) tc_mma<N3 / 16>(tmem + Sh::tA, Yk, W3t, id_dh, false);
@@ -919,7 +919,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
         if (k + 1 < n_items) load_x(k + 1, xv);
         tc_publish();
         if (NH == 2) {
-            // round 3: dH1 (epilogue), then dW2, db2, dW3
+            // stage 3: dH1 (epilogue), then dW2, db2, dW3
             if (tid == 0) {
                 tc_mma<4>(tmem + Sh::tA, Zk, W2t, id_dh, false);
                 tc::commit(&bar[0]);
@@ -939,7 +939,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             stage16_2(h1s, row, 16 * slice, 64, Sh::CH1, dz);
             tc_publish();
         }
-        // last round: dX (epilogue), then dW1, db1 (one hidden layer: dW3)
+        // last stage: dX (epilogue), then dW1, db1 (one hidden layer: dW3)
         if (tid == 0) {
             tc_mma<4>(tmem + Sh::tB, D1k, W1t, id_dx, false);
             tc::commit(&bar[0]);
