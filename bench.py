@@ -559,6 +559,10 @@ def run_ours(args):
                    "initial model, empty optimizer moments, the analytic occupancy grid, 8192 "
                    "rays and the same global step, then W warm-up steps; the per-call pass "
                    "replays the value pass's ray batches, e2e draws its own on the host"},
+        # rays/s follows the samples per ray (the ray count is resized toward
+        # 2^18 samples); the per-sample figures are the steadier comparison
+        "samples_per_s": round(R["samples_per_step"] * world / (R["ms_per_step"] * 1e-3), 1),
+        "ns_per_sample": round(R["ms_per_step"] * 1e6 / max(R["samples_per_step"], 1.0), 3),
         "e2e": R["e2e"], "roofline": R["roofline"], "clocks": R["clocks"],
         "gpu_launches": R["gpu_launches"], "kernel_ms": R["kernel_ms"],
         "forms": {f: {"value": round(v["value"], 1), "ms_per_step": round(v["ms_per_step"], 3),
