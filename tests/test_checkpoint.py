@@ -93,3 +93,18 @@ def test_pickled_objects_need_trusted(tmp_path):
         checkpoint.load_reference_checkpoint(m2, str(path))
     checkpoint.load_reference_checkpoint(m2, str(path), trusted=True)
     _assert_same(m, m2)
+
+
+def test_pack_unpack_bits_round_trip():
+    """pack_bits / unpack_bits: bit c % 32 of word c // 32, sizes that are not
+    multiples of 32, the sign bit included."""
+    g = torch.Generator().manual_seed(9)
+    for n in (1, 31, 32, 33, 1000, 4097):
+        m = torch.rand(n, generator=g) < 0.5
+        w = checkpoint.pack_bits(m)
+        assert w.dtype == torch.int32 and w.numel() == (n + 31) // 32
+        assert torch.equal(checkpoint.unpack_bits(w, n), m)
+        for c in torch.nonzero(m)[:, 0].tolist()[:20]:
+            assert (int(w[c // 32]) >> (c % 32)) & 1 == 1
+    full = torch.ones(64, dtype=torch.bool)
+    assert checkpoint.pack_bits(full).tolist() == [-1, -1]
