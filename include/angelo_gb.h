@@ -151,8 +151,11 @@ int angelo_scan(const int32_t *counts, int64_t n, int64_t *offsets, void *worksp
  * every GPU loading the library keeps until the process exits; n may be at
  * most ANGELO_SCAN_NOALLOC_MAX_N (larger n returns ANGELO_E_INVALID).  All
  * calls share that array: calls whose kernels overlap on the GPU race, so
- * order them on one stream.  The first call on a device looks up the array's
- * address with that device current; make it before any stream capture. */
+ * order them on one stream.  Each call made outside stream capture looks up
+ * the array's address with the calling device current (so a re-created
+ * context is followed); a call under capture reuses the last address looked
+ * up on that device, so make the first call on a device before any stream
+ * capture (a first call under capture returns ANGELO_E_INVALID). */
 #define ANGELO_SCAN_NOALLOC_MAX_N (1LL << 24)
 int angelo_scan_noalloc(const int32_t *counts, int64_t n, int64_t *offsets, void *stream);
 
@@ -163,6 +166,14 @@ int angelo_march_fill(const float *rays_o, const float *rays_d, const float *t_m
                       float cone_angle, int64_t max_steps, const int64_t *offsets,
                       int64_t capacity, int32_t *ray_indices, float *t_starts, float *t_ends,
                       int32_t *status, void *stream);
+
+/* offsets[0..n_rays] = min(offsets, capacity), in place.  After a
+ * march_fill into a fixed capacity (which drops the samples at or past it),
+ * this keeps every consumer that walks [offsets[r], offsets[r+1]) -- the
+ * weights, accumulation and fused compositing -- inside the capacity; the
+ * overflow itself stays flagged in the fill's status (bit 1).  No
+ * counterpart in the reference (nerfacc sizes its outputs exactly). */
+int angelo_offsets_clamp(int64_t *offsets, int64_t n_rays, int64_t capacity, void *stream);
 
 /* Single-march variant of passes 1 and 2 (no counterpart in the reference;
  * same samples): march_record marches every ray once, writing its sample
@@ -332,32 +343,6 @@ int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32_t active_l
  * on a CUDA error.  A diagnostic counter: the one piece of mutable device
  * state of the library besides the allocation-free scan's workspace. */
 int64_t angelo_tc_timeouts(int32_t reset);
-
-/* A (M x K) * B (N x K)^T, M = 64 or 128, on the 5th-generation tensor
- * cores (tcgen05.mma, operands in shared memory, fp32 accumulation in tensor
- * memory) with both operands split into bf16 hi/lo (three products).  D
- * (128 x W, fp32, row-major, W = N for M = 128 and 2N for M = 64) receives
- * every tensor-memory lane of the accumulator's first W columns: for M = 128
- * lane i is row i of the product.
- * a_mn_major / b_mn_major stage the operand MN-major (0: K-major); variant 0
- * is the descriptor convention the fused kernels use, 1 exchanges the
- * descriptor's two core-matrix strides (a layout self-check).  N in 16..256
- * (multiple of 16; at most 128 for M = 64), K in 16..64 (multiple of 16).
- * *status (zeroed by the caller) becomes 1 if the completion wait timed out.
- * No counterpart in the reference: it pins the layouts the fused MLP kernels
- * rely on. */
-int angelo_tc_gemm_x3(const float *A, const float *B, float *D, int32_t M, int32_t N, int32_t K,
-                      int32_t a_mn_major, int32_t b_mn_major, int32_t variant, int32_t *status,
-                      void *stream);
-
-/* Issue cost of the tensor-core instruction the fused MLPs are built from:
- * one thread issues n (1..4096) back-to-back tcgen05.mma of shape M x N x 16
- * (bf16, fp32 accumulation; M 64 or 128, N 16..256, multiple of 16) on
- * zero operands.  cycles[0] = SM clocks spent issuing, cycles[1] = until
- * the last product completed.  *status (zeroed by the caller) becomes 1 if
- * the completion wait timed out.  No counterpart in the reference. */
-int angelo_tc_mma_rate(int32_t M, int32_t N, int32_t n, int64_t *cycles, int32_t *status,
-                       void *stream);
 
 /* ------------------------------------------------------------------- AdamW */
 

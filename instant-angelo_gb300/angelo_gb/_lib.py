@@ -77,6 +77,7 @@ SIGNATURES = {
     "angelo_scan_noalloc": (c_i32, [c_vp, c_i64, c_vp, c_vp]),
     "angelo_march_fill": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, _P(GridDesc), c_f32, c_f32,
                                   c_i64, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_offsets_clamp": (c_i32, [c_vp, c_i64, c_i64, c_vp]),
     "angelo_march_record": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, _P(GridDesc), c_f32, c_f32,
                                     c_i64, c_i32, c_vp, c_vp, c_vp, c_vp]),
     "angelo_march_compact": (c_i32, [c_vp, c_i32, c_vp, c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp,
@@ -106,9 +107,6 @@ SIGNATURES = {
                                        c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_i32, c_i32, c_vp,
                                        c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp]),
     "angelo_tc_timeouts": (c_i64, [c_i32]),
-    "angelo_tc_gemm_x3": (c_i32, [c_vp, c_vp, c_vp, c_i32, c_i32, c_i32, c_i32, c_i32, c_i32, c_vp,
-                                  c_vp]),
-    "angelo_tc_mma_rate": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_vp]),
     "angelo_adamw_step": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_i64, c_f32, c_f32, c_f32, c_f32, c_f32,
                                   c_f32, c_f32, c_vp]),
     "angelo_adamw_step_multi": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,

@@ -282,7 +282,7 @@ def occ_update(occs, cells, occ, decay, thre, bits):
     ws = torch.empty(_lib.raw("angelo_occ_workspace_size")(n_cells), device=occs.device,
                      dtype=torch.uint8)
     call("angelo_occ_update", _p(occs), n_cells, _p(cells), _p(occ), cells.numel(), float(decay),
-         float(thre), _p(bits), _p(ws), _s(occs.device), launches=4 if cells.numel() else 3)
+         float(thre), _p(bits), _p(ws), _s(occs.device), launches=5 if cells.numel() else 4)
 
 
 # ---------------------------------------------------------------- compositing

@@ -14,7 +14,9 @@ A render bucket is: clip to the near/far planes or the scene box, march
 point and its 6 FD taps: the normal needs them, the curvature does not), the
 fused radiance network and the fused compositing.  Nothing in it synchronises
 with the host, so it is captured once.  A bucket whose samples overflow the
-capacity is re-rendered through the exact-size path (the same kernels).
+capacity is re-rendered through the exact-size path (the same kernels); its
+offsets are clamped to the capacity first, so the bucket's own compositing
+reads and writes only the samples the fill kept.
 
 The reference serves one request at a time through NeuSModel.forward in eval
 mode, in 2048-ray chunks moved to the CPU (models/neus.py:285-293,
@@ -182,6 +184,10 @@ class RenderBucket:
         _lib.call("angelo_march_fill", P(oc), P(dc), P(t_min), P(t_max), self.B,
                   ctypes.byref(self.grid), float(m.render_step_size), 0.0, int(m.max_march_steps),
                   P(self.offsets), self.cap, P(self.ri), P(self.t0), P(self.t1), P(self.status), s)
+        # an overflowing bucket keeps the samples below the capacity: clamp
+        # the offsets so the compositing walks only those (the bucket is then
+        # re-rendered exactly, status bit 1)
+        _lib.call("angelo_offsets_clamp", P(self.offsets), self.B, self.cap, s)
         self.out = _shade(m, oc, dc, self.ri, self.t0, self.t1, self.offsets, self.bg)
 
     @torch.no_grad()

@@ -89,17 +89,55 @@ def fused_loss_terms(out, rgb, eikonal_weight=0.1, curvature_weight=5e-4, rgb_ms
     return total, terms
 
 
+# lambda_* keys of the reference's loss config (systems/neus.py:130-196) that
+# this step does not compute; each names the term it weights.  lambda_normal
+# belongs to the sdf_l1 term (it is added inside that branch, :182-194).
+UNSUPPORTED_LOSS_TERMS = {
+    "lambda_rgb_l1": "rgb L1 (systems/neus.py:134-136)",
+    "lambda_mask": "foreground-mask BCE (systems/neus.py:142-145)",
+    "lambda_opaque": "opacity BCE (systems/neus.py:147-149)",
+    "lambda_sparsity": "SDF sparsity (systems/neus.py:151-153)",
+    "lambda_distortion": "distortion (systems/neus.py:163-166)",
+    "lambda_distortion_bg": "background distortion (systems/neus.py:168-171)",
+    "lambda_sdf_l1": "SDF L1 + normal on SfM points (systems/neus.py:180-194)",
+}
+
+
+def unsupported_loss_terms(loss_cfg, global_step, has_mask=True):
+    """The loss terms a config asks for at global_step (scheduled weight > 0)
+    that this step does not compute, as {key: description}.  The mask term
+    counts only when the data has masks (the reference multiplies it by 0
+    otherwise, systems/neus.py:145)."""
+    out = {}
+    for key, what in UNSUPPORTED_LOSS_TERMS.items():
+        if key not in loss_cfg:
+            continue
+        if key == "lambda_mask" and not has_mask:
+            continue
+        if scheduled_value(loss_cfg[key], global_step) > 0:
+            out[key] = what
+    return out
+
+
 class NeuSTrainer:
     """One training step = update_step (band mask, FD eps, cosine anneal,
     occupancy refresh every 16 steps) -> forward -> losses -> backward ->
     AdamW (angelo_gb.optim, one native pass per parameter).  Ray counts follow
-    the reference's dynamic sampling rule."""
+    the reference's dynamic sampling rule.
+
+    The step computes the rgb MSE, eikonal and curvature terms; a loss config
+    that gives any other term a weight > 0 at the current step raises
+    NotImplementedError instead of training a different objective
+    (has_mask: whether the rays come with foreground masks, which the
+    reference's mask term needs)."""
 
     def __init__(self, model, system_config=None, train_num_rays=256, max_train_num_rays=8192,
-                 train_num_samples=1 << 18, dynamic_ray_sampling=True):
+                 train_num_samples=1 << 18, dynamic_ray_sampling=True, has_mask=True):
         self.model = model
         sc = to_config(system_config or {})
         self.loss_cfg = to_config(sc.get("loss", {}))
+        self.has_mask = bool(has_mask)
+        self._check_loss(0)
         opt = to_config(sc.get("optimizer", {}))
         args = dict(opt.get("args", {"lr": 0.01, "betas": [0.9, 0.99], "eps": 1e-15}))
         groups = []
@@ -122,7 +160,15 @@ class NeuSTrainer:
     def C(self, v):
         return scheduled_value(v, self.global_step)
 
+    def _check_loss(self, step):
+        bad = unsupported_loss_terms(self.loss_cfg, step, self.has_mask)
+        if bad:
+            raise NotImplementedError(
+                "loss terms with a non-zero weight at step %d are not computed by this training "
+                "step: %s" % (step, "; ".join(f"{k} = {v}" for k, v in bad.items())))
+
     def step(self, rays, rgb, background_color):
+        self._check_loss(self.global_step)
         m = self.model
         m.update_step(0, self.global_step)
         m.background_color = background_color

@@ -467,3 +467,19 @@ extern "C" int angelo_march_compact(const float *scratch, int32_t per_ray, const
         t_ends, status);
     return check_launch("march_compact");
 }
+
+// Offsets of a fill into a fixed sample capacity, clamped to that capacity:
+// the fill drops every sample at or past `capacity`, so a consumer that walks
+// [offsets[r], offsets[r+1]) must not walk past it either.
+__global__ void offsets_clamp_kernel(int64_t *offsets, int64_t n, int64_t capacity) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && offsets[i] > capacity) offsets[i] = capacity;
+}
+
+extern "C" int angelo_offsets_clamp(int64_t *offsets, int64_t n_rays, int64_t capacity, void *stream) {
+    ANGELO_REQUIRE(n_rays >= 0 && capacity >= 0, "offsets_clamp: bad arguments");
+    ANGELO_REQUIRE(offsets != nullptr, "offsets_clamp: null offsets");
+    const int64_t n = n_rays + 1;
+    offsets_clamp_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(offsets, n, capacity);
+    return check_launch("offsets_clamp");
+}

@@ -19,9 +19,11 @@
 //     and may both return wrong offsets; order them on one stream;
 //   * the array keeps whatever the last call wrote; the kernels below write
 //     every slot they read before reading it, so nothing needs clearing;
-//   * the first call on each device looks up the array's device address
-//     (cudaGetSymbolAddress) with that device current; make that first call
-//     before capturing a stream into a CUDA graph.
+//   * every call made outside stream capture looks up the array's device
+//     address (cudaGetSymbolAddress) with the calling device current; a
+//     call under capture reuses the address of that device's last uncaptured
+//     call, so the first call on a device must come before any stream
+//     capture (a first call under capture is refused with ANGELO_E_INVALID).
 // Nothing here calls cudaMalloc, cudaFree or any allocating library routine.
 #include <mutex>
 
@@ -113,13 +115,26 @@ __global__ void __launch_bounds__(kThreadsNA) na_add(int64_t *__restrict__ out, 
         if (base + k < n) out[base + k] += add;
 }
 
-// Device address of the workspace for the current device, looked up once.
-int workspace_for_current_device(int64_t **ws) {
+// Device address of the workspace for the current device.  Looked up on
+// every call that is not being captured into a graph (a lookup is cheap, and
+// a context torn down and re-created, e.g. by cudaDeviceReset, may place the
+// array elsewhere); a call under stream capture uses the address of the
+// device's last uncaptured call, so the first call on a device must come
+// before any capture.
+int workspace_for_current_device(cudaStream_t s, int64_t **ws) {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return check_launch("scan_noalloc(cudaGetDevice)");
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess)
+        return check_launch("scan_noalloc(cudaStreamIsCapturing)");
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (g_ws_ptr[dev] == nullptr) {
+    if (cap != cudaStreamCaptureStatusNone && g_ws_ptr[dev] == nullptr) {
+        set_error("scan_noalloc: the first call on device %d is under stream capture; "
+                  "call it once outside capture first", dev);
+        return ANGELO_E_INVALID;
+    }
+    if (cap == cudaStreamCaptureStatusNone) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scan_ws);
         if (e != cudaSuccess || p == nullptr) {
@@ -150,7 +165,7 @@ extern "C" int angelo_scan_noalloc(const int32_t *counts, int64_t n, int64_t *of
     }
     ANGELO_REQUIRE(counts != nullptr, "scan_noalloc: null counts");
     int64_t *ws = nullptr;
-    if (int e = workspace_for_current_device(&ws)) return e;
+    if (int e = workspace_for_current_device(s, &ws)) return e;
     const int64_t tiles = (n + kTileNA - 1) / kTileNA;
     na_tiles<<<(unsigned)tiles, kThreadsNA, 0, s>>>(counts, n, offsets, ws);
     na_sums<<<1, kThreadsNA, 0, s>>>(ws, tiles, offsets + n);

@@ -181,7 +181,9 @@ def run(name, c, models):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <path of the Instant-angelo source tree>")
+    ref = sys.argv[1]
     models = H.install(ref)
     for name, c in CONFIGS.items():
         run(name, c, models)

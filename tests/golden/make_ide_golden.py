@@ -45,4 +45,6 @@ def main(reference_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_ide_golden.py <path of the Instant-angelo source tree>")
+    main(sys.argv[1])

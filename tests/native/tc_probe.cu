@@ -7,12 +7,33 @@
 // which a row-major [sample][unit] staging buffer is the transposed operand
 // of a GEMM over samples).  Used by the tests to pin the descriptor and
 // accumulator layouts the fused kernels rely on.
+//
+// Test-only: this file builds libangelo_tcprobe.so (tests/native/build.py),
+// not the product library; it reuses the product's tensor-core helpers
+// (tc.cuh) so that the layouts it pins are the ones the kernels use.
 #include <algorithm>
+#include <cstdarg>
 
 #include <cuda_bf16.h>
 
 #include "common.cuh"
 #include "tc.cuh"
+#include "tc_probe.h"
+
+// The probe library's own error message (common.cuh's status helpers write
+// it); read with angelo_probe_last_error_string().
+static thread_local char g_probe_err[512];
+
+namespace angelo {
+void set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_probe_err, sizeof(g_probe_err), fmt, ap);
+    va_end(ap);
+}
+}  // namespace angelo
+
+extern "C" const char *angelo_probe_last_error_string(void) { return g_probe_err; }
 
 using namespace angelo;
 

@@ -68,8 +68,19 @@ def test_overflowing_bucket_is_rendered_exactly(dev):
     q = RenderRequest(0, a.c2w, a.W, a.H)
     srv.run([q], realtime=False)
     assert srv.overflows > 0
+    # the bucket's own compositing walked only the samples the fill kept:
+    # its offsets end at the capacity and never pass it
+    off = srv.rb.offsets.cpu()
+    assert int(off[-1]) == srv.rb.cap and bool((off[1:] >= off[:-1]).all())
     full, op, dep = render_exact(m, request_rays(q, 0, q.n, dev), srv.bg)
     assert torch.equal(q.rgb, full)
+
+
+def test_offsets_clamp(dev):
+    from angelo_gb import _lib, ops
+    off = torch.tensor([0, 5, 9, 20, 31, 40], device=dev, dtype=torch.int64)
+    _lib.call("angelo_offsets_clamp", ops._p(off), off.numel() - 1, 19, ops._s(dev))
+    assert off.cpu().tolist() == [0, 5, 9, 19, 19, 19]
 
 
 def test_sdf_grid_matches_forward_level(dev):

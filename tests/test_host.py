@@ -128,3 +128,16 @@ def test_sdf_net_layout_query_and_struct(lib):
     assert lib.angelo_sdf_net_layout_query(16, 3, 65, ctypes.byref(L)) != 0
     assert _lib.SdfNetLayout.mma_passes.offset == 5 * 4 + 4 + 8 * 8
     assert ctypes.sizeof(_lib.SdfNetLayout) == 5 * 4 + 4 + 8 * 8 + 8
+
+
+def test_probe_library_is_separate_and_complete(lib):
+    """The tensor-core probes live in the test-only library
+    (tests/native/tc_probe.h), not in the product library."""
+    from native import build as probe
+    txt = open(os.path.join(ROOT, "tests", "native", "tc_probe.h")).read()
+    declared = sorted(set(re.findall(r"\b(angelo_[a-z0-9_]+)\s*\(", txt)))
+    assert declared == sorted(probe.SIGNATURES)
+    P = probe.load()
+    for s in declared:
+        assert hasattr(P, s), s
+        assert not hasattr(lib, s), s
