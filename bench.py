@@ -19,9 +19,10 @@ library's encode / march / composite kernels) and, when built, "fused"; and
 "fused_bg", the fused step with the sparse configs' learned NeRF++ background
 added (a wider workload than the headline, reported under "forms").
 
---impl reference times the oracle's CPU restatement of the same step on the
-host cores (the reference itself is Python over tcnn/nerfacc CUDA kernels,
-none of which exists here).
+--impl reference times the oracle's vectorised CPU restatement of the same
+step (oracle/cpu_step.py) on the host cores, in 1024-ray sub-batches (the
+reference itself is Python over tcnn/nerfacc CUDA kernels, none of which
+exists here or has a CPU implementation).
 """
 from __future__ import annotations
 
@@ -169,6 +170,8 @@ def make_views(dev):
 
 
 MAX_RAYS = 8192   # the full workload's ray budget (--max-rays shrinks it for kernel captures)
+VALUE_PASSES = 3  # timed passes per form for `value` (the median is reported)
+E2E_PASSES = 3    # timed passes per form for `e2e` (the median is reported)
 
 
 def make_trainer(form, dev, seed=0):
@@ -382,65 +385,66 @@ def roofline(summary, hbm_peak, peak_kind):
 # -------------------------------------------------------------- CPU baseline
 
 
-def cpu_step(model, views_cpu, n_rays, seed):
-    """One training forward + backward of the same step, in the oracle's
-    float32 CPU restatement (oracle/neus_fp64.py), on n_rays rays."""
-    from oracle import cref
-    from oracle import neus_fp64 as O
-    g = np.random.default_rng(seed)
-    images, c2w, dirs, Wd, Hd = views_cpu
-    from angelo_gb.scenes import rays_from
-    idx = torch.from_numpy(g.integers(0, images.shape[0], n_rays))
-    pix = torch.from_numpy(g.integers(0, Wd * Hd, n_rays))
-    rays = rays_from(dirs[pix], c2w[idx]).float()
-    rgb = images[idx, pix].float()
-    cfg = model.config
-    h = cfg.geometry.xyz_encoding_config
-    lay = O.HashGridLayout(h.n_levels, h.n_features_per_level, h.log2_hashmap_size,
-                           h.base_resolution, h.per_level_scale)
-    G = dict(radius=cfg.radius, eps=model.geometry._finite_difference_eps, lay=lay,
-             active_levels=model.geometry.encoding.encoding.mask_levels,
-             n_layers=cfg.geometry.mlp_network_config.n_hidden_layers + 1,
-             feature_dim=cfg.geometry.feature_dim, hg=h)
-    T = dict(kind="dual" if cfg.texture.name == "volume-dual-color" else "radiance",
-             n_layers=cfg.texture.mlp_network_config.n_hidden_layers + 1)
-    P = {k: v.detach().cpu().float().clone().requires_grad_(v.dtype.is_floating_point)
-         for k, v in model.state_dict().items() if not k.startswith("occupancy_grid")}
-    grid = model.occupancy_grid
-    binary = grid.binary.cpu().numpy().astype(np.uint8)
-    aabb = model.scene_aabb.cpu().numpy()
-    t0c = time.perf_counter()
-    tmin, tmax = cref.ray_aabb(rays[:, :3].numpy(), rays[:, 3:].numpy(), aabb)
-    tmin = (tmin + g.random(n_rays, dtype=np.float32) * np.float32(model.render_step_size))
-    _, off, ri, t0, t1, _ = cref.march(rays[:, :3].numpy(), rays[:, 3:].numpy(),
-                                       tmin.astype(np.float32), tmax, aabb, binary,
-                                       model.render_step_size)
-    rd = torch.randn(len(t0), 3)
-    out = O.neus_render(rays, P, G, T, (off, ri, t0, t1), rd, model.cos_anneal_ratio,
-                        torch.rand(3))
-    loss = O.neus_losses(out, rgb)
-    loss.backward()
-    return time.perf_counter() - t0c, len(t0)
+class CpuStep:
+    """The same training step on the host cores: oracle/cpu_step.py (the
+    reference's step restated in vectorised float32 torch: C restatement of
+    nerfacc's march, reference initialisation, AdamW), on rays drawn like the
+    GPU workload's (8 poses on the radius-1.5 sphere, 1600x1200 pixels),
+    targets rendered from the analytic scene outside the timed part.  Touches
+    neither CUDA nor libangelo_gb.so."""
+
+    def __init__(self, seed=0):
+        from angelo_gb import scenes, workloads
+        from oracle import cpu_step
+        torch.set_num_threads(os.cpu_count() or 1)
+        self.scene = scenes.UnionScene()
+        occ = scenes.analytic_occupancy(self.scene, 128, device="cpu").reshape(-1)
+        self.step_fn = cpu_step.TrainStep(workloads.model_config("full"), workloads.SYSTEM,
+                                          GLOBAL_STEP, INV_S_VARIANCE, occ, seed=seed)
+        self.poses = scenes.sphere_poses(N_VIEWS, CAM_R, 0).float()
+        self.dirs = scenes.pixel_directions(W, H, FOV).reshape(-1, 3)
+        self.rng = np.random.default_rng(seed + 7)
+
+    def batch(self, n):
+        from angelo_gb import scenes
+        pix = torch.from_numpy(self.rng.integers(0, W * H, n))
+        cam = torch.from_numpy(self.rng.integers(0, N_VIEWS, n))
+        rays = scenes.rays_from(self.dirs[pix], self.poses[cam]).float().contiguous()
+        rgb = scenes.render_analytic(self.scene, rays).float()
+        return rays, rgb
+
+    def step(self, n):
+        rays, rgb = self.batch(n)
+        return self.step_fn.step(rays, rgb)
 
 
-def cpu_baseline(model, views, budget_s=15.0):
-    views_cpu = (views.images.cpu(), views.c2w.cpu(), views.dirs.cpu(), views.W, views.H)
-    torch.set_num_threads(os.cpu_count() or 1)
-    dt, _ = cpu_step(model, views_cpu, 16, 123)
-    per_ray = dt / 16
-    n = int(max(16, min(2048, (budget_s / 3) / max(per_ray, 1e-6))))
+CPU_SUB_BATCH = 1024   # rays per CPU step: the 1024-ray sub-batches of the full step
+
+
+def cpu_sub_batch(cs, budget_s):
+    """The sub-batch size: 1024 rays, or fewer when one step of 1024 would
+    exceed budget_s (estimated from a 128-ray step)."""
+    dt, _ = cs.step(128)
+    est = dt * CPU_SUB_BATCH / 128
+    if est <= budget_s:
+        return CPU_SUB_BATCH
+    return int(max(64, CPU_SUB_BATCH * budget_s / est))
+
+
+def cpu_baseline(steps=3, budget_s=8.0):
+    cs = CpuStep(seed=11)
+    n = cpu_sub_batch(cs, budget_s)
     tot_t, tot_r, tot_s = 0.0, 0, 0
-    k = 0
-    while tot_t < budget_s * 0.6 and k < 3:
-        dt, s = cpu_step(model, views_cpu, n, 200 + k)
+    for k in range(steps):
+        dt, s = cs.step(n)
         tot_t += dt
         tot_r += n
         tot_s += s
-        k += 1
     return {"value": round(tot_r / tot_t, 2), "unit": "rays/s", "cores": torch.get_num_threads(),
             "kind": "port",
-            "sample": f"{k} step(s) of {n} rays ({tot_s} samples) of the same workload, "
-                      "forward+backward in the oracle's float32 CPU restatement"}
+            "sample": f"{steps} step(s) of {n} rays ({tot_s} samples) of the same workload "
+                      "(forward, backward, AdamW), in the oracle's vectorised float32 CPU "
+                      "restatement (oracle/cpu_step.py), after one 128-ray warm-up step"}
 
 
 # ---------------------------------------------------------------------- arms
@@ -490,17 +494,28 @@ def run_ours(args):
             gen.manual_seed(1234 + rank)   # the same ray batches as the first pass
 
         gen = torch.Generator(device=dev).manual_seed(1234 + rank)
+        # `value` is the median of VALUE_PASSES passes, each from the same
+        # state with the same ray batches (so the same samples), each after
+        # its own W warm-up steps: a pass that meets a one-off cost (a first
+        # kernel load, an allocator growth, a clock ramp) does not set it
+        runs = []
         with Clocks(local) as clk:
-            for _ in range(args.warmup):
-                step_device(tr, views, gen)
-            # profiler range (cudaProfilerStart/Stop) marks the timed steps
-            # for a capture started with --profile-from-start off; the
-            # backward kernels launch from autograd's own thread, which an
-            # NVTX range of this thread would not cover
-            torch.cuda.profiler.start()
-            ms, acc = timed(lambda: step_device(tr, views, gen), args.steps, dev, world, clk)
-            torch.cuda.profiler.stop()
+            for p in range(VALUE_PASSES):
+                reset()
+                for _ in range(args.warmup):
+                    step_device(tr, views, gen)
+                # profiler range (cudaProfilerStart/Stop) marks the timed
+                # steps for a capture started with --profile-from-start off;
+                # the backward kernels launch from autograd's own thread,
+                # which an NVTX range of this thread would not cover
+                torch.cuda.profiler.start()
+                runs.append(timed(lambda: step_device(tr, views, gen), args.steps, dev, world,
+                                  clk if p == 0 else None))
+                torch.cuda.profiler.stop()
+            clk.mark(1)
         torch.cuda.synchronize(dev)
+        pass_ms = [r[0] for r in runs]
+        ms, acc = sorted(runs, key=lambda r: r[0])[len(runs) // 2]
         # per-call CUDA events (roofline, kernel shares, launch count) over a
         # second timed pass of as many steps: recording them costs host time,
         # so they stay out of the pass that gives `value`
@@ -516,21 +531,28 @@ def run_ours(args):
         rays = sum(a[0] for a in acc)
         samples = sum(a[1] for a in acc)
         rl, shares = roofline(summ, hbm_peak, peak_kind)
-        # host-fed end-to-end through the public API
-        feed = HostFeed(views, seed=77 + rank)
-        reset()
-        for _ in range(args.warmup):
-            step_host(tr, feed, dev)
-        feed.read_result()
-        ms_e2e, acc_e = timed(lambda: step_host(tr, feed, dev), args.steps, dev, world)
-        feed.read_result()
-        assert len(feed.losses) >= args.steps and all(np.isfinite(feed.losses[-args.steps:]))
+        # host-fed end-to-end through the public API; median of E2E_PASSES
+        # passes, each from the same state with the same host batches
+        runs_e = []
+        for p in range(E2E_PASSES):
+            feed = HostFeed(views, seed=77 + rank)
+            reset()
+            for _ in range(args.warmup):
+                step_host(tr, feed, dev)
+            feed.read_result()
+            runs_e.append(timed(lambda: step_host(tr, feed, dev), args.steps, dev, world))
+            feed.read_result()
+            assert len(feed.losses) >= args.steps and all(np.isfinite(feed.losses[-args.steps:]))
+        pass_ms_e2e = [r[0] for r in runs_e]
+        ms_e2e, acc_e = sorted(runs_e, key=lambda r: r[0])[len(runs_e) // 2]
         rays_e = sum(a[0] for a in acc_e)
         samples_e = sum(a[1] for a in acc_e)
         rays, rays_e, samples = sum_over_ranks([rays, rays_e, samples], dev, world)
         results[form] = dict(
             value=rays / (ms * 1e-3), ms_per_step=ms / args.steps, rays_per_step=rays / args.steps
             / world, samples_per_step=samples / args.steps / world, roofline=rl,
+            pass_ms_per_step=[round(t / args.steps, 3) for t in pass_ms],
+            e2e_pass_ms_per_step=[round(t / args.steps, 3) for t in pass_ms_e2e],
             kernel_ms=shares, gpu_launches=launches, clocks=clk.summary(),
             e2e=dict(value=round(rays_e / (ms_e2e * 1e-3), 1), unit="rays/s",
                      h2d_bytes_per_step=int(np.mean([a[2] for a in acc_e])),
@@ -545,13 +567,18 @@ def run_ours(args):
         "metric": "train rays/s", "value": round(R["value"], 1), "unit": "rays/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(R["ms_per_step"], 3), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic: 8 seeded 1600x1200 views of an "
+        "vs_baseline": None, "dtype": "f32/bf16x3" if head != "plain" else "f32",
+        "data": "synthetic: 8 seeded 1600x1200 views of an "
         "analytic torus/box/sphere union, Gaussian noise 0.01",
         "config": {"workload": "neuralangelo-sparse-train (16 lv x 2^22, 128^3 grid, 2^18 "
                    "samples/step target, FD + curvature)", "form": head,
                    "rays_per_step": round(R["rays_per_step"], 1),
                    "samples_per_step": round(R["samples_per_step"], 1),
                    "global_step": GLOBAL_STEP, "parallelism": f"replicas x{world}",
+                   "precision": "hash table, encodings, alpha, transmittance, loss and AdamW in "
+                   "fp32; the geometry and radiance MLPs on tcgen05 with every operand split into "
+                   "a bf16 hi + lo pair (three products, ~16 significant bits per operand) and "
+                   "fp32 accumulation in tensor memory" if head != "plain" else "fp32",
                    "l2": "inputs larger than L2 (hash table 0.37 GB + AdamW state 0.73 GB)",
                    "per_call_events": "roofline, kernel_ms and gpu_launches from a second "
                    "timed pass of the same number of steps",
@@ -567,18 +594,26 @@ def run_ours(args):
         "gpu_launches": R["gpu_launches"], "kernel_ms": R["kernel_ms"],
         "forms": {f: {"value": round(v["value"], 1), "ms_per_step": round(v["ms_per_step"], 3),
                       "samples_per_step": round(v["samples_per_step"], 1),
-                      "e2e": v["e2e"]["value"]} for f, v in results.items()},
+                      "ns_per_sample": round(v["ms_per_step"] * 1e6 / max(v["samples_per_step"], 1.0), 3),
+                      "pass_ms_per_step": v["pass_ms_per_step"],
+                      "e2e": v["e2e"]["value"], "e2e_ms_per_step": v["e2e"]["ms_per_step"],
+                      "e2e_samples_per_step": v["e2e"]["samples_per_step"],
+                      "e2e_pass_ms_per_step": v["e2e_pass_ms_per_step"]}
+                  for f, v in results.items()},
     }
     if "fused" in results and "plain" in results:
         line["fused_vs_plain"] = round(results["fused"]["value"] / results["plain"]["value"], 3)
+        ns = {f: results[f]["ms_per_step"] / max(results[f]["samples_per_step"], 1.0)
+              for f in ("fused", "plain")}
+        line["fused_vs_plain_per_sample"] = round(ns["plain"] / ns["fused"], 3)
+        line["fused_vs_plain_e2e"] = round(results["fused"]["e2e"]["value"] /
+                                           results["plain"]["e2e"]["value"], 3)
     if rank == 0 and not args.no_serving and "fused" in forms:
         line["serving"] = run_serving(dev, seed=1000 + rank)
     if rank == 0 and not args.no_mesh:
         line["mesh"] = run_mesh(dev, hbm_peak)
     if rank == 0 and not args.no_cpu_baseline:
-        model, tr = make_trainer("plain", dev)
-        model.update_step(0, GLOBAL_STEP)
-        line["cpu_baseline"] = cpu_baseline(model, views)
+        line["cpu_baseline"] = cpu_baseline()
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -772,30 +807,25 @@ def run_mesh(dev, hbm_peak, res=MESH_RES):
 
 
 def run_reference(args):
-    """The reference arm: the oracle's CPU restatement of the same training
-    step (forward + backward) on the host cores, bounded samples per step."""
+    """The reference arm: the reference's training step restated on the host
+    cores (oracle/cpu_step.py: vectorised float32 torch over the C
+    restatement of nerfacc's march), one 1024-ray sub-batch per step (fewer
+    only if a step would take longer than a few seconds), W untimed and K
+    timed steps.  The reference itself is Python over tcnn / nerfacc CUDA
+    kernels that have no CPU implementation, and its source tree is not
+    present where the benchmark runs.  No GPU work: neither CUDA nor
+    libangelo_gb.so is touched."""
     rank, world, local = dist_env()
     if rank != 0:
         return
-    dev = torch.device("cuda:0") if torch.cuda.is_available() else None
-    if dev is None:
-        print(json.dumps({"impl": "reference", "unavailable": "needs a GPU to build the views"}))
-        return
-    from angelo_gb import build
-    build.build()
-    views = make_views(dev)
-    model, tr = make_trainer("plain", dev)
-    model.update_step(0, GLOBAL_STEP)
-    views_cpu = (views.images.cpu(), views.c2w.cpu(), views.dirs.cpu(), views.W, views.H)
-    torch.set_num_threads(os.cpu_count() or 1)
-    dt, _ = cpu_step(model, views_cpu, 16, 5)
-    budget = 120.0 / max(1, args.steps + args.warmup)
-    n = int(max(16, min(2048, budget / max(dt / 16, 1e-6))))
-    for k in range(min(args.warmup, 1)):
-        cpu_step(model, views_cpu, n, 10 + k)
+    budget = max(2.0, min(8.0, 150.0 / max(1, args.steps + args.warmup)))
+    cs = CpuStep(seed=0)
+    n = cpu_sub_batch(cs, budget)
+    for _ in range(args.warmup):
+        cs.step(n)
     t_tot, r_tot, s_tot = 0.0, 0, 0
-    for k in range(args.steps):
-        dt, s = cpu_step(model, views_cpu, n, 100 + k)
+    for _ in range(args.steps):
+        dt, s = cs.step(n)
         t_tot += dt
         r_tot += n
         s_tot += s
@@ -806,10 +836,13 @@ def run_reference(args):
         "ms_per_step": round(1e3 * t_tot / args.steps, 2), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "neuralangelo-sparse-train (16 lv x 2^22, 128^3 grid, 2^18 "
-                   "samples/step target, FD + curvature)", "rays_per_step": n},
+                   "samples/step target, FD + curvature)", "rays_per_step": n,
+                   "samples_per_step": round(s_tot / args.steps, 1), "global_step": GLOBAL_STEP},
+        "samples_per_s": round(s_tot / t_tot, 1),
         "cpu_baseline": {"value": round(v, 2), "unit": "rays/s", "cores": torch.get_num_threads(),
                          "kind": "port", "sample": f"{args.steps} steps of {n} rays "
-                         f"({s_tot} samples) in the oracle's float32 CPU restatement"},
+                         f"({s_tot} samples), forward + backward + AdamW, in the oracle's "
+                         "vectorised float32 CPU restatement (oracle/cpu_step.py)"},
         "e2e": {"value": round(v, 2), "unit": "rays/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0}}), flush=True)
 

@@ -261,8 +261,12 @@ int angelo_accumulate_bwd(const float *weights, const float *values, int32_t cha
 
 /* ------------------------------------------------------------ fused VolumeSDF */
 
+#define ANGELO_OPERAND_BF16 0
+#define ANGELO_OPERAND_FP16 1
+
 /* Prepared geometry-MLP operands: fp32 biases and output row 0, and the
- * three layers as bf16 hi/lo tensor-core operands.  Layout by query. */
+ * three layers as bf16 (or fp16) hi/lo tensor-core operands.  Layout by
+ * query. */
 typedef struct {
     int32_t k_tiles1, n_hidden, n_tiles3, k_tiles3b, out_dim;
     int64_t off_b1, off_b2, off_b3, off_w3row0;
@@ -272,9 +276,15 @@ typedef struct {
     int64_t bytes;
     /* tensor-core products per layer in the forward kernels: 3 (bf16x3, the
      * default the query sets: hi*hi + lo*hi + hi*lo, ~16 mantissa bits per
-     * operand) or 1 (a single bf16 pass, the precision form); the backward
+     * operand) or 1 (the hi parts alone, a single pass); the backward
      * recompute is always bf16x3 */
     int32_t mma_passes;
+    /* number format of the prepared weights and of the forward kernels'
+     * staged activations: ANGELO_OPERAND_BF16 (the default the query sets) or
+     * ANGELO_OPERAND_FP16 (11 significant bits: with one pass, the precision
+     * form).  Set it before angelo_sdf_prep; the backward accepts only a
+     * bf16-prepared buffer. */
+    int32_t operand_format;
 } angelo_sdf_net_layout;
 
 int angelo_sdf_net_layout_query(int32_t n_levels, int32_t n_hidden, int32_t out_dim,
@@ -412,15 +422,22 @@ int64_t angelo_radiance_net_bytes(int32_t feat_dim);
  * dW3 (16 x 64), db1 (64), db2 (64), db3 (16)]. */
 int64_t angelo_radiance_grad_size(int32_t feat_dim);
 /* Effective fp32 weights of VanillaMLP(in, 3, 2 hidden ReLU layers of 64)
- * (models/texture.py:19,47) -> prepared buffer. */
+ * (models/texture.py:19,47) -> prepared buffer (bf16 hi/lo operands). */
 int angelo_radiance_prep(int32_t feat_dim, const float *W1, const float *b1, const float *W2,
                          const float *b2, const float *W3, const float *b3, void *net,
                          void *stream);
+/* The same with the operands in ANGELO_OPERAND_BF16 or ANGELO_OPERAND_FP16
+ * parts; an fp16 buffer serves angelo_radiance_fwd with flags bit 2 only
+ * (the backward reads bf16 operands). */
+int angelo_radiance_prep_format(int32_t feat_dim, int32_t operand_format, const float *W1,
+                                const float *b1, const float *W2, const float *b2,
+                                const float *W3, const float *b3, void *net, void *stream);
 /* VolumeRadiance / VolumeDualColor forward (models/texture.py:23-30,50-58):
  * rgb = sigmoid(MLP([feature, SH4((d+1)/2), normalize(grad)])) (+ sigmoid of
  * feature[1:4] when dual), d = rays_d[ray_idx].  flags bit 0: dual colour;
- * bit 1: the MLP in a single bf16 pass (the precision form) instead of
- * bf16x3. */
+ * bit 1: the MLP in a single pass (hi parts alone) instead of three
+ * products; bit 2: fp16 operands (a buffer from angelo_radiance_prep_format
+ * with ANGELO_OPERAND_FP16) instead of bf16. */
 int angelo_radiance_fwd(int32_t feat_dim, const void *net, const float *feature,
                         int64_t feat_stride, const float *grad, const int32_t *ray_idx,
                         const float *rays_d, int64_t n, int32_t flags, float *rgb, void *stream);

@@ -19,6 +19,8 @@ ANGELO_E_CAPACITY = 4
 MAX_LEVELS = 32
 DTYPE_F32 = 0
 DTYPE_F16 = 1
+OPERAND_BF16 = 0
+OPERAND_FP16 = 1
 
 c_i32, c_i64, c_f32, c_vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_void_p
 
@@ -47,7 +49,8 @@ class SdfNetLayout(ctypes.Structure):
                 ("k_tiles3b", c_i32), ("out_dim", c_i32),
                 ("off_b1", c_i64), ("off_b2", c_i64), ("off_b3", c_i64),
                 ("off_w3row0", c_i64), ("off_tcw1", c_i64), ("off_tcw2", c_i64),
-                ("off_tcw3", c_i64), ("bytes", c_i64), ("mma_passes", c_i32)]
+                ("off_tcw3", c_i64), ("bytes", c_i64), ("mma_passes", c_i32),
+                ("operand_format", c_i32)]
 
 
 class AngeloError(RuntimeError):
@@ -121,6 +124,8 @@ SIGNATURES = {
     "angelo_radiance_net_bytes": (c_i64, [c_i32]),
     "angelo_radiance_grad_size": (c_i64, [c_i32]),
     "angelo_radiance_prep": (c_i32, [c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_radiance_prep_format": (c_i32, [c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                            c_vp]),
     "angelo_radiance_fwd": (c_i32, [c_i32, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i64, c_i32, c_vp,
                                     c_vp]),
     "angelo_radiance_bwd": (c_i32, [c_i32, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i64, c_i32, c_vp,

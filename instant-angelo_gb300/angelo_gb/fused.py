@@ -34,9 +34,10 @@ class SdfNet:
     """Prepared tensor-core operands of the geometry MLP (bf16 hi/lo fragments
     of every layer in forward and backward order, fp32 biases)."""
 
-    def __init__(self, n_levels, n_hidden, out_dim, device):
+    def __init__(self, n_levels, n_hidden, out_dim, device, operand_format=_lib.OPERAND_BF16):
         self.layout = SdfNetLayout()
         call("angelo_sdf_net_layout_query", n_levels, n_hidden, out_dim, ctypes.byref(self.layout))
+        self.layout.operand_format = int(operand_format)
         self.n_levels, self.n_hidden, self.out_dim = n_levels, n_hidden, out_dim
         self.buf = torch.empty(self.layout.bytes, dtype=torch.uint8, device=device)
         self.grad_size = _lib.raw("angelo_sdf_grad_size")(ctypes.byref(self.layout))
@@ -92,7 +93,13 @@ class _FusedSdf(torch.autograd.Function):
         geom, net, flags = meta["geom"], meta["net"], meta["flags"]
         with_grad, with_laplace, with_feature = flags
         Ws = [(weights[2 * i], weights[2 * i + 1]) for i in range(len(weights) // 2)]
-        net.prepare(Ws)
+        training = any(ctx.needs_input_grad[2:])
+        # the forward's operands (fp16 in the fp16 precision form); the
+        # backward always reads the bf16 buffer
+        fnet = meta.get("net_fwd", net)
+        fnet.prepare(Ws)
+        if training and fnet is not net:
+            net.prepare(Ws)
         spec = geom.hashgrid.encoding.spec
         active = geom.hashgrid.mask_levels
         S = pos.shape[0]
@@ -102,12 +109,11 @@ class _FusedSdf(torch.autograd.Function):
         grad = torch.empty(S, 3, device=dev) if with_grad else None
         feature = torch.empty(S, od + 3, device=dev) if with_feature else None
         lap = torch.empty(S, 1, device=dev) if with_laplace else None
-        training = any(ctx.needs_input_grad[2:])
         work = torch.empty(workspace_floats(spec, S, with_grad, with_laplace, False), device=dev)
         rd = rand_dirs.contiguous() if rand_dirs is not None else None
         n_ev = 13 if with_laplace else (7 if with_grad else 1)
         call("angelo_sdf_stencil_fwd", ctypes.byref(spec.layout), int(active), _p(table),
-             _table_dtype(table), ctypes.byref(net.layout), _p(net.buf), _p(pos), _p(rd), S,
+             _table_dtype(table), ctypes.byref(fnet.layout), _p(fnet.buf), _p(pos), _p(rd), S,
              float(geom.radius), float(geom._finite_difference_eps or 1.0), int(with_grad),
              int(with_laplace), int(with_feature), _p(sdf), _p(grad), _p(feature),
              od + 3, _p(lap), _p(work), _s(dev),
@@ -209,13 +215,28 @@ def effective_weights(mlp):
     return [(next(ws) if isinstance(m, WNLinear) else m.weight, m.bias) for m in lins]
 
 
-def _net_for(geom):
-    net = getattr(geom, "_fused_net", None)
+# fused_precision of the drop-in config: "fp32" (the default: bf16x3 operands,
+# fp32 accumulation), "bf16" (one bf16 pass per forward layer) or "fp16"
+# (one fp16 pass per forward layer: the precision form); the backward is
+# bf16x3 in every form
+PRECISIONS = ("fp32", "bf16", "fp16")
+
+
+def _precision(mod):
+    p = getattr(mod, "fused_precision", "fp32")
+    if p not in PRECISIONS:
+        raise ValueError(f"fused_precision {p!r}: one of {PRECISIONS}")
+    return p
+
+
+def _net_for(geom, operand_format=_lib.OPERAND_BF16):
+    attr = "_fused_net" if operand_format == _lib.OPERAND_BF16 else "_fused_net_fp16"
+    net = getattr(geom, attr, None)
     mlp = geom.network
     if net is None or net.buf.device != geom.hashgrid.encoding.params.device:
         net = SdfNet(geom.hashgrid.n_level, mlp.n_hidden_layers, geom.n_output_dims,
-                     geom.hashgrid.encoding.params.device)
-        geom._fused_net = net
+                     geom.hashgrid.encoding.params.device, operand_format)
+        setattr(geom, attr, net)
     return net
 
 
@@ -233,9 +254,14 @@ def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
     for W, b in effective_weights(geom.network):
         weights += [W, b]
     table = geom.hashgrid.encoding.params
-    net.layout.mma_passes = 1 if getattr(geom, "fused_precision", "fp32") == "bf16" else 3
+    prec = _precision(geom)
+    net.layout.mma_passes = 1 if prec == "bf16" else 3
     meta = dict(geom=geom, net=net, flags=(bool(with_grad), bool(with_laplace),
                                            bool(with_feature)))
+    if prec == "fp16":
+        fnet = _net_for(geom, _lib.OPERAND_FP16)
+        fnet.layout.mma_passes = 1
+        meta["net_fwd"] = fnet
     with torch.set_grad_enabled(geom.training and torch.is_grad_enabled()):
         sdf, grad, feature, lap = _FusedSdf.apply(pos, rd, table, meta, *weights)
     shp = points.shape[:-1]
@@ -261,8 +287,9 @@ class RadNet:
     """Prepared tensor-core operands of a 2-hidden-layer ReLU radiance MLP
     (VolumeRadiance / VolumeDualColor, models/texture.py:10-64)."""
 
-    def __init__(self, feat_dim, device):
+    def __init__(self, feat_dim, device, operand_format=_lib.OPERAND_BF16):
         self.feat_dim = int(feat_dim)
+        self.operand_format = int(operand_format)
         nbytes = _lib.raw("angelo_radiance_net_bytes")(self.feat_dim)
         if nbytes < 0:
             raise ValueError(f"radiance feature width {feat_dim} not supported by the fused kernel")
@@ -273,8 +300,8 @@ class RadNet:
 
     def prepare(self, Ws):
         ts = [t.detach().float().contiguous() for W, b in Ws for t in (W, b)]
-        call("angelo_radiance_prep", self.feat_dim, *[_p(t) for t in ts], _p(self.buf),
-             _s(self.buf.device))
+        call("angelo_radiance_prep_format", self.feat_dim, self.operand_format,
+             *[_p(t) for t in ts], _p(self.buf), _s(self.buf.device))
 
     def unpack_grads(self, g):
         k1 = self.k1cols
@@ -292,13 +319,18 @@ class _FusedRadiance(torch.autograd.Function):
     @staticmethod
     def forward(ctx, feature, grad, ray_idx, rays_d, meta, *weights):
         net, dual = meta["net"], meta["dual"]
-        net.prepare([(weights[2 * i], weights[2 * i + 1]) for i in range(3)])
+        Ws = [(weights[2 * i], weights[2 * i + 1]) for i in range(3)]
+        fnet = meta.get("net_fwd", net)
+        fnet.prepare(Ws)
+        if fnet is not net and any(ctx.needs_input_grad):
+            net.prepare(Ws)
         feature = feature.contiguous()
         grad = grad.contiguous()
         S = feature.shape[0]
         rgb = torch.empty(S, 3, device=feature.device)
-        flags = int(dual) | (2 if meta.get("one_pass") else 0)
-        call("angelo_radiance_fwd", net.feat_dim, _p(net.buf), _p(feature), feature.stride(0),
+        flags = int(dual) | (2 if meta.get("one_pass") else 0) | \
+            (4 if fnet.operand_format == _lib.OPERAND_FP16 else 0)
+        call("angelo_radiance_fwd", net.feat_dim, _p(fnet.buf), _p(feature), feature.stride(0),
              _p(grad), _p(ray_idx), _p(rays_d), S, flags, _p(rgb), _s(feature.device),
              units=dict(n=S, F=net.feat_dim, bwd=False))
         ctx.save_for_backward(feature, grad, ray_idx, rays_d)
@@ -333,8 +365,14 @@ def radiance_forward(texture, feature, grad, ray_idx, rays_d):
     weights = []
     for W, b in texture.network.effective_weights():
         weights += [W, b]
-    meta = dict(net=net, dual=bool(getattr(texture, "dual", False)),
-                one_pass=getattr(texture, "fused_precision", "fp32") == "bf16")
+    prec = _precision(texture)
+    meta = dict(net=net, dual=bool(getattr(texture, "dual", False)), one_pass=prec in ("bf16", "fp16"))
+    if prec == "fp16":
+        fnet = getattr(texture, "_fused_net_fp16", None)
+        if fnet is None or fnet.feat_dim != F_ or fnet.buf.device != feature.device:
+            fnet = RadNet(F_, feature.device, _lib.OPERAND_FP16)
+            texture._fused_net_fp16 = fnet
+        meta["net_fwd"] = fnet
     return _FusedRadiance.apply(feature, grad, ray_idx, rays_d, meta, *weights)
 
 

@@ -11,6 +11,15 @@ from .config import scheduled_value, to_config
 from .optim import AdamW
 
 
+def psnr(inputs, targets, valid_mask=None):
+    """PSNR of systems/criterions.py:40-53 (reduction 'mean'):
+    -10 log10(mean((inputs - targets)^2)) over the valid entries."""
+    value = (inputs - targets) ** 2
+    if valid_mask is not None:
+        value = value[valid_mask]
+    return -10.0 * torch.log10(torch.mean(value))
+
+
 def loss_terms(out, rgb, eikonal_weight=0.1, curvature_weight=5e-4, rgb_mse_weight=10.0):
     """Weighted loss terms of systems/neus.py:130-159 (the ones the hot path
     seeds).  Returns (total, dict of unweighted terms)."""

@@ -67,7 +67,7 @@ __device__ __forceinline__ float rad_w(int layer, int n, int k, const float *W1,
 }
 
 __global__ void rad_prep_kernel(const float *W1, const float *b1, const float *W2, const float *b2,
-                                const float *W3, const float *b3, RadLayout L, char *net) {
+                                const float *W3, const float *b3, RadLayout L, int fp16, char *net) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int K1 = 16 * L.k_tiles1;
     const int n1 = 64 * K1, n2 = 64 * 64, n3 = 16 * 64;
@@ -91,7 +91,8 @@ __global__ void rad_prep_kernel(const float *W1, const float *b1, const float *W
         else if (i < 144 + 192) fw3[i - 144] = W3[i - 144];
         return;
     }
-    const Split sp = split2(rad_w(layer, n, k, W1, W2, W3, L.in_dim), 0.0f);
+    const float w = rad_w(layer, n, k, W1, W2, W3, L.in_dim);
+    const Split sp = fp16 ? split2h(w, 0.0f) : split2(w, 0.0f);
     const uint32_t o = tc::kmajor_offset(n, k, K);
     *reinterpret_cast<uint16_t *>(net + off + o) = (uint16_t)(sp.hi & 0xFFFFu);
     *reinterpret_cast<uint16_t *>(net + off + half + o) = (uint16_t)(sp.lo & 0xFFFFu);
@@ -109,7 +110,8 @@ struct RadParams {
     const float *rays_d;
     int64_t S;
     int dual;
-    int passes;   // forward tensor-core products per layer: 3 (bf16x3) or 1 (one bf16 pass)
+    int passes;   // forward tensor-core products per layer: 3 (hi/lo x3) or 1 (hi parts alone)
+    int fp16;     // forward operands fp16 (the buffer prepared in fp16) instead of bf16
     float *rgb;
     const float *g_rgb;
     float *d_feature;
@@ -137,9 +139,9 @@ __device__ __forceinline__ void rad_sh_normal(const RadParams &P, int64_t s, flo
 
 // The input row [feature (F), SH (16), normal (3), 0 ...] of sample s, the
 // 16-column blocks slice, slice + 4, ... of it staged K-major (16 KT1 columns)
-template <int KT1>
+template <int KT1, bool FP16 = false>
 __device__ __forceinline__ void rad_stage_x(const RadParams &P, int64_t s, bool v, int row, int slice, char *xh,
-                                            char *xl) {
+                                            char *xl, bool with_lo = true) {
     const int F = P.L.feat_dim;
     for (int b = slice; b < KT1; b += 4) {
         const int c0 = 16 * b;
@@ -156,7 +158,7 @@ __device__ __forceinline__ void rad_stage_x(const RadParams &P, int64_t s, bool 
                 else if (c >= 16 && c < 19) x[j] = nrm[c - 16];
             }
         }
-        stage16(xh, xl, row, c0, 16 * KT1, x);
+        stage16f<FP16>(xh, xl, row, c0, 16 * KT1, x, with_lo);
     }
 }
 
@@ -183,8 +185,9 @@ struct RadShape {
 // Radiance forward on tcgen05 (models/texture.py:23-58 with the dual colour of
 // :100-149): per 128-sample tile, Z1 = X W1^T, ReLU, Z2 = H1 W2^T, ReLU,
 // out = H2 W3^T, sigmoid (+ sigmoid(feature[1:4])).  The next tile's input is
-// staged while the current tile's later layers run.
-template <int KT1>
+// staged while the current tile's later layers run.  FP16: fp16 operands
+// (the buffer prepared in fp16); one pass stages and multiplies the hi parts.
+template <int KT1, bool FP16>
 __global__ void __launch_bounds__(kTcThreads, 1) rad_fwd_tc_kernel(const __grid_constant__ RadParams P) {
     using Sh = RadShape<KT1>;
     constexpr int K1 = Sh::K1;
@@ -219,12 +222,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) rad_fwd_tc_kernel(const __grid_
                    sW3 = tc::smem_addr(smem + Sh::off_w3), sX = tc::smem_addr(xh), sH = tc::smem_addr(hh);
     const TcOp Xk = op_k(sX, Sh::x, K1), Hk = op_k(sH, Sh::h, 64);
     const TcOp W1k = op_k(sW1, Sh::w1, K1), W2k = op_k(sW2, Sh::w2, 64), W3k = op_k(sW3, Sh::w3, 64);
-    constexpr uint32_t id64 = tc::idesc_bf16_f32(128, 64), id16 = tc::idesc_bf16_f32(128, 16);
+    constexpr uint32_t id64 = tc::idesc_f32(128, 64, FP16), id16 = tc::idesc_f32(128, 16, FP16);
+    const bool with_lo = P.passes != 1;
     uint32_t phase = 0;
     bool alive = true;
     const int64_t n_tiles = (P.S + 127) / 128;
-    if ((int64_t)blockIdx.x < n_tiles) rad_stage_x<KT1>(P, blockIdx.x * 128 + row, blockIdx.x * 128 + row < P.S,
-                                                       row, slice, xh, xl);
+    if ((int64_t)blockIdx.x < n_tiles)
+        rad_stage_x<KT1, FP16>(P, blockIdx.x * 128 + row, blockIdx.x * 128 + row < P.S, row, slice, xh, xl, with_lo);
     for (int64_t t = blockIdx.x; t < n_tiles; t += gridDim.x) {
         const int64_t s = t * 128 + row;
         const bool v = s < P.S;
@@ -237,14 +241,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) rad_fwd_tc_kernel(const __grid_
         phase ^= 1;
         // the input staging is free: the next tile's
         const int64_t tn = t + gridDim.x;
-        if (tn < n_tiles) rad_stage_x<KT1>(P, tn * 128 + row, tn * 128 + row < P.S, row, slice, xh, xl);
+        if (tn < n_tiles) rad_stage_x<KT1, FP16>(P, tn * 128 + row, tn * 128 + row < P.S, row, slice, xh, xl, with_lo);
 #pragma unroll 1
         for (int layer = 0; layer < 2; ++layer) {
             float z[16];
             tc::ld16(tmem + lane_off + 64 * layer + 16 * slice, z);
 #pragma unroll
             for (int j = 0; j < 16; ++j) z[j] = fmaxf(z[j] + vec[64 * layer + 16 * slice + j], 0.f);
-            stage16(hh, hl, row, 16 * slice, 64, z);
+            stage16f<FP16>(hh, hl, row, 16 * slice, 64, z, with_lo);
             tc_publish();
             if (tid == 0) {
                 if (layer == 0) tc_mma_p<4>(tmem + 64, Hk, W2k, id64, false, P.passes);
@@ -817,24 +821,32 @@ extern "C" int64_t angelo_radiance_grad_size(int32_t feat_dim) {
     return 64 * 16 * kt + 64 * 64 + 16 * 64 + 64 + 64 + 16;
 }
 
-extern "C" int angelo_radiance_prep(int32_t feat_dim, const float *W1, const float *b1,
-                                    const float *W2, const float *b2, const float *W3,
-                                    const float *b3, void *net, void *stream) {
+extern "C" int angelo_radiance_prep_format(int32_t feat_dim, int32_t operand_format, const float *W1,
+                                           const float *b1, const float *W2, const float *b2,
+                                           const float *W3, const float *b3, void *net, void *stream) {
     ANGELO_REQUIRE(feat_dim >= 1 && feat_dim + 19 <= kXCols, "radiance_prep: feature width %d",
                    feat_dim);
     ANGELO_REQUIRE(W1 && b1 && W2 && b2 && W3 && b3 && net, "radiance_prep: null pointer");
+    ANGELO_REQUIRE(operand_format == ANGELO_OPERAND_BF16 || operand_format == ANGELO_OPERAND_FP16,
+                   "radiance_prep: operand_format %d", operand_format);
     const RadLayout L = rad_layout(feat_dim);
     rad_prep_kernel<<<blocks_for(rad_prep_threads(L), 256), 256, 0, as_stream(stream)>>>(
-        W1, b1, W2, b2, W3, b3, L, reinterpret_cast<char *>(net));
+        W1, b1, W2, b2, W3, b3, L, operand_format == ANGELO_OPERAND_FP16, reinterpret_cast<char *>(net));
     return check_launch("radiance_prep");
 }
 
+extern "C" int angelo_radiance_prep(int32_t feat_dim, const float *W1, const float *b1,
+                                    const float *W2, const float *b2, const float *W3,
+                                    const float *b3, void *net, void *stream) {
+    return angelo_radiance_prep_format(feat_dim, ANGELO_OPERAND_BF16, W1, b1, W2, b2, W3, b3, net, stream);
+}
+
 namespace {
-template <int KT1, bool BWD>
+template <int KT1, bool BWD, bool FP16 = false>
 int launch_rad(const RadParams &P, cudaStream_t st) {
     using Sh = RadShape<KT1>;
     const size_t smem = BWD ? Sh::b_bytes : Sh::f_bytes;
-    auto k = BWD ? rad_bwd_tc_kernel<KT1> : rad_fwd_tc_kernel<KT1>;
+    auto k = BWD ? rad_bwd_tc_kernel<KT1> : rad_fwd_tc_kernel<KT1, FP16>;
     static PersistentLaunch cfg;
     const int rc = persistent_setup(k, smem, kTcThreads, cfg, BWD ? "radiance_bwd" : "radiance_fwd");
     if (rc != ANGELO_OK) return rc;
@@ -848,9 +860,10 @@ int launch_rad(const RadParams &P, cudaStream_t st) {
 
 template <bool BWD>
 int dispatch_rad(const RadParams &P, cudaStream_t st) {
+    const bool f16 = !BWD && P.fp16;
     switch (P.L.k_tiles1) {
-        case 3: return launch_rad<3, BWD>(P, st);
-        case 6: return launch_rad<6, BWD>(P, st);
+        case 3: return f16 ? launch_rad<3, BWD, true>(P, st) : launch_rad<3, BWD>(P, st);
+        case 6: return f16 ? launch_rad<6, BWD, true>(P, st) : launch_rad<6, BWD>(P, st);
         default:
             set_error("radiance: input width %d not instantiated (feature width 16 or 68)", P.L.in_dim);
             return ANGELO_E_UNSUPPORTED;
@@ -862,7 +875,7 @@ extern "C" int angelo_radiance_fwd(int32_t feat_dim, const void *net, const floa
                                    int64_t feat_stride, const float *grad, const int32_t *ray_idx,
                                    const float *rays_d, int64_t n, int32_t flags, float *rgb,
                                    void *stream) {
-    ANGELO_REQUIRE((flags & ~3) == 0, "radiance_fwd: flags %d", flags);
+    ANGELO_REQUIRE((flags & ~7) == 0, "radiance_fwd: flags %d", flags);
     ANGELO_REQUIRE(feat_dim >= 1 && feat_dim + 19 <= kXCols, "radiance_fwd: feature width");
     ANGELO_REQUIRE(n >= 0, "radiance_fwd: negative n");
     if (n == 0) return ANGELO_OK;
@@ -879,6 +892,7 @@ extern "C" int angelo_radiance_fwd(int32_t feat_dim, const void *net, const floa
     P.S = n;
     P.dual = flags & 1;
     P.passes = (flags & 2) ? 1 : 3;
+    P.fp16 = (flags & 4) != 0;
     P.rgb = rgb;
     return dispatch_rad<false>(P, as_stream(stream));
 }

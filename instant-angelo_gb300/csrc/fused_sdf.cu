@@ -99,7 +99,8 @@ __global__ void sdf_prep_vec_kernel(const float *__restrict__ b1, const float *_
 
 // tcgen05 operands of the three layers (Y = X W^T, kernel column order):
 // element (n, k) at kmajor_offset(n, k, K) of the region's hi half, its lo
-// part at the same offset of the lo half.
+// part at the same offset of the lo half; bf16 or fp16 parts as the layout's
+// operand_format says.
 __global__ void sdf_prep_tc_kernel(const float *__restrict__ W1, const float *__restrict__ W2,
                                    const float *__restrict__ W3, int in_dim, int n_hash,
                                    angelo_sdf_net_layout lay, char *__restrict__ net) {
@@ -118,7 +119,7 @@ __global__ void sdf_prep_tc_kernel(const float *__restrict__ W1, const float *__
         return;
     }
     const float v = layer_w(layer, n, k, W1, W2, W3, in_dim, n_hash, lay.out_dim);
-    const Split sp = split2(v, 0.0f);
+    const Split sp = lay.operand_format == ANGELO_OPERAND_FP16 ? split2h(v, 0.0f) : split2(v, 0.0f);
     const uint32_t o = tc::kmajor_offset(n, k, K);
     *reinterpret_cast<uint16_t *>(net + off + o) = (uint16_t)(sp.hi & 0xFFFFu);
     *reinterpret_cast<uint16_t *>(net + off + half + o) = (uint16_t)(sp.lo & 0xFFFFu);
@@ -344,7 +345,10 @@ struct TcFwdShape {
     static constexpr uint32_t tmem_cols = 256;   // Z1 [0, 64), Z2 [64, 128), output [128, 128 + N3)
 };
 
-template <int KH, int NH, int NT3, int GROUP>
+// FP16: the operands (weights prepared with operand_format fp16 and the
+// staged activations) are fp16 instead of bf16; with one pass per layer
+// (nl.mma_passes == 1) only the hi parts are staged and multiplied.
+template <int KH, int NH, int NT3, int GROUP, bool FP16>
 __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid_constant__ SdfParams P) {
     using Sh = TcFwdShape<KH, NH, NT3>;
     constexpr int K1 = Sh::K1, N3 = Sh::N3;
@@ -384,8 +388,9 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
     const uint32_t sW1h = tc::smem_addr(smem + Sh::off_w1), sW1l = sW1h + Sh::w1;
     const uint32_t sW2h = tc::smem_addr(smem + Sh::off_w2), sW2l = sW2h + Sh::w2;
     const uint32_t sW3h = tc::smem_addr(smem + Sh::off_w3), sW3l = sW3h + Sh::w3;
-    constexpr uint32_t id_hidden = tc::idesc_bf16_f32(128, 64);
-    constexpr uint32_t id_out_main = tc::idesc_bf16_f32(128, N3), id_out_tap = tc::idesc_bf16_f32(128, 16);
+    constexpr uint32_t id_hidden = tc::idesc_f32(128, 64, FP16);
+    constexpr uint32_t id_out_main = tc::idesc_f32(128, N3, FP16), id_out_tap = tc::idesc_f32(128, 16, FP16);
+    const bool with_lo = P.nl.mma_passes != 1;
 
     constexpr int e0 = GROUP == kCurv ? 7 : 0;
     constexpr int ne = GROUP == kPoint ? 1 : (GROUP == kFD ? 7 : 6);
@@ -418,7 +423,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
                 x[2 * j] = f.x;
                 x[2 * j + 1] = f.y;
             }
-            stage16(a1h, a1l, row, 16 * slice, K1, x);
+            stage16f<FP16>(a1h, a1l, row, 16 * slice, K1, x, with_lo);
         } else if (slice == KH) {
             float b[3], xc[3], x[16];
             int m;
@@ -429,7 +434,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
             x[0] = x2m1(xc[0]);
             x[1] = x2m1(xc[1]);
             x[2] = x2m1(xc[2]);
-            stage16(a1h, a1l, row, 16 * KH, K1, x);
+            stage16f<FP16>(a1h, a1l, row, 16 * KH, K1, x, with_lo);
         }
     };
     if (n_items > 0) stage_x(0);
@@ -462,7 +467,7 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
                     tc::ld16(tmem + lane_off + zcol + 16 * slice, z);
 #pragma unroll
                     for (int j = 0; j < 16; ++j) z[j] = softplus100(z[j] + bias[64 * layer + 16 * slice + j]);
-                    stage16(a2h, a2l, row, 16 * slice, 64, z);
+                    stage16f<FP16>(a2h, a2l, row, 16 * slice, 64, z, with_lo);
                 }
                 tc_publish();
                 if (tid == 0) {
@@ -1148,6 +1153,7 @@ extern "C" int angelo_sdf_net_layout_query(int32_t n_levels, int32_t n_hidden, i
     L.off_tcw3 = take(2 * (16 * L.k_tiles3b) * 64 * 2);
     L.bytes = o;
     L.mma_passes = 3;
+    L.operand_format = ANGELO_OPERAND_BF16;
     *out = L;
     return ANGELO_OK;
 }
@@ -1158,6 +1164,8 @@ extern "C" int angelo_sdf_prep(const angelo_sdf_net_layout *lay, int32_t n_level
     ANGELO_REQUIRE(lay && W1 && b1 && W3 && b3 && net, "sdf_prep: null pointer");
     ANGELO_REQUIRE(lay->n_hidden == 1 || (W2 && b2), "sdf_prep: missing hidden layer 2");
     ANGELO_REQUIRE(in_dim == 3 + 2 * n_levels, "sdf_prep: in_dim %d != 3 + 2*levels", in_dim);
+    ANGELO_REQUIRE(lay->operand_format == ANGELO_OPERAND_BF16 || lay->operand_format == ANGELO_OPERAND_FP16,
+                   "sdf_prep: operand_format %d", lay->operand_format);
     const int K1 = lay->k_tiles1, nh = lay->n_hidden;
     sdf_prep_vec_kernel<<<1, 192 + 8 * lay->n_tiles3, 0, as_stream(stream)>>>(
         b1, b2, W3, b3, *lay, reinterpret_cast<char *>(net));
@@ -1190,10 +1198,10 @@ int launch_scatter(const SdfParams &P, cudaStream_t s) {
     return check_launch("sdf_stencil_scatter");
 }
 
-template <int KH, int NH, int NT3, int GROUP>
-int launch_mlp_fwd(const SdfParams &P, cudaStream_t s) {
+template <int KH, int NH, int NT3, int GROUP, bool FP16>
+int launch_mlp_fwd_fmt(const SdfParams &P, cudaStream_t s) {
     const size_t smem = TcFwdShape<KH, NH, NT3>::bytes;
-    auto k = sdf_mlp_fwd_kernel<KH, NH, NT3, GROUP>;
+    auto k = sdf_mlp_fwd_kernel<KH, NH, NT3, GROUP, FP16>;
     static PersistentLaunch cfg;
     const int rc = persistent_setup(k, smem, kTcThreads, cfg, "sdf_mlp_fwd");
     if (rc != ANGELO_OK) return rc;
@@ -1205,6 +1213,12 @@ int launch_mlp_fwd(const SdfParams &P, cudaStream_t s) {
     const int grid = (int)std::min<int64_t>(tiles, (int64_t)cfg.sms * 2);
     k<<<grid, kTcThreads, smem, s>>>(P);
     return check_launch("sdf_mlp_fwd");
+}
+
+template <int KH, int NH, int NT3, int GROUP>
+int launch_mlp_fwd(const SdfParams &P, cudaStream_t s) {
+    return P.nl.operand_format == ANGELO_OPERAND_FP16 ? launch_mlp_fwd_fmt<KH, NH, NT3, GROUP, true>(P, s)
+                                                      : launch_mlp_fwd_fmt<KH, NH, NT3, GROUP, false>(P, s);
 }
 
 template <int KH, int NH, int NT3, int GROUP>
@@ -1297,6 +1311,8 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
     ANGELO_REQUIRE(eps > 0.f && radius > 0.f, "sdf_stencil_fwd: eps/radius");
     ANGELO_REQUIRE(nl->mma_passes == 1 || nl->mma_passes == 3, "sdf_stencil_fwd: mma_passes %d (1 or 3)",
                    nl->mma_passes);
+    ANGELO_REQUIRE(nl->operand_format == ANGELO_OPERAND_BF16 || nl->operand_format == ANGELO_OPERAND_FP16,
+                   "sdf_stencil_fwd: operand_format %d", nl->operand_format);
     ANGELO_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 7) == 0, "sdf_stencil_fwd: workspace alignment");
     SdfParams P{};
     P.lay = *lay;
@@ -1367,6 +1383,9 @@ extern "C" int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32
     ANGELO_REQUIRE(!with_laplace || (with_grad && rand_dirs), "sdf_stencil_bwd: laplace inputs");
     ANGELO_REQUIRE(g_feature == nullptr || gfeat_stride >= nl->out_dim, "sdf_stencil_bwd: stride");
     ANGELO_REQUIRE(eps > 0.f && radius > 0.f, "sdf_stencil_bwd: eps/radius");
+    ANGELO_REQUIRE(nl->operand_format == ANGELO_OPERAND_BF16,
+                   "sdf_stencil_bwd: the backward runs in bf16x3 and needs weights prepared with "
+                   "operand_format bf16 (got %d)", nl->operand_format);
     ANGELO_REQUIRE((reinterpret_cast<uintptr_t>(workspace) & 7) == 0 &&
                        (reinterpret_cast<uintptr_t>(bwd_workspace) & 7) == 0,
                    "sdf_stencil_bwd: workspace alignment");

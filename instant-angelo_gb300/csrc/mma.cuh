@@ -16,6 +16,7 @@
 #pragma once
 
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 
 namespace angelo {
@@ -33,6 +34,29 @@ __device__ __forceinline__ Split split2(float x0, float x1) {
     s.hi = *reinterpret_cast<const uint32_t *>(&h);
     s.lo = *reinterpret_cast<const uint32_t *>(&l);
     return s;
+}
+
+// the same split into fp16 hi and lo parts (11 significant bits each: the
+// operand format of the fp16 precision form)
+__device__ __forceinline__ Split split2h(float x0, float x1) {
+    const __half2 h = __floats2half2_rn(x0, x1);
+    const float2 hf = __half22float2(h);
+    const __half2 l = __floats2half2_rn(x0 - hf.x, x1 - hf.y);
+    Split s;
+    s.hi = *reinterpret_cast<const uint32_t *>(&h);
+    s.lo = *reinterpret_cast<const uint32_t *>(&l);
+    return s;
+}
+
+// packed fp16x2 or bf16x2 of (x0, x1) alone (a single-pass operand)
+template <bool FP16>
+__device__ __forceinline__ uint32_t pack2(float x0, float x1) {
+    if (FP16) {
+        const __half2 h = __floats2half2_rn(x0, x1);
+        return *reinterpret_cast<const uint32_t *>(&h);
+    }
+    const __nv_bfloat162 h = __floats2bfloat162_rn(x0, x1);
+    return *reinterpret_cast<const uint32_t *>(&h);
 }
 
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0,

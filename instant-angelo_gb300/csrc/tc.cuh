@@ -68,6 +68,19 @@ __host__ __device__ constexpr uint32_t idesc_bf16_f32(int M, int N, int a_mn = 0
            | ((uint32_t)(M >> 4) << 24);   // M / 16
 }
 
+// The same for A and B in fp16 (format field 0).  A and B always share one
+// type in a kind::f16 product.
+__host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N, int a_mn = 0, int b_mn = 0) {
+    return (1u << 4)                       // D format: f32
+           | ((uint32_t)(a_mn & 1) << 15)  // A major
+           | ((uint32_t)(b_mn & 1) << 16)  // B major
+           | ((uint32_t)(N >> 3) << 17)    // N / 8
+           | ((uint32_t)(M >> 4) << 24);   // M / 16
+}
+__host__ __device__ constexpr uint32_t idesc_f32(int M, int N, bool fp16) {
+    return fp16 ? idesc_f16_f32(M, N) : idesc_bf16_f32(M, N);
+}
+
 // ---- tensor memory allocation (one full warp)
 __device__ __forceinline__ void tmem_alloc(uint32_t *slot_smem, uint32_t ncols) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n"

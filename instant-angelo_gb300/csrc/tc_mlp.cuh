@@ -57,6 +57,38 @@ __device__ __forceinline__ void stage16(char *hi, char *lo, int r, int c0, int K
     *reinterpret_cast<uint4 *>(lo + o1) = make_uint4(l[4], l[5], l[6], l[7]);
 }
 
+// stage16 in the operand format of the forward kernels: bf16 or fp16, with
+// the lo part (three products) or the hi part alone (one pass: the lo half
+// is not written and not read)
+template <bool FP16>
+__device__ __forceinline__ void stage16f(char *hi, char *lo, int r, int c0, int K, const float (&v)[16],
+                                         bool with_lo) {
+    const uint32_t o0 = tc::kmajor_offset(r, c0, K), o1 = tc::kmajor_offset(r, c0 + 8, K);
+    if (!with_lo) {
+        uint32_t h[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) h[i] = pack2<FP16>(v[2 * i], v[2 * i + 1]);
+        *reinterpret_cast<uint4 *>(hi + o0) = make_uint4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<uint4 *>(hi + o1) = make_uint4(h[4], h[5], h[6], h[7]);
+        return;
+    }
+    if (!FP16) {
+        stage16(hi, lo, r, c0, K, v);
+        return;
+    }
+    uint32_t h[8], l[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const Split sp = split2h(v[2 * i], v[2 * i + 1]);
+        h[i] = sp.hi;
+        l[i] = sp.lo;
+    }
+    *reinterpret_cast<uint4 *>(hi + o0) = make_uint4(h[0], h[1], h[2], h[3]);
+    *reinterpret_cast<uint4 *>(hi + o1) = make_uint4(h[4], h[5], h[6], h[7]);
+    *reinterpret_cast<uint4 *>(lo + o0) = make_uint4(l[0], l[1], l[2], l[3]);
+    *reinterpret_cast<uint4 *>(lo + o1) = make_uint4(l[4], l[5], l[6], l[7]);
+}
+
 // descriptor fields of one staged operand for one K step of 16
 struct TcOp {
     uint32_t hi, lo, lbo, sbo, step;

@@ -1,23 +1,35 @@
 """Precision study (the precision form of the small configuration): the fused
 path with an FP16 or FP32 hash table, the geometry and radiance MLPs on
-tensor cores (bf16 hi/lo operands, fp32 accumulation), fp32 alpha with the
-FP64-gated sigmoid difference above inv_s = 2048 and the log-space
-transmittance scan; the plain FP32 path beside it.  Every error is against
-the FP64 oracle run on the GPU (oracle/neus_fp64.py):
+tensor cores with fp32 accumulation, fp32 alpha with the FP64-gated sigmoid
+difference above inv_s = 2048 and the log-space transmittance scan; the
+plain FP32 path beside it.  Every error is against the FP64 oracle run on the
+GPU (oracle/neus_fp64.py), on a field first trained for TRAIN_STEPS steps
+on the analytic sphere scene (so that its renders resemble the targets and
+PSNR means something):
 
 * SDF and unit normals (finite-difference gradient, eps 1e-2) on 2^20 uniform
   points in [-1, 1]^3;
-* per-ray colour and per-sample weights on 8192 rays;
+* per-ray colour and per-sample weights on 8192 rays of the scene's views,
+  and PSNR (systems/criterions.py:40-53) of every form's colour against the
+  FP64 oracle's render and against the views' target colours;
 * alpha at inv_s in {20, 2048, 1e4, 1e5} from the same fp32 inputs (the FP64
   sigmoid difference of those inputs is the reference, so the comparison
   isolates the alpha arithmetic from the conditioning of alpha in the SDF).
 
-The report (max / mean absolute errors) goes to $ANGELO_PRECISION_REPORT when
-that is set.  Bounds: 1e-3 for every fused output with the FP32 table and for
-the gated alpha at every inv_s.  The precision form proper (FP16 table, the
-forward MLPs in one bf16 pass: fused_precision "bf16") is reported beside
-them; its SDF error must exceed the bf16x3 form's (the single pass is in
-effect) and stay below 0.1."""
+Forms: plain FP32; fused with the FP32 table (MLP operands bf16x3, the
+training form); fused with the FP16 table; the precision form proper (FP16
+table, every forward MLP layer one fp16 tensor-core pass with fp32
+accumulation: fused_precision "fp16"); and the single-bf16-pass variant
+(fused_precision "bf16") for comparison.
+
+Bounds (the precision target): SDF max-abs error <= 1e-3 and target PSNR
+within 0.1 dB of the FP64 oracle's for the plain, fused and precision forms;
+1e-3 on the colour and weights of the FP32-table forms; 1e-3 on the gated
+alpha at every inv_s.  The single bf16 pass is reported, and must be worse
+than bf16x3 (the pass count is in effect).
+
+The report (max / mean absolute errors, PSNR) goes to
+$ANGELO_PRECISION_REPORT when that is set."""
 import json
 import math
 import os
@@ -30,7 +42,16 @@ pytestmark = pytest.mark.gpu
 
 N_POINTS = 1 << 20
 N_RAYS = 8192
+TRAIN_STEPS = 300
 REPORT = {}
+FORMS = {  # name: (fused, fp16 table, fused_precision)
+    "plain_fp32": (False, False, "fp32"),
+    "fused_fp32_table": (True, False, "fp32"),
+    "fused_fp16_table": (True, True, "fp32"),
+    "fused_fp16_table_fp16_mlp": (True, True, "fp16"),
+    "fused_fp16_table_bf16_mlp": (True, True, "bf16"),
+}
+PRECISION_FORM = "fused_fp16_table_fp16_mlp"
 
 
 @pytest.fixture(scope="module")
@@ -42,22 +63,50 @@ def dev():
     return torch.device("cuda:0")
 
 
-def _model(dev, fused, fp16_table=False, one_pass=False):
+@pytest.fixture(scope="module")
+def views(dev):
+    from angelo_gb import scenes
+    return scenes.TargetViews(scenes.SphereScene(), 8, 256, 256, 64.0, 2.5, seed=3, device=dev)
+
+
+@pytest.fixture(scope="module")
+def trained(dev, views):
+    """State of the small fused model after TRAIN_STEPS training steps on the
+    sphere views from a perturbed start (U(-0.05, 0.05) table, N(0, 0.05^2)
+    hash columns of the first layer), white background."""
     from angelo_gb import models, workloads
+    from angelo_gb.system import NeuSTrainer
     torch.manual_seed(0)
-    extra = {"fused_precision": "bf16"} if one_pass else {}
-    m = models.make("neus", workloads.model_config("small", fused=fused, **extra)).to(dev)
-    m.update_step(0, 5000)
+    m = models.make("neus", workloads.model_config("small", fused=True)).to(dev)
     with torch.no_grad():
         g = torch.Generator(device="cpu").manual_seed(7)
         p = m.geometry.hashgrid.encoding.params
         p.copy_((torch.rand(p.shape, generator=g) * 0.1 - 0.05).to(dev))
-        # the sphere initialisation leaves the hash-feature columns of the
-        # first layer at zero: give them weight so that the table matters
         wv = m.geometry.network.layers[0].weight_v
         wv[:, 3:].copy_((torch.randn(wv[:, 3:].shape, generator=g) * 0.05).to(dev))
-        if fp16_table:
-            m.geometry.hashgrid.encoding.params.data = p.data.half()
+    m.train()
+    tr = NeuSTrainer(m, workloads.SYSTEM, train_num_rays=1024, max_train_num_rays=1024,
+                     dynamic_ray_sampling=False)
+    tr.global_step = 5000
+    gen = torch.Generator(device=dev).manual_seed(11)
+    white = torch.ones(3, device=dev)
+    for _ in range(TRAIN_STEPS):
+        rays, rgb = views.sample_rays(1024, generator=gen)
+        tr.step(rays, rgb, white)
+    torch.cuda.synchronize()
+    return {k: v.detach().clone() for k, v in m.state_dict().items()}
+
+
+def _model(dev, trained, name):
+    from angelo_gb import models, workloads
+    fused, fp16_table, prec = FORMS[name]
+    extra = {"fused_precision": prec} if prec != "fp32" else {}
+    m = models.make("neus", workloads.model_config("small", fused=fused, **extra)).to(dev)
+    m.load_state_dict(trained)
+    m.update_step(0, 5000)
+    if fp16_table:
+        p = m.geometry.hashgrid.encoding.params
+        p.data = p.data.half()
     return m.train()
 
 
@@ -92,11 +141,9 @@ def _write():
             json.dump(REPORT, f, indent=1, sort_keys=True)
 
 
-def test_precision_sdf_and_normals(dev):
+def test_precision_sdf_and_normals(dev, trained):
     from oracle import neus_fp64 as O
-    forms = {"plain_fp32": _model(dev, False), "fused_fp32_table": _model(dev, True),
-             "fused_fp16_table": _model(dev, True, fp16_table=True),
-             "fused_fp16_table_bf16_mlp": _model(dev, True, fp16_table=True, one_pass=True)}
+    forms = {name: _model(dev, trained, name) for name in FORMS}
     P, G, _ = _oracle_cfg(forms["plain_fp32"])
     g = torch.Generator(device="cpu").manual_seed(11)
     pts = (torch.rand(N_POINTS, 3, generator=g) * 2.0 - 1.0).to(dev)
@@ -117,34 +164,25 @@ def test_precision_sdf_and_normals(dev):
     for name in ("plain_fp32", "fused_fp32_table"):
         assert out[name]["sdf"]["max"] < 1e-3, (name, out[name])
         assert out[name]["normal"]["mean"] < 1e-3, (name, out[name])
-    assert out["fused_fp16_table"]["sdf"]["max"] < 1e-2, out["fused_fp16_table"]
-    # the precision form proper (FP16 table, one bf16 pass per layer): its SDF
-    # error is bf16's (~2^-9 relative); the FD normal divides it by 2 eps
+    # the precision target: SDF within 1e-3 of FP64 with FP16 storage
+    for name in ("fused_fp16_table", PRECISION_FORM):
+        assert out[name]["sdf"]["max"] <= 1e-3, (name, out[name])
+    # the single bf16 pass is in effect: its error is bf16's (~2^-9 relative)
     one = out["fused_fp16_table_bf16_mlp"]
-    assert one["sdf"]["max"] < 0.1 and math.isfinite(one["normal"]["max"]), one
     assert one["sdf"]["max"] > out["fused_fp16_table"]["sdf"]["max"], (one, out["fused_fp16_table"])
+    # fp16 (11 significant bits) resolves the SDF better than bf16 (8)
+    assert out[PRECISION_FORM]["sdf"]["max"] < one["sdf"]["max"], out
 
 
-def _rays(dev):
-    from angelo_gb.scenes import look_at_c2w, pixel_directions, rays_from
-    g = np.random.default_rng(5)
-    dirs = pixel_directions(256, 256, 64.0, device=dev).reshape(-1, 3)
-    out = []
-    for k in range(N_RAYS // 1024):
-        v = g.normal(size=3)
-        c2w = torch.as_tensor(look_at_c2w(tuple(2.5 * v / np.linalg.norm(v))), dtype=torch.float32,
-                              device=dev)
-        pix = torch.from_numpy(g.integers(0, dirs.shape[0], 1024)).to(dev)
-        out.append(rays_from(dirs[pix], c2w[None].expand(1024, 3, 4)))
-    return torch.cat(out).float().contiguous()
-
-
-def test_precision_render(dev):
+def test_precision_render(dev, trained, views):
     from angelo_gb import fused
+    from angelo_gb.system import psnr
     from oracle import neus_fp64 as O
-    rays = _rays(dev)
+    gen = torch.Generator(device=dev).manual_seed(5)
+    rays, target = views.sample_rays(N_RAYS, generator=gen)
+    rays = rays.float().contiguous()
     o, d = rays[:, :3].contiguous(), rays[:, 3:].contiguous()
-    plain = _model(dev, False)
+    plain = _model(dev, trained, "plain_fp32")
     bg = torch.ones(3, device=dev)
     plain.background_color = bg
     plain.randomized = False
@@ -154,23 +192,30 @@ def test_precision_render(dev):
     with torch.no_grad():
         ref = O.neus_render(rays.double(), P, G, T, (off.cpu().numpy(), ri.long(), t0, t1), rd.double(),
                             1.0, bg.double(), training=True)
-    out = {}
-    for name, m in (("plain_fp32", plain), ("fused_fp32_table", _model(dev, True)),
-                    ("fused_fp16_table", _model(dev, True, fp16_table=True)),
-                    ("fused_fp16_table_bf16_mlp", _model(dev, True, fp16_table=True, one_pass=True))):
+    psnr_ref = float(psnr(ref["comp_rgb_full"], target.double()))
+    out = {"fp64_oracle": {"psnr_vs_target": psnr_ref}}
+    for name in FORMS:
+        m = plain if name == "plain_fp32" else _model(dev, trained, name)
         m.background_color = bg
         m.geometry.curvature_dirs_fn = lambda t: rd
         m.train()
         m.randomized = False
         with torch.no_grad():
             r = m.forward_(rays)
+        p_t = float(psnr(r["comp_rgb_full"].double(), target.double()))
         out[name] = {"colour": _err(r["comp_rgb_full"], ref["comp_rgb_full"]),
-                     "weights": _err(r["weights"].view(-1), ref["weights"])}
+                     "weights": _err(r["weights"].view(-1), ref["weights"]),
+                     "psnr_vs_fp64": float(psnr(r["comp_rgb_full"].double(), ref["comp_rgb_full"])),
+                     "psnr_vs_target": p_t, "psnr_delta_db": p_t - psnr_ref}
     REPORT["rays_8192"] = out
     _write()
+    # the trained field renders the scene: PSNR is a meaningful comparison
+    assert psnr_ref > 15.0, out
     for name in ("plain_fp32", "fused_fp32_table"):
         assert out[name]["colour"]["max"] < 1e-3, (name, out[name])
         assert out[name]["weights"]["max"] < 1e-3, (name, out[name])
+    for name in ("plain_fp32", "fused_fp32_table", "fused_fp16_table", PRECISION_FORM):
+        assert abs(out[name]["psnr_delta_db"]) <= 0.1, (name, out[name])
 
     # alpha at increasing sharpness, from the same fp32 inputs
     sdf32 = ref["sdf_samples"].float()

@@ -127,7 +127,9 @@ def test_sdf_net_layout_query_and_struct(lib):
     assert (L.k_tiles1, L.n_hidden, L.n_tiles3, L.mma_passes) == (2, 1, 2, 3)
     assert lib.angelo_sdf_net_layout_query(16, 3, 65, ctypes.byref(L)) != 0
     assert _lib.SdfNetLayout.mma_passes.offset == 5 * 4 + 4 + 8 * 8
+    assert _lib.SdfNetLayout.operand_format.offset == 5 * 4 + 4 + 8 * 8 + 4
     assert ctypes.sizeof(_lib.SdfNetLayout) == 5 * 4 + 4 + 8 * 8 + 8
+    assert L.operand_format == _lib.OPERAND_BF16
 
 
 def test_probe_library_is_separate_and_complete(lib):
@@ -141,3 +143,27 @@ def test_probe_library_is_separate_and_complete(lib):
     for s in declared:
         assert hasattr(P, s), s
         assert not hasattr(lib, s), s
+
+
+def test_backward_refuses_fp16_prepared_weights(lib):
+    """The fused VolumeSDF backward reads bf16 operands: a weight buffer whose
+    layout says fp16 (the precision form's forward buffer) is refused on the
+    host, before anything is launched (the pointers here are host memory)."""
+    import torch
+    from angelo_gb import _lib
+    L = _lib.SdfNetLayout()
+    assert lib.angelo_sdf_net_layout_query(8, 1, 13, ctypes.byref(L)) == 0
+    L.operand_format = _lib.OPERAND_FP16
+    lay = _lib.HashGridLayout()
+    desc = _lib.HashGridDesc(8, 2, 16, 16, 1.5)
+    assert lib.angelo_hashgrid_layout(ctypes.byref(desc), ctypes.byref(lay)) == 0
+    host = torch.zeros(64)
+    p = host.data_ptr()
+    rc = lib.angelo_sdf_stencil_bwd(ctypes.byref(lay), 8, p, 0, ctypes.byref(L), p, p, None, 1, 1.0,
+                                    1e-2, 1, 0, p, p, None, None, None, 0, None, None, p, None)
+    assert rc == _lib.ANGELO_E_INVALID
+    assert b"operand_format" in lib.angelo_last_error_string()
+    L.operand_format = 7
+    rc = lib.angelo_sdf_stencil_fwd(ctypes.byref(lay), 8, p, 0, ctypes.byref(L), p, p, None, 1, 1.0,
+                                    1e-2, 0, 0, 0, p, None, None, 0, None, p, None)
+    assert rc == _lib.ANGELO_E_INVALID
