@@ -142,9 +142,12 @@ _lock = threading.Lock()
 _lib = None
 
 
-def load(path: str = LIB_PATH):
-    """Load libangelo_gb.so and bind every entry point of the C ABI."""
+def load(path: str = None):
+    """Load libangelo_gb.so and bind every entry point of the C ABI.  The
+    library next to this package, or the file $ANGELO_GB_LIB names (a build
+    of the same sources with other compile-time settings)."""
     global _lib
+    path = path or os.environ.get("ANGELO_GB_LIB") or LIB_PATH
     with _lock:
         if _lib is None:
             if not os.path.exists(path):

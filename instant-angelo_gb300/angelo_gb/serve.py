@@ -6,8 +6,9 @@ on the device.  Requests of uneven size arrive over time; the loop admits them
 while enough HBM is free, cuts them into fixed-shape buckets (rays or lattice
 points) and runs the buckets of all admitted requests back to back as
 CUDA-graph replays on two streams, so renders and SDF grids overlap on the
-device.  Completion is observed through events: a request that arrives while
-others are on the GPU joins the next bucket.
+device (two render buckets take turns, so renders also overlap each other).
+Completion is observed through events: a request that arrives while others
+are on the GPU joins the next bucket.
 
 A render bucket is: clip to the near/far planes or the scene box, march
 (count, scan, fill into a fixed sample capacity), the fused VolumeSDF (the
@@ -260,21 +261,26 @@ class Server:
     ray_bucket rays per render bucket (each at most max_samples_per_ray
     samples), point_bucket lattice points per SDF bucket; a request is
     admitted when the HBM left after its result buffers stays above
-    hbm_reserve bytes."""
+    hbm_reserve bytes.  render_streams render buckets (each its own captured
+    graph, buffers and stream) take turns, so consecutive render buckets
+    overlap on the device as well as renders and SDF grids."""
 
     def __init__(self, model, ray_bucket=1 << 14, max_samples_per_ray=128, point_bucket=1 << 20,
-                 use_graph=True, hbm_reserve=4 << 30, background=(1.0, 1.0, 1.0)):
+                 use_graph=True, hbm_reserve=4 << 30, background=(1.0, 1.0, 1.0),
+                 render_streams=2):
         if not torch.cuda.is_available():
             raise RuntimeError("the serving loop runs on the GPU")
         self.m = model.eval()
         dev = model.scene_aabb.device
         self.dev = dev
         self.bg = torch.tensor(background, device=dev, dtype=torch.float32)
-        self.rs = torch.cuda.Stream(dev)
+        self.rbs = [RenderBucket(model, ray_bucket, max_samples_per_ray, torch.cuda.Stream(dev),
+                                 self.bg, use_graph) for _ in range(max(1, int(render_streams)))]
+        self.rb = self.rbs[0]
         self.ss = torch.cuda.Stream(dev)
-        self.rb = RenderBucket(model, ray_bucket, max_samples_per_ray, self.rs, self.bg, use_graph)
         self.sb = SdfBucket(model, point_bucket, self.ss, use_graph)
-        self.rb.prepare()
+        for rb in self.rbs:
+            rb.prepare()
         self.sb.prepare()
         self.reserve = int(hbm_reserve)
         self.overflows = 0
@@ -340,11 +346,12 @@ class Server:
                     k += 1
                 turn += 1
                 if parts:
-                    with torch.cuda.stream(self.rs):
+                    rb = self.rbs[self.buckets % len(self.rbs)]
+                    with torch.cuda.stream(rb.stream):
                         rays = torch.cat([request_rays(q, s, n, self.dev) for q, s, n in parts])
-                    full, op, dep, st = self.rb.launch(rays, rays.shape[0])
+                    full, op, dep, st = rb.launch(rays, rays.shape[0])
                     o = 0
-                    with torch.cuda.stream(self.rs):
+                    with torch.cuda.stream(rb.stream):
                         for q, s, n in parts:
                             q.rgb[s:s + n].copy_(full[o:o + n])
                             q.opacity[s:s + n].copy_(op[o:o + n])
@@ -352,7 +359,7 @@ class Server:
                             o += n
                             q.pending += 1
                         ev = torch.cuda.Event()
-                        ev.record(self.rs)
+                        ev.record(rb.stream)
                     inflight.append((ev, parts, st, rays))
                     self.buckets += 1
                     launched = True

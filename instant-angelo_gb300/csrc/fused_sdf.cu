@@ -48,6 +48,14 @@ using namespace angelo;
 namespace {
 
 constexpr int kEncThreads = 128;
+// resident blocks per SM the encode and scatter kernels are compiled for
+// (their register budget: 65536 / (128 x blocks) per thread)
+#ifndef ANGELO_ENCODE_MIN_BLOCKS
+#define ANGELO_ENCODE_MIN_BLOCKS 1
+#endif
+#ifndef ANGELO_SCATTER_MIN_BLOCKS
+#define ANGELO_SCATTER_MIN_BLOCKS 1
+#endif
 constexpr int kState = 16;      // per sample: sdf of the 13 evaluations, shifted point (3)
 constexpr int kBState = 8;      // per sample, backward: dL/dshifted (3), dL/dnormal from curvature (3)
 constexpr uint32_t kAggregateRes = 300;  // levels up to this resolution aggregate their atomics
@@ -237,7 +245,8 @@ __device__ __forceinline__ float2 centre_value(const float2 (&vc)[8], int delta,
 // ---------------------------------------------------------------- encode
 
 template <int GROUP>
-__global__ void __launch_bounds__(kEncThreads) stencil_encode_kernel(const __grid_constant__ SdfParams P) {
+__global__ void __launch_bounds__(kEncThreads, ANGELO_ENCODE_MIN_BLOCKS)
+    stencil_encode_kernel(const __grid_constant__ SdfParams P) {
     const int l = blockIdx.y;
     const int64_t s = (int64_t)blockIdx.x * kEncThreads + threadIdx.x;
     if (s >= P.S) return;
@@ -1032,7 +1041,8 @@ __device__ __forceinline__ void centre_add(float2 (&acc)[8], int delta, int cc, 
 }
 
 template <int GROUP>
-__global__ void __launch_bounds__(kEncThreads) stencil_scatter_kernel(const __grid_constant__ SdfParams P) {
+__global__ void __launch_bounds__(kEncThreads, ANGELO_SCATTER_MIN_BLOCKS)
+    stencil_scatter_kernel(const __grid_constant__ SdfParams P) {
     const int l = blockIdx.y;
     const int64_t s = (int64_t)blockIdx.x * kEncThreads + threadIdx.x;
     const bool valid = s < P.S;

@@ -226,22 +226,28 @@ def accumulate_along_rays(weights, ray_indices, values=None, n_rays=None):
 # ---------------------------------------------------------------- installation
 
 
-def install(reference_root):
+def install(reference_root, kernel_modules=None):
     """Insert the stand-in modules and import the reference's ``models``
-    package from ``reference_root``.  Returns the imported ``models`` module."""
+    package from ``reference_root``.  Returns the imported ``models`` module.
+    kernel_modules ({name: module} for tinycudann, nerfacc and
+    nerfacc.intersection, e.g. angelo_gb.seam.modules()) replaces the
+    oracle's tcnn / nerfacc restatements."""
     def mod(name, **attrs):
         m = types.ModuleType(name)
         m.__dict__.update(attrs)
         sys.modules[name] = m
         return m
 
-    mod("tinycudann", Encoding=_tcnn_encoding, Network=None,
-        NetworkWithInputEncoding=None, free_temporary_memory=lambda: None)
-    nerfacc = mod("nerfacc", ContractionType=ContractionType, OccupancyGrid=OccupancyGrid,
-                  ray_marching=ray_marching, render_weight_from_alpha=render_weight_from_alpha,
-                  render_weight_from_density=render_weight_from_density,
-                  accumulate_along_rays=accumulate_along_rays)
-    nerfacc.intersection = mod("nerfacc.intersection", ray_aabb_intersect=ray_aabb_intersect)
+    if kernel_modules is not None:
+        sys.modules.update(kernel_modules)
+    else:
+        mod("tinycudann", Encoding=_tcnn_encoding, Network=None,
+            NetworkWithInputEncoding=None, free_temporary_memory=lambda: None)
+        nerfacc = mod("nerfacc", ContractionType=ContractionType, OccupancyGrid=OccupancyGrid,
+                      ray_marching=ray_marching, render_weight_from_alpha=render_weight_from_alpha,
+                      render_weight_from_density=render_weight_from_density,
+                      accumulate_along_rays=accumulate_along_rays)
+        nerfacc.intersection = mod("nerfacc.intersection", ray_aabb_intersect=ray_aabb_intersect)
     noop = lambda *a, **k: None  # noqa: E731
     pl = mod("pytorch_lightning", LightningModule=nn.Module)
     pl.utilities = mod("pytorch_lightning.utilities")

@@ -270,4 +270,4 @@ def test_full_model_backward_matches_fp64(dev):
         print(row)
     scale = max(abs(r_[3]) for r_ in rows)
     for k, i, a, ag in rows:
-        assert abs(a - ag) <= 1e-2 * max(abs(ag), 1e-2 * scale), ("fused", k, i, a, ag)
+        assert abs(a - ag) <= 5e-3 * max(abs(ag), 1e-2 * scale), ("fused", k, i, a, ag)

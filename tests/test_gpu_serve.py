@@ -57,6 +57,22 @@ def test_render_same_alone_and_in_mix(dev):
         assert q.done is not None and q.done >= q.arrival
     assert srv.overflows == 0
     assert float(a.opacity.max()) > 0.5      # the view sees the surface
+    assert len(srv.rbs) == 2 and srv.buckets > 2
+
+
+def test_single_render_stream_gives_the_same_result(dev):
+    from angelo_gb.serve import RenderRequest, Server
+    m = _model(dev)
+    a, b, grid, c = _requests(dev)
+    outs = []
+    for streams in (1, 2):
+        srv = Server(m, ray_bucket=2048, max_samples_per_ray=128, point_bucket=1 << 12,
+                     hbm_reserve=1 << 30, render_streams=streams)
+        qs = [RenderRequest(q.rid, q.c2w, q.W, q.H) for q in (a, b, c)]
+        srv.run(qs, realtime=False)
+        outs.append(qs)
+    for q1, q2 in zip(*outs):
+        assert torch.equal(q1.rgb, q2.rgb) and torch.equal(q1.depth, q2.depth)
 
 
 def test_overflowing_bucket_is_rendered_exactly(dev):
@@ -68,10 +84,15 @@ def test_overflowing_bucket_is_rendered_exactly(dev):
     q = RenderRequest(0, a.c2w, a.W, a.H)
     srv.run([q], realtime=False)
     assert srv.overflows > 0
-    # the bucket's own compositing walked only the samples the fill kept:
-    # its offsets end at the capacity and never pass it
-    off = srv.rb.offsets.cpu()
-    assert int(off[-1]) == srv.rb.cap and bool((off[1:] >= off[:-1]).all())
+    # each bucket's own compositing walked only the samples the fill kept:
+    # its offsets never pass the capacity, and those of an overflowed replay
+    # end at it
+    ends = []
+    for rb in srv.rbs:
+        off = rb.offsets.cpu()
+        assert int(off[-1]) <= rb.cap and bool((off[1:] >= off[:-1]).all())
+        ends.append(int(off[-1]) == rb.cap)
+    assert any(ends)
     full, op, dep = render_exact(m, request_rays(q, 0, q.n, dev), srv.bg)
     assert torch.equal(q.rgb, full)
 
