@@ -65,6 +65,10 @@ def parse():
     ap.add_argument("--sdf-case", type=int, default=0, metavar="N",
                     help="profiling case: 3 fused VolumeSDF training passes (16 levels x 2^22, "
                          "FD + curvature) on N points of the full model, then exit")
+    ap.add_argument("--sdf-timing", action="store_true",
+                    help="time the fused VolumeSDF forward and backward calls (CUDA events, "
+                         "median of --steps passes) on the samples of one training step's march "
+                         "(8192 rays through the analytic occupancy grid), then exit")
     return ap.parse_args()
 
 
@@ -179,7 +183,11 @@ def make_trainer(form, dev, seed=0):
     from angelo_gb.system import NeuSTrainer
     torch.manual_seed(seed)
     extra = workloads.background() if form == "fused_bg" else {}
-    cfg = workloads.model_config("full", fused=form in ("fused", "fused_bg"), **extra)
+    if form == "fused_fp16_table":
+        # the encode gathers from an fp16 copy of the fp32 table (made once
+        # per pass); gradients and AdamW stay fp32
+        extra["fused_table_dtype"] = "fp16"
+    cfg = workloads.model_config("full", fused=form != "plain", **extra)
     model = models.make("neus", cfg).to(dev)
     model.train()
     with torch.no_grad():
@@ -455,7 +463,7 @@ def available_forms():
     try:
         from angelo_gb import fused  # noqa: F401
         if fused.available():
-            forms += ["fused", "fused_bg"]
+            forms += ["fused", "fused_fp16_table", "fused_bg"]
     except ImportError:
         pass
     return forms
@@ -548,7 +556,17 @@ def run_ours(args):
         rays_e = sum(a[0] for a in acc_e)
         samples_e = sum(a[1] for a in acc_e)
         rays, rays_e, samples = sum_over_ranks([rays, rays_e, samples], dev, world)
+        call_gbs = {}
+        for name in ("angelo_sdf_stencil_fwd", "angelo_sdf_stencil_bwd", "angelo_hashgrid_fwd",
+                     "angelo_hashgrid_bwd"):
+            if name in summ:
+                c_, t_, u_ = summ[name]
+                b_ = [algorithmic_bytes(name, u) for u in u_]
+                if all(x is not None for x in b_):
+                    call_gbs[name] = round(sum(b_) / (t_ * 1e-3) / 1e9, 1)
         results[form] = dict(
+            call_ms_per_step={k: round(v[1] / args.steps, 4) for k, v in summ.items()},
+            call_gbs=call_gbs,
             value=rays / (ms * 1e-3), ms_per_step=ms / args.steps, rays_per_step=rays / args.steps
             / world, samples_per_step=samples / args.steps / world, roofline=rl,
             pass_ms_per_step=[round(t / args.steps, 3) for t in pass_ms],
@@ -598,7 +616,9 @@ def run_ours(args):
                       "pass_ms_per_step": v["pass_ms_per_step"],
                       "e2e": v["e2e"]["value"], "e2e_ms_per_step": v["e2e"]["ms_per_step"],
                       "e2e_samples_per_step": v["e2e"]["samples_per_step"],
-                      "e2e_pass_ms_per_step": v["e2e_pass_ms_per_step"]}
+                      "e2e_pass_ms_per_step": v["e2e_pass_ms_per_step"],
+                      "call_ms_per_step": v["call_ms_per_step"],
+                      "call_algorithmic_gbs": v["call_gbs"]}
                   for f, v in results.items()},
     }
     if "fused" in results and "plain" in results:
@@ -879,12 +899,64 @@ def run_sdf_case(n):
     print(json.dumps({"sdf_case": n, "ok": True}), flush=True)
 
 
+def run_sdf_timing(steps, warmup):
+    """Median CUDA-event time of angelo_sdf_stencil_fwd and _bwd on a fixed
+    sample set: the march of 8192 camera rays (seeded) through the analytic
+    occupancy grid of the full workload, the model at the benchmark's state
+    with the table U(-0.05, 0.05) and the first layer's hash columns
+    N(0, 0.05^2).  The same work on every build, for comparing kernels."""
+    from angelo_gb import _lib, scenes
+    dev = torch.device("cuda:0")
+    model, tr = make_trainer("fused", dev)
+    model.update_step(0, GLOBAL_STEP)
+    g = model.geometry
+    with torch.no_grad():
+        gen = torch.Generator(device="cpu").manual_seed(7)
+        p = g.hashgrid.encoding.params
+        p.copy_((torch.rand(p.shape, generator=gen) * 0.1 - 0.05).to(dev))
+        wv = g.network.layers[0].weight_v
+        wv[:, 3:].copy_((torch.randn(wv[:, 3:].shape, generator=gen) * 0.05).to(dev))
+    poses = scenes.sphere_poses(N_VIEWS, CAM_R, 0).float().to(dev)
+    dirs = scenes.pixel_directions(W, H, FOV, device=dev).reshape(-1, 3)
+    rg = torch.Generator(device=dev).manual_seed(3)
+    pix = torch.randint(0, W * H, (MAX_RAYS,), device=dev, generator=rg)
+    cam = torch.randint(0, N_VIEWS, (MAX_RAYS,), device=dev, generator=rg)
+    rays = scenes.rays_from(dirs[pix], poses[cam]).contiguous()
+    model.randomized = False
+    o, d = rays[:, :3].contiguous(), rays[:, 3:].contiguous()
+    ri, t0, t1, _ = model.march_rays(o, d)
+    pos = (o[ri.long()] + d[ri.long()] * ((t0 + t1) * 0.5)[:, None]).contiguous()
+    n = pos.shape[0]
+    rd = torch.randn(n, 3, device=dev, generator=torch.Generator(device=dev).manual_seed(5))
+    g.curvature_dirs_fn = lambda t: rd
+    times = {"angelo_sdf_stencil_fwd": [], "angelo_sdf_stencil_bwd": []}
+    for it in range(warmup + steps):
+        g.zero_grad()
+        _lib.PROFILER.start()
+        sdf, grad, feat, lap = g(pos, True, True, True)
+        (sdf.sum() + grad.sum() + feat.sum() + lap.sum()).backward()
+        _lib.PROFILER.stop()
+        torch.cuda.synchronize(dev)
+        if it >= warmup:
+            for name, (c, ms, _) in _lib.PROFILER.summary().items():
+                if name in times:
+                    times[name].append(ms)
+    out = {"samples": n, "passes": steps}
+    for name, t in times.items():
+        out[name + "_ms"] = round(statistics.median(t), 4)
+        out[name + "_ns_per_sample"] = round(statistics.median(t) * 1e6 / n, 3)
+    print(json.dumps({"sdf_timing": out}), flush=True)
+
+
 def main():
     global MAX_RAYS
     args = parse()
     MAX_RAYS = args.max_rays
     if args.sdf_case:
         run_sdf_case(args.sdf_case)
+        return
+    if args.sdf_timing:
+        run_sdf_timing(args.steps, args.warmup)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -112,6 +112,8 @@ class _FusedSdf(torch.autograd.Function):
         work = torch.empty(workspace_floats(spec, S, with_grad, with_laplace, False), device=dev)
         rd = rand_dirs.contiguous() if rand_dirs is not None else None
         n_ev = 13 if with_laplace else (7 if with_grad else 1)
+        # the table the encode gathers from (an fp16 copy in the fp16-table form)
+        table = meta.get("table_fwd", table)
         call("angelo_sdf_stencil_fwd", ctypes.byref(spec.layout), int(active), _p(table),
              _table_dtype(table), ctypes.byref(fnet.layout), _p(fnet.buf), _p(pos), _p(rd), S,
              float(geom.radius), float(geom._finite_difference_eps or 1.0), int(with_grad),
@@ -255,6 +257,9 @@ def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
         weights += [W, b]
     table = geom.hashgrid.encoding.params
     prec = _precision(geom)
+    table_fwd = None
+    if getattr(geom, "fused_table_dtype", "fp32") == "fp16" and table.dtype == torch.float32:
+        table_fwd = table.detach().half()
     net.layout.mma_passes = 1 if prec == "bf16" else 3
     meta = dict(geom=geom, net=net, flags=(bool(with_grad), bool(with_laplace),
                                            bool(with_feature)))
@@ -262,6 +267,8 @@ def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
         fnet = _net_for(geom, _lib.OPERAND_FP16)
         fnet.layout.mma_passes = 1
         meta["net_fwd"] = fnet
+    if table_fwd is not None:
+        meta["table_fwd"] = table_fwd
     with torch.set_grad_enabled(geom.training and torch.is_grad_enabled()):
         sdf, grad, feature, lap = _FusedSdf.apply(pos, rd, table, meta, *weights)
     shp = points.shape[:-1]

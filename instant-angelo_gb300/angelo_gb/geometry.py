@@ -157,6 +157,11 @@ class VolumeSDF(nn.Module):
                 raise NotImplementedError(f"{k} is not used by the NeuS configs of the hot path")
         self.fused = bool(config.get("fused", False))
         self.fused_precision = config.get("fused_precision", "fp32")
+        # "fp16": the fused forward reads an fp16 copy of the (fp32) hash table,
+        # made once per pass; gradients still accumulate into the fp32 table
+        self.fused_table_dtype = config.get("fused_table_dtype", "fp32")
+        if self.fused_table_dtype not in ("fp32", "fp16"):
+            raise ValueError(f"fused_table_dtype {self.fused_table_dtype!r}: 'fp32' or 'fp16'")
         # torch.randn_like at models/geometry.py:238; replaceable for parity runs
         self.curvature_dirs_fn = torch.randn_like
         self.contraction_type = None

@@ -168,13 +168,15 @@ class NeuSModel(nn.Module):
         fused = bool(config.get("fused", False))
         config.geometry["fused"] = fused
         config.texture["fused"] = fused
-        if "fused_precision" in config:
-            config.geometry["fused_precision"] = config.fused_precision
+        for k in ("fused_precision", "fused_table_dtype"):
+            if k in config:
+                config.geometry[k] = config[k]
         self.fused = fused
         self.geometry = models.make(config.geometry.name, config.geometry)
         self.texture = models.make(config.texture.name, config.texture)
-        # "bf16": the forward MLPs of the fused kernels in one bf16 pass (the
-        # precision form); "fp32" (default): bf16x3
+        # forward MLP arithmetic of the fused kernels: "fp32" (default,
+        # bf16x3), "fp16" (one fp16 pass: the precision form) or "bf16" (one
+        # bf16 pass)
         self.texture.fused_precision = config.get("fused_precision", "fp32")
         self.geometry.contraction_type = "aabb"
         self.learned_background = bool(config.get("learned_background", False))

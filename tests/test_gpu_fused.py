@@ -236,3 +236,37 @@ def test_fused_composite_matches_plain(dev, name, inv_s_var):
     for name_, a, b in zip(("sdf", "grad", "rgb", "variance"), grads_f, grads_p):
         scale = max(np.abs(b).max(), 1e-6)
         assert np.abs(a - b).max() / scale < 2e-3, (name_, np.abs(a - b).max() / scale)
+
+
+def test_fp16_table_form_equals_fp32_table_with_rounded_values(dev):
+    """fused_table_dtype 'fp16': the encode gathers from an fp16 copy of the
+    fp32 table.  Every gathered value is then exactly its fp16 rounding, so
+    the outputs equal, bit for bit, the fp32-table form run on a table that
+    holds the rounded values, and so does the table gradient up to the
+    order of its atomic additions (the backward never reads the table)."""
+    from angelo_gb import models, workloads
+    torch.manual_seed(0)
+    a = models.make("neus", workloads.model_config("full", fused=True, fused_table_dtype="fp16")).to(dev)
+    b = models.make("neus", workloads.model_config("full", fused=True)).to(dev)
+    with torch.no_grad():
+        p = a.geometry.hashgrid.encoding.params
+        p.copy_((torch.rand(p.shape, generator=torch.Generator().manual_seed(3)) * 0.1 - 0.05).to(dev))
+        b.load_state_dict(a.state_dict())
+        b.geometry.hashgrid.encoding.params.copy_(p.half().float())
+    assert not torch.equal(a.geometry.hashgrid.encoding.params, b.geometry.hashgrid.encoding.params)
+    g = torch.Generator().manual_seed(4)
+    pts = ((torch.rand(5000, 3, generator=g) - 0.5) * 0.9).to(dev)
+    rd = torch.randn(5000, 3, generator=g).to(dev)
+    outs, grads = [], []
+    for m in (a, b):
+        m.update_step(0, 6000)
+        m.train()
+        m.geometry.curvature_dirs_fn = lambda t: rd
+        m.zero_grad()
+        sdf, grad, feat, lap = m.geometry(pts, with_grad=True, with_feature=True, with_laplace=True)
+        (sdf.square().sum() + grad.sum() + feat.sum() + lap.sum()).backward()
+        outs.append((sdf, grad, feat, lap))
+        grads.append(m.geometry.hashgrid.encoding.params.grad.clone())
+    for x, y in zip(*outs):
+        assert torch.equal(x, y)
+    torch.testing.assert_close(grads[0], grads[1], rtol=1e-5, atol=1e-9)
