@@ -156,7 +156,7 @@ class _FusedSdf(torch.autograd.Function):
              float(geom.radius), float(geom._finite_difference_eps or 1.0), int(with_grad),
              int(with_laplace), _p(work), _p(bwork), _p(gs), _p(gg), _p(gf),
              gf.stride(0) if gf is not None else 0, _p(gl), _p(d_table), _p(d_net), _s(dev),
-             launches=4 if with_laplace else 2,
+             launches=3 if with_laplace else 2,
              units=dict(n=S, od=net.out_dim, evals=n_ev, active=int(active),
                         levels=spec.layout.n_levels, tbytes=table.element_size(), train=True))
         grads = net.unpack_grads(d_net, ctx.in_dim)

@@ -11,24 +11,28 @@
 //                    computed exactly as encoding that tap alone (same cell,
 //                    fraction, weights and summation order).  Output: the
 //                    encodings X[e][l][s] (float2, level-major).
-//   sdf_mlp_fwd      warp per 16 samples: the geometry MLP of every evaluation
-//                    on tensor cores (bf16x3 split, fp32 accumulation) from X,
-//                    then the stencil arithmetic (sdf, FD gradient, tangent
-//                    shift, curvature) in fp32.
-//   sdf_mlp_bwd      warp per 16 samples: recomputes the activations from X,
+//   sdf_mlp_fwd      CTA of 16 warps per 128-sample tile: the geometry MLP of
+//                    every evaluation on tcgen05 tensor cores (bf16x3 split,
+//                    fp32 accumulation in tensor memory) from X, then the
+//                    stencil arithmetic (sdf, FD gradient, tangent shift,
+//                    curvature) in fp32.
+//   sdf_mlp_bwd      the same layout: recomputes the activations from X,
 //                    back-propagates the stencil arithmetic and the MLP and
-//                    writes dL/dX.  dL/dW is a GEMM whose reduction dimension
-//                    is the sample: each CTA stages 128 rows of (dZ, layer
-//                    input) in shared memory, every warp owns a slice of the
-//                    dW tiles and keeps it in registers for the whole kernel;
-//                    one atomic flush per CTA at the end.
+//                    writes dL/dX; dL/dW accumulates in tensor memory over the
+//                    CTA's tiles (one atomic flush per CTA).  The curvature
+//                    taps' pass also forms dL/d(shifted point): the xyz
+//                    columns and the hash grid's positional derivative, from
+//                    the Jacobian dX/dfrac the curvature encode kept.
 //   stencil_scatter  thread per (sample, level): dL/dtable of the taps with the
 //                    same corner sharing (one atomic per distinct corner, warp-
-//                    aggregated at coarse levels), and for the curvature taps
-//                    the hash grid's positional derivative into dL/d(shifted).
+//                    aggregated at coarse levels); both tap groups in one
+//                    launch.
 //
 // Order: forward   encode(FD) -> mlp_fwd(FD) -> encode(curv) -> mlp_fwd(curv)
-//        backward  mlp_bwd(curv) -> scatter(curv) -> mlp_bwd(FD) -> scatter(FD)
+//        backward  mlp_bwd(curv) -> mlp_bwd(FD) -> scatter(FD and curv, one launch)
+// (the curvature MLP backward takes the hash grid's positional derivative
+// of its taps from the Jacobian the curvature encode kept, so the FD pass
+// has dL/dshifted before the scatters run)
 #include <math.h>
 
 #include <algorithm>
@@ -624,7 +628,9 @@ struct TcBwdShape {
                               off_ds = off_vec + 3 * 64 * 4,                 // dL/dsdf [7][128]
                               off_db3 = off_ds + 7 * 128 * 4,
                               off_w3g = off_db3 + N3 * 4,                    // taps' dW3 row 0
-                              off_bar = off_w3g + 64 * 4, bytes = off_bar + 32;
+                              off_bar = off_w3g + 64 * 4,
+                              off_dsh = off_bar + 32,                        // dL/dshifted [128][3]
+                              bytes = off_dsh + 128 * 3 * 4;
     // tensor-memory columns: per evaluation A, B; CTA-resident gradients: dW1
     // and dW2 (+ bias sums) as M = 128 products, rows hi then lo units, columns
     // the operand's hi then lo (four blocks summed at the end); dW3^T (M = 64)
@@ -740,6 +746,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
     for (int i = tid; i < N3; i += kTcThreads) db3[i] = 0.f;
     float *w3g = reinterpret_cast<float *>(smem + Sh::off_w3g);
     for (int i = tid; i < 64; i += kTcThreads) w3g[i] = 0.f;
+    float *dsh_s = reinterpret_cast<float *>(smem + Sh::off_dsh);   // curvature: per-row dL/dshifted
+    for (int i = tid; i < 128 * 3; i += kTcThreads) dsh_s[i] = 0.f;
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem + Sh::off_bar);   // [0] epilogue, [1] round
     uint32_t *slot = reinterpret_cast<uint32_t *>(bar + 2);
     if (warp == 0) {
@@ -824,7 +832,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
         const int i = (int)(k % ne), e = e0 + i;
         const bool point = GROUP != kCurv && e == 0;
         int m = 7;
-        if (GROUP == kCurv && slice == 0) {
+        if (GROUP == kCurv) {
             // which coordinates of this tap passed the clamp (for dL/dshifted)
             float base[3], xc[3];
             const float *src = P.state + s * kState + 13;
@@ -974,17 +982,50 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
                 if (v && l < P.active) P.dX[xidx(P, e, l, s)] = make_float2(dx[2 * j], dx[2 * j + 1]);
             }
         }
-        if (GROUP == kCurv && slice == 0) {
-            // xyz columns x*2-1 to dL/dshifted; the scatter pass adds the hash
-            // grid's positional derivative atomically
-            float dx[8];
-            tc::ld8(tmem + lane_off + Sh::tB + 16 * KH, dx);
+        if (GROUP == kCurv) {
+            // dL/dshifted: the xyz columns x*2-1 (slice 0) and the hash grid's
+            // positional derivative dL/dX . dX/dfrac * scale of this slice's
+            // levels, from the Jacobian the forward encode kept; both
+            // through the clamp (mask m) and the contraction (1 / 2r)
+            if (slice == 0) {
+                float dx[8];
+                tc::ld8(tmem + lane_off + Sh::tB + 16 * KH, dx);
 #pragma unroll
-            for (int d = 0; d < 3; ++d)
-                if ((m >> d) & 1) dsh[d] += 2.f * dx[d] * inv2r;
-            if (i == ne - 1 && v) {
+                for (int d = 0; d < 3; ++d)
+                    if ((m >> d) & 1) dsh[d] += 2.f * dx[d] * inv2r;
+            }
+            if (v) {
+                constexpr int CPS = 4 * KH;
+                float dx[CPS];
+                tc::ldn(tmem + lane_off + Sh::tB + CPS * slice, dx);
+                const int k6 = e - 7;
 #pragma unroll
-                for (int d = 0; d < 3; ++d) P.bstate[s * kBState + d] = dsh[d];
+                for (int j = 0; j < CPS / 2; ++j) {
+                    const int l = (CPS / 2) * slice + j;
+                    if (l >= P.active) continue;
+                    const float sc = P.lay.scales[l] * inv2r;
+#pragma unroll
+                    for (int dd = 0; dd < 3; ++dd) {
+                        if (!((m >> dd) & 1)) continue;
+                        const float2 jv = __ldg(P.J + ((int64_t)(k6 * P.lay.n_levels + l) * 3 + dd) * P.S + s);
+                        dsh[dd] += sc * (dx[2 * j] * jv.x + dx[2 * j + 1] * jv.y);
+                    }
+                }
+            }
+            if (i == ne - 1) {
+                // the four slices of a row add up in shared memory
+                if (v) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) atomicAdd(dsh_s + row * 3 + d, dsh[d]);
+                }
+                __syncthreads();
+                if (slice == 0) {
+#pragma unroll
+                    for (int d = 0; d < 3; ++d) {
+                        if (v) P.bstate[s * kBState + d] = dsh_s[row * 3 + d];
+                        dsh_s[row * 3 + d] = 0.f;
+                    }
+                }
             }
         }
     }
@@ -1040,9 +1081,10 @@ __device__ __forceinline__ void centre_add(float2 (&acc)[8], int delta, int cc, 
     acc[o].y += z ? 0.f : v.y;
 }
 
+// dL/dtable of one (sample, level) of tap group GROUP: thread (blockIdx.x,
+// threadIdx.x) = sample, blockIdx.y = level
 template <int GROUP>
-__global__ void __launch_bounds__(kEncThreads, ANGELO_SCATTER_MIN_BLOCKS)
-    stencil_scatter_kernel(const __grid_constant__ SdfParams P) {
+__device__ __forceinline__ void scatter_body(const SdfParams &P) {
     const int l = blockIdx.y;
     const int64_t s = (int64_t)blockIdx.x * kEncThreads + threadIdx.x;
     const bool valid = s < P.S;
@@ -1059,7 +1101,6 @@ __global__ void __launch_bounds__(kEncThreads, ANGELO_SCATTER_MIN_BLOCKS)
     float2 acc[8];
 #pragma unroll
     for (int cc = 0; cc < 8; ++cc) acc[cc] = make_float2(0.f, 0.f);
-    float dsh[3] = {0.f, 0.f, 0.f};
     if (GROUP != kCurv) {
         const float2 gx = valid ? P.dX[xidx(P, 0, l, s)] : make_float2(0.f, 0.f);
         const bool live = valid && (gx.x != 0.f || gx.y != 0.f);
@@ -1099,22 +1140,7 @@ __global__ void __launch_bounds__(kEncThreads, ANGELO_SCATTER_MIN_BLOCKS)
                 if (corner_shared(aligned, delta, cc, d)) centre_add(acc, delta, cc, d, v);
                 else if (live && dt) atomicAdd(dt + off + corner_index(P.lay, l, p, cc), v);
             }
-            if (GROUP == kCurv && live) {
-                // positional derivative of the interpolation: dL/dX . dX/dfrac,
-                // the Jacobian kept by the forward encode
-#pragma unroll
-                for (int dd = 0; dd < 3; ++dd) {
-                    const float2 jv = P.J[((int64_t)(k * P.lay.n_levels + l) * 3 + dd) * P.S + s];
-                    if ((m >> dd) & 1) dsh[dd] += sc * (gx.x * jv.x + gx.y * jv.y);
-                }
-            }
         }
-    }
-    if (GROUP == kCurv && valid) {
-        const float inv2r = 1.0f / __fsub_rn(r, -r);
-#pragma unroll
-        for (int dd = 0; dd < 3; ++dd)
-            if (dsh[dd] != 0.f) atomicAdd(P.bstate + s * kBState + dd, dsh[dd] * inv2r);
     }
     if (dt) {
         const bool coarse = P.lay.resolutions[l] <= kAggregateRes;
@@ -1126,6 +1152,22 @@ __global__ void __launch_bounds__(kEncThreads, ANGELO_SCATTER_MIN_BLOCKS)
             else if (nz) atomicAdd(dt + ent, acc[cc]);
         }
     }
+}
+
+
+template <int GROUP>
+__global__ void __launch_bounds__(kEncThreads, ANGELO_SCATTER_MIN_BLOCKS)
+    stencil_scatter_kernel(const __grid_constant__ SdfParams P) {
+    scatter_body<GROUP>(P);
+}
+
+// Both tap groups in one launch: blockIdx.z 0 = the point and its FD taps,
+// 1 = the curvature taps (their scatters are independent once the
+// curvature taps' positional derivative is taken in their MLP backward)
+__global__ void __launch_bounds__(kEncThreads, ANGELO_SCATTER_MIN_BLOCKS)
+    stencil_scatter_both_kernel(const __grid_constant__ SdfParams P) {
+    if (blockIdx.z == 0) scatter_body<kFD>(P);
+    else scatter_body<kCurv>(P);
 }
 
 }  // namespace
@@ -1202,9 +1244,16 @@ int launch_encode(const SdfParams &P, cudaStream_t s) {
 
 template <int GROUP>
 int launch_scatter(const SdfParams &P, cudaStream_t s) {
-    if (P.active == 0 || (GROUP != kCurv && P.d_table == nullptr)) return ANGELO_OK;
+    if (P.active == 0 || P.d_table == nullptr) return ANGELO_OK;
     const dim3 grid((unsigned)((P.S + kEncThreads - 1) / kEncThreads), (unsigned)P.active);
     stencil_scatter_kernel<GROUP><<<grid, kEncThreads, 0, s>>>(P);
+    return check_launch("sdf_stencil_scatter");
+}
+
+int launch_scatter_both(const SdfParams &P, cudaStream_t s) {
+    if (P.active == 0 || P.d_table == nullptr) return ANGELO_OK;
+    const dim3 grid((unsigned)((P.S + kEncThreads - 1) / kEncThreads), (unsigned)P.active, 2);
+    stencil_scatter_both_kernel<<<grid, kEncThreads, 0, s>>>(P);
     return check_launch("sdf_stencil_scatter");
 }
 
@@ -1267,8 +1316,12 @@ template <int KH, int NH, int NT3>
 int run_bwd(const SdfParams &P, cudaStream_t s) {
     int rc;
     if (P.with_laplace) {
+        // the curvature taps' MLP backward leaves dL/dshifted (with the hash
+        // grid's positional derivative) for the FD pass; both groups' table
+        // scatters then run as one launch
         if ((rc = launch_mlp_bwd<KH, NH, NT3, kCurv>(P, s)) != ANGELO_OK) return rc;
-        if ((rc = launch_scatter<kCurv>(P, s)) != ANGELO_OK) return rc;
+        if ((rc = launch_mlp_bwd<KH, NH, NT3, kFD>(P, s)) != ANGELO_OK) return rc;
+        return launch_scatter_both(P, s);
     }
     if (P.with_grad) {
         if ((rc = launch_mlp_bwd<KH, NH, NT3, kFD>(P, s)) != ANGELO_OK) return rc;
