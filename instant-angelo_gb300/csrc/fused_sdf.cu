@@ -994,7 +994,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
                 for (int d = 0; d < 3; ++d)
                     if ((m >> d) & 1) dsh[d] += 2.f * dx[d] * inv2r;
             }
-            if (v) {
+            {
+                // tcgen05.ld is warp-collective: every lane loads, only the
+                // rows of valid samples use the values
                 constexpr int CPS = 4 * KH;
                 float dx[CPS];
                 tc::ldn(tmem + lane_off + Sh::tB + CPS * slice, dx);
@@ -1002,7 +1004,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
 #pragma unroll
                 for (int j = 0; j < CPS / 2; ++j) {
                     const int l = (CPS / 2) * slice + j;
-                    if (l >= P.active) continue;
+                    if (!v || l >= P.active) continue;
                     const float sc = P.lay.scales[l] * inv2r;
 #pragma unroll
                     for (int dd = 0; dd < 3; ++dd) {
