@@ -358,7 +358,27 @@ def algorithmic_bytes(name, u):
 TRAFFIC_BYTES_PER_SAMPLE = {"angelo_sdf_stencil_bwd": 2.479e9 / 284088}
 
 
-def roofline(summary, hbm_peak, peak_kind):
+def mlp_flops(name, u):
+    """Algorithmic tensor-core FLOPs of the geometry MLP inside one fused
+    VolumeSDF call (the per-unit figures of the hot-path measurement plan:
+    the point 2(35*64 + 64*64 + 64*65), a stencil tap 2(35*64 + 64*64 + 64)
+    for the 16-level model); the backward recomputes the forward and runs the
+    two backward products (dX and dW): 3x the forward."""
+    if u is None or name not in ("angelo_sdf_stencil_fwd", "angelo_sdf_stencil_bwd"):
+        return None
+    if u.get("levels") != 16:
+        return None
+    point, tap = 2 * (35 * 64 + 64 * 64 + 64 * 65), 2 * (35 * 64 + 64 * 64 + 64)
+    fwd = point + (u["evals"] - 1) * tap
+    return u["n"] * fwd * (3 if name == "angelo_sdf_stencil_bwd" else 1)
+
+
+# tensor-pipe activity of the backward MLP kernels, from the ncu capture of
+# the 65,536-point case (sm__pipe_tensor_cycles_active, both tap groups)
+TENSOR_PIPE_ACTIVE = {"angelo_sdf_stencil_bwd": 0.11}
+
+
+def roofline(summary, hbm_peak, peak_kind, tensor_peak=None):
     best = None
     for name, (calls, ms, units) in summary.items():
         if best is None or ms > best[2]:
@@ -382,12 +402,28 @@ def roofline(summary, hbm_peak, peak_kind):
     traffic = None
     if name in TRAFFIC_BYTES_PER_SAMPLE:
         traffic = int(TRAFFIC_BYTES_PER_SAMPLE[name] * sum(u["n"] for u in units) / calls)
-    return {"kernel": name, "bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_peak,
-            "unit": "GB/s", "frac": round(gbs / hbm_peak, 4), "traffic": traffic,
-            "traffic_source": "ncu DRAM bytes per sample of this call on the full step, "
-            "times the launch's samples" if traffic else None,
-            "bytes_per_launch": int(total_bytes / calls), "launches": calls,
-            "ms_per_launch": round(ms / calls, 4), "peak_source": peak_kind}, shares
+    out = {"kernel": name, "bound": "hbm", "achieved": round(gbs, 1), "peak": hbm_peak,
+           "unit": "GB/s", "frac": round(gbs / hbm_peak, 4), "traffic": traffic,
+           "traffic_source": "ncu DRAM bytes per sample of this call on the full step, "
+           "times the launch's samples" if traffic else None,
+           "bytes_per_launch": int(total_bytes / calls), "launches": calls,
+           "ms_per_launch": round(ms / calls, 4), "peak_source": peak_kind}
+    if name == "angelo_sdf_stencil_bwd":
+        # the measured limiters of the call's kernels: the table scatter's L2
+        # atomics and the tcgen05 MLP backward's epilogue issue (not HBM
+        # bandwidth: its DRAM traffic is a third of the algorithmic bytes)
+        out["limiter"] = ("L2 atomics (table scatter) and instruction issue of the tensor-core "
+                          "MLP epilogue; DRAM traffic ~1/3 of the algorithmic bytes")
+        fl = [mlp_flops(name, u) for u in units]
+        if tensor_peak and all(f is not None for f in fl):
+            tf = sum(fl) / (ms * 1e-3) / 1e12
+            out["tensor"] = {"achieved": round(tf, 2), "peak": tensor_peak, "unit": "TFLOP/s",
+                             "frac": round(tf / tensor_peak, 4),
+                             "flops_per_launch": int(sum(fl) / calls),
+                             "pipe_active_ncu": TENSOR_PIPE_ACTIVE.get(name),
+                             "note": "useful MLP FLOPs (one bf16 product each) over the whole "
+                                     "call's time; the bf16x3 form issues ~3x as many"}
+    return out, shares
 
 
 # -------------------------------------------------------------- CPU baseline
@@ -480,7 +516,7 @@ def run_ours(args):
     views = make_views(dev)
     forms = available_forms() if args.forms == "auto" else args.forms.split(",")
     results = {}
-    hbm_peak, _, peak_kind = measured_peaks()
+    hbm_peak, tensor_peak, peak_kind = measured_peaks()
     for form in forms:
         model, tr = make_trainer(form, dev)
         # every measured pass starts from the same state: the model's
@@ -538,7 +574,7 @@ def run_ours(args):
         launches = _lib.PROFILER.launches
         rays = sum(a[0] for a in acc)
         samples = sum(a[1] for a in acc)
-        rl, shares = roofline(summ, hbm_peak, peak_kind)
+        rl, shares = roofline(summ, hbm_peak, peak_kind, tensor_peak)
         # host-fed end-to-end through the public API; median of E2E_PASSES
         # passes, each from the same state with the same host batches
         runs_e = []
