@@ -64,6 +64,10 @@ constexpr int kEncThreads = 128;
 #ifndef ANGELO_SCATTER_MIN_BLOCKS
 #define ANGELO_SCATTER_MIN_BLOCKS 8
 #endif
+// both tap groups' table scatters in one launch (1) or one launch each (0)
+#ifndef ANGELO_SCATTER_MERGED
+#define ANGELO_SCATTER_MERGED 1
+#endif
 constexpr int kState = 16;      // per sample: sdf of the 13 evaluations, shifted point (3)
 constexpr int kBState = 8;      // per sample, backward: dL/dshifted (3), dL/dnormal from curvature (3)
 constexpr uint32_t kAggregateRes = 300;  // levels up to this resolution aggregate their atomics
@@ -163,6 +167,8 @@ struct SdfParams {
     float2 *J;        // curvature taps: d(encoding)/d(cell fraction),
                       // J[((k * n_levels + l) * 3 + axis) * S + s], k = tap 0..5
     float *state;     // (S, kState): sdf of the 13 evaluations, shifted point
+    int32_t *perm;    // curvature pass: sample order by dead-tap pattern (may be null)
+    int32_t *perm_blk;  // its per-block bucket counts (8 x ceil(S / 256))
     // backward inputs
     const float *g_sdf, *g_grad, *g_feature, *g_laplace;
     int64_t gfeat_stride;
@@ -248,6 +254,93 @@ __device__ __forceinline__ bool corner_shared(bool aligned, int delta, int cc, i
 __device__ __forceinline__ float2 centre_value(const float2 (&vc)[8], int delta, int cc, int d) {
     const float2 other = ((cc >> d) & 1) == 0 ? vc[cc | (1 << d)] : vc[cc & ~(1 << d)];
     return delta == 0 ? vc[cc] : other;
+}
+
+// ------------------------------------------- curvature pass: dead tap pairs
+// The curvature stencil is evaluated at contracted coordinates treated as
+// world coordinates (models/geometry.py:246,264-265), so on every axis where
+// the shifted point lies beyond r + eps both taps clamp to the same point:
+// their SDFs are equal (the FD difference is exactly 0) and their backward
+// contributions are 0.  The curvature pass orders its samples by that
+// dead-axis pattern (a stable partition into 8 buckets), so that whole
+// 128-sample tiles share it and the MLP kernels skip a tap whose pair is dead
+// on every row of the tile; results are unchanged.
+
+constexpr int kPermThreads = 256;
+
+__device__ __forceinline__ int dead_pattern(const SdfParams &P, int64_t s) {
+    const float *st = P.state + s * kState + 13;
+    int p = 0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) p |= (int)coincident_taps(st[d], P.radius, P.eps) << d;
+    return p;
+}
+
+// per block of kPermThreads samples: the count of each pattern,
+// blk[pattern * nblk + block]
+__global__ void __launch_bounds__(kPermThreads) perm_count_kernel(const __grid_constant__ SdfParams P, int nblk) {
+    const int64_t s = (int64_t)blockIdx.x * kPermThreads + threadIdx.x;
+    const int p = s < P.S ? dead_pattern(P, s) : -1;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const int c = __syncthreads_count(p == b);
+        if (threadIdx.x == 0) P.perm_blk[b * nblk + blockIdx.x] = c;
+    }
+}
+
+// one block: exclusive prefix sum of the counts in pattern-major order
+__global__ void __launch_bounds__(1024) perm_scan_kernel(int32_t *blk, int total) {
+    __shared__ int32_t wsum[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int32_t carry = 0;
+    for (int base = 0; base < total; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int32_t v = i < total ? blk[i] : 0;
+        int32_t x = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) wsum[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            int32_t w = wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            wsum[lane] = w;
+        }
+        __syncthreads();
+        const int32_t before = (warp > 0 ? wsum[warp - 1] : 0) + x - v;
+        if (i < total) blk[i] = carry + before;
+        carry += wsum[31];
+        __syncthreads();
+    }
+}
+
+// position of each sample: its pattern's base in this block + its rank among
+// the block's samples of that pattern (in sample order)
+__global__ void __launch_bounds__(kPermThreads) perm_write_kernel(const __grid_constant__ SdfParams P, int nblk) {
+    __shared__ int32_t wcnt[8][kPermThreads / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int64_t s = (int64_t)blockIdx.x * kPermThreads + threadIdx.x;
+    const int p = s < P.S ? dead_pattern(P, s) : -1;
+    int rank = 0;
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+        const unsigned m = __ballot_sync(0xffffffffu, p == b);
+        if (lane == 0) wcnt[b][warp] = __popc(m);
+        if (p == b) rank = __popc(m & ((1u << lane) - 1u));
+    }
+    __syncthreads();
+    if (p >= 0) {
+        int32_t off = P.perm_blk[p * nblk + blockIdx.x] + rank;
+        for (int w = 0; w < warp; ++w) off += wcnt[p][w];
+        P.perm[off] = (int32_t)s;
+    }
 }
 
 // ---------------------------------------------------------------- encode
@@ -419,7 +512,13 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
     const int64_t n_tiles = (P.S + 127) / 128;
     const int64_t my_tiles = (int64_t)blockIdx.x < n_tiles ? (n_tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     const int64_t n_items = my_tiles * ne;
-    auto item_sample = [&](int64_t k) { return (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row; };
+    // position k of the pass -> sample (the curvature pass visits its samples
+    // in P.perm's order); positions past S are padding rows
+    auto item_pos = [&](int64_t k) { return (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row; };
+    auto item_sample = [&](int64_t k) {
+        const int64_t pk = item_pos(k);
+        return (GROUP == kCurv && P.perm && pk < P.S) ? (int64_t)P.perm[pk] : pk;
+    };
     auto item_base = [&](int64_t sk, float b[3]) {
         const bool vk = sk < P.S;
         const float *src = GROUP == kCurv ? P.state + sk * kState + 13 : P.pos + sk * 3;
@@ -463,7 +562,15 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
         int m;
         item_base(s, base);
         tap_point(r_, eps, base, e, xc, &m);
-        {
+        // a curvature tap whose pair is dead on every row of the tile: its
+        // SDF is the same for both taps, any value will do (0)
+        bool skip = false;
+        if (GROUP == kCurv)
+            skip = !__syncthreads_or(v && !coincident_taps(base[(e - 7) >> 1], r_, eps));
+        if (skip) {
+            if (k + 1 < n_items) stage_x(k + 1);
+            if (slice == 0) s13[e * 128 + row] = 0.f;
+        } else {
             tc_publish();
             if (tid == 0) {
                 tc_mma_p<K1 / 16>(tmem, op_k(sA1h, Sh::a1, K1), op_k(sW1h, Sh::w1, K1), id_hidden, false,
@@ -802,8 +909,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
     constexpr int kDsSlice = 3;   // slice that runs a tile's ds prologue (stages no input)
     // layer-1 operand of item k (slice q < KH: hash levels 8q .. 8q + 7; slice
     // KH: xyz) into registers; issued two rounds before it is staged
+    // position k of the pass -> sample (the curvature pass in P.perm's order)
+    auto item_sample = [&](int64_t k) {
+        const int64_t pk = (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row;
+        return (GROUP == kCurv && P.perm && pk < P.S) ? (int64_t)P.perm[pk] : pk;
+    };
     auto load_x = [&](int64_t k, float (&xv)[16]) {
-        const int64_t s = (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row;
+        const int64_t s = item_sample(k);
         const bool v = s < P.S;
         const int e = e0 + (int)(k % ne);
 #pragma unroll
@@ -830,12 +942,30 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
     };
     float xv[16];
     if (n_items > 0) load_x(0, xv);
+    // after a tile's last curvature tap: the four slices of a row add their
+    // dL/dshifted up in shared memory and slice 0 stores it
+    auto curv_tail = [&](int64_t s, bool v) {
+        if (v) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) atomicAdd(dsh_s + row * 3 + d, dsh[d]);
+        }
+        __syncthreads();
+        if (slice == 0) {
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                if (v) P.bstate[s * kBState + d] = dsh_s[row * 3 + d];
+                dsh_s[row * 3 + d] = 0.f;
+            }
+        }
+    };
+    bool pending1 = false;   // weight-gradient products committed to bar[1], not yet waited for
     for (int64_t k = 0; k < n_items; ++k) {
-        const int64_t s = (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row;
+        const int64_t s = item_sample(k);
         const bool v = s < P.S;
         const int i = (int)(k % ne), e = e0 + i;
         const bool point = GROUP != kCurv && e == 0;
         int m = 7;
+        bool dead = false;
         if (GROUP == kCurv) {
             // which coordinates of this tap passed the clamp (for dL/dshifted)
             float base[3], xc[3];
@@ -843,10 +973,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
 #pragma unroll
             for (int d = 0; d < 3; ++d) base[d] = v ? src[d] : 0.f;
             tap_point(r_, eps, base, e, xc, &m);
+            dead = !v || coincident_taps(base[(e - 7) >> 1], r_, eps);
         }
-        if (k > 0) {
+        if (pending1) {
             if (!(alive = tc_wait_all(&bar[1], ph1))) break;
             ph1 ^= 1;
+            pending1 = false;
         }
         if (slice <= KH) stage16_2(xs, row, 16 * slice, K1, Sh::CX, xv);
         if (i == 0) {
@@ -883,6 +1015,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             }
         }
         tc_publish();
+        if (GROUP == kCurv && !__syncthreads_or(!dead)) {
+            // the tap's pair is dead on every row: no contribution (its dL/dX
+            // is not written; the scatter skips dead taps the same way)
+            if (k + 1 < n_items) load_x(k + 1, xv);
+            if (i == ne - 1) curv_tail(s, v);
+            continue;
+        }
         // stage 1: Z1 (one hidden layer, point: also dH1 = dY W3)
         if (tid == 0) {
             tc_mma<K1 / 16>(tmem + Sh::tA, Xk, W1k, id_fwd, false);
@@ -973,6 +1112,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             if (NH == 1 && point) tc_mma<8>(tmem + Sh::tW3, HLt, Yt, id_w3, true);
             tc::commit(&bar[1]);
         }
+        pending1 = true;
         if (!(alive = tc_wait_all(&bar[0], ph0))) break;
         ph0 ^= 1;
         {
@@ -1018,24 +1158,10 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
                     }
                 }
             }
-            if (i == ne - 1) {
-                // the four slices of a row add up in shared memory
-                if (v) {
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) atomicAdd(dsh_s + row * 3 + d, dsh[d]);
-                }
-                __syncthreads();
-                if (slice == 0) {
-#pragma unroll
-                    for (int d = 0; d < 3; ++d) {
-                        if (v) P.bstate[s * kBState + d] = dsh_s[row * 3 + d];
-                        dsh_s[row * 3 + d] = 0.f;
-                    }
-                }
-            }
+            if (i == ne - 1) curv_tail(s, v);
         }
     }
-    if (alive && n_items > 0) alive = tc_wait_all(&bar[1], ph1);
+    if (alive && pending1) alive = tc_wait_all(&bar[1], ph1);
     if (alive) {
         // add the CTA's gradients.  dW1, dW2: lane r = row r of an M = 128
         // product (unit r % 64, hi rows then lo rows), column = operand column
@@ -1132,6 +1258,9 @@ __device__ __forceinline__ void scatter_body(const SdfParams &P) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             const int d = k >> 1;
+            // a curvature tap whose pair is dead contributes nothing (and its
+            // dL/dX is not written when its whole tile was dead)
+            if (GROUP == kCurv && coincident_taps(base[d], r, eps)) continue;
             const float2 gx = valid ? P.dX[xidx(P, e0 + k, l, s)] : make_float2(0.f, 0.f);
             const bool live = valid && (gx.x != 0.f || gx.y != 0.f);
             float xc[3];
@@ -1240,6 +1369,24 @@ constexpr int kSmallKH = 1, kSmallNH = 1, kSmallNT3 = 2;   // 8 levels, 1 hidden
 constexpr int kFullKH = 2, kFullNH = 2, kFullNT3 = 9;      // 16 levels, 2 hidden layers, 65 outputs
 
 
+int64_t perm_blocks(int64_t n) { return (n + kPermThreads - 1) / kPermThreads; }
+
+// the curvature pass's sample order, in the forward workspace after the
+// Jacobians
+void set_perm(SdfParams &P, float *workspace, int64_t n, int levels) {
+    float *p = workspace + 2 * 13 * (int64_t)levels * n + kState * n + 2 * 6 * 3 * (int64_t)levels * n;
+    P.perm = reinterpret_cast<int32_t *>(p);
+    P.perm_blk = P.perm + n;
+}
+
+int launch_perm(const SdfParams &P, cudaStream_t s) {
+    const int nblk = (int)perm_blocks(P.S);
+    perm_count_kernel<<<nblk, kPermThreads, 0, s>>>(P, nblk);
+    perm_scan_kernel<<<1, 1024, 0, s>>>(P.perm_blk, 8 * nblk);
+    perm_write_kernel<<<nblk, kPermThreads, 0, s>>>(P, nblk);
+    return check_launch("sdf_curvature_order");
+}
+
 template <int GROUP>
 int launch_encode(const SdfParams &P, cudaStream_t s) {
     if (P.active == 0) return ANGELO_OK;
@@ -1313,6 +1460,7 @@ int run_fwd(const SdfParams &P, cudaStream_t s) {
     }
     if (P.with_laplace) {
         if ((rc = launch_encode<kCurv>(P, s)) != ANGELO_OK) return rc;
+        if ((rc = launch_perm(P, s)) != ANGELO_OK) return rc;
         if ((rc = launch_mlp_fwd<KH, NH, NT3, kCurv>(P, s)) != ANGELO_OK) return rc;
     }
     return ANGELO_OK;
@@ -1327,7 +1475,12 @@ int run_bwd(const SdfParams &P, cudaStream_t s) {
         // scatters then run as one launch
         if ((rc = launch_mlp_bwd<KH, NH, NT3, kCurv>(P, s)) != ANGELO_OK) return rc;
         if ((rc = launch_mlp_bwd<KH, NH, NT3, kFD>(P, s)) != ANGELO_OK) return rc;
+#if ANGELO_SCATTER_MERGED
         return launch_scatter_both(P, s);
+#else
+        if ((rc = launch_scatter<kFD>(P, s)) != ANGELO_OK) return rc;
+        return launch_scatter<kCurv>(P, s);
+#endif
     }
     if (P.with_grad) {
         if ((rc = launch_mlp_bwd<KH, NH, NT3, kFD>(P, s)) != ANGELO_OK) return rc;
@@ -1347,6 +1500,7 @@ bool shape_full(const angelo_sdf_net_layout &nl) {
 
 int64_t n_evals(int with_grad, int with_laplace) { return with_laplace ? 13 : (with_grad ? 7 : 1); }
 
+
 }  // namespace
 
 extern "C" int64_t angelo_sdf_workspace_floats(const angelo_hashgrid_layout_t *lay, int64_t n,
@@ -1354,7 +1508,11 @@ extern "C" int64_t angelo_sdf_workspace_floats(const angelo_hashgrid_layout_t *l
                                                int32_t backward) {
     if (lay == nullptr || n < 0 || lay->n_levels < 1 || lay->n_levels > ANGELO_MAX_LEVELS) return -1;
     const int64_t x = 2 * n_evals(with_grad, with_laplace) * lay->n_levels * n;
-    const int64_t j = (with_laplace && !backward) ? 2 * 6 * 3 * (int64_t)lay->n_levels * n : 0;
+    // the curvature taps' Jacobians and the curvature pass's sample order
+    // (int32 per sample + 8 counts per 256 samples)
+    const int64_t j = (with_laplace && !backward)
+                          ? 2 * 6 * 3 * (int64_t)lay->n_levels * n + n + 8 * perm_blocks(n)
+                          : 0;
     return x + (backward ? kBState : kState) * n + j;
 }
 
@@ -1406,6 +1564,7 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
     P.X = reinterpret_cast<float2 *>(workspace);
     P.state = workspace + 2 * n_evals(with_grad, with_laplace) * lay->n_levels * n;
     P.J = with_laplace ? reinterpret_cast<float2 *>(P.state + kState * n) : nullptr;
+    if (with_laplace) set_perm(P, workspace, n, lay->n_levels);
     cudaStream_t s = as_stream(stream);
     if (shape_full(*nl)) return run_fwd<kFullKH, kFullNH, kFullNT3>(P, s);
     if (shape_small(*nl)) return run_fwd<kSmallKH, kSmallNH, kSmallNT3>(P, s);
@@ -1476,6 +1635,7 @@ extern "C" int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32
     P.X = reinterpret_cast<float2 *>(const_cast<float *>(workspace));
     P.state = const_cast<float *>(workspace) + x;
     P.J = with_laplace ? reinterpret_cast<float2 *>(P.state + kState * n) : nullptr;
+    if (with_laplace) set_perm(P, const_cast<float *>(workspace), n, lay->n_levels);
     P.dX = reinterpret_cast<float2 *>(bwd_workspace);
     P.bstate = bwd_workspace + x;
     P.g_sdf = g_sdf;
