@@ -437,16 +437,107 @@ int angelo_radiance_prep_format(int32_t feat_dim, int32_t operand_format, const 
  * feature[1:4] when dual), d = rays_d[ray_idx].  flags bit 0: dual colour;
  * bit 1: the MLP in a single pass (hi parts alone) instead of three
  * products; bit 2: fp16 operands (a buffer from angelo_radiance_prep_format
- * with ANGELO_OPERAND_FP16) instead of bf16. */
+ * with ANGELO_OPERAND_FP16) instead of bf16.  grad may be NULL: a network
+ * without a normal input (VolumeRadiance on [feature, SH4], the learned
+ * background's texture), whose W1 normal columns the caller sets to zero. */
 int angelo_radiance_fwd(int32_t feat_dim, const void *net, const float *feature,
                         int64_t feat_stride, const float *grad, const int32_t *ray_idx,
                         const float *rays_d, int64_t n, int32_t flags, float *rgb, void *stream);
-/* Backward: d_feature (written, n x feat_stride), d_grad (written, n x 3),
- * d_net (accumulated). */
+/* Backward: d_feature (written, n x feat_stride), d_grad (written, n x 3;
+ * NULL exactly when grad is NULL), d_net (accumulated). */
 int angelo_radiance_bwd(int32_t feat_dim, const void *net, const float *feature,
                         int64_t feat_stride, const float *grad, const int32_t *ray_idx,
                         const float *rays_d, int64_t n, int32_t dual, const float *g_rgb,
                         float *d_feature, float *d_grad, float *d_net, void *stream);
+
+/* ------------------------------------------------------------ fused VanillaMLP */
+
+/* VanillaMLP with ReLU between layers and no output activation
+ * (models/network_utils.py:96-140 as the learned background's density
+ * network uses it, models/geometry.py:152-177): in_dim (1..64) inputs,
+ * n_hidden (1 or 2) hidden layers of 64, out_dim (1..16) outputs, on the
+ * tensor cores (bf16x3 operands, fp32 accumulation).  Bytes of the prepared
+ * buffer; -1 when the shape is unsupported. */
+int64_t angelo_mlp_net_bytes(int32_t in_dim, int32_t n_hidden, int32_t out_dim);
+/* Floats of the flat weight gradient: [dW1 (64 x 16*ceil(in_dim/16)),
+ * dW2 (64 x 64, two hidden layers), dW3 (16 x 64), db1 (64), db2 (64, two
+ * hidden layers), db3 (16)]; -1 when unsupported. */
+int64_t angelo_mlp_grad_size(int32_t in_dim, int32_t n_hidden, int32_t out_dim);
+/* fp32 weights (row-major [out][in], as nn.Linear keeps them; W2, b2 may be
+ * NULL with one hidden layer) -> prepared buffer. */
+int angelo_mlp_prep(int32_t in_dim, int32_t n_hidden, int32_t out_dim, const float *W1,
+                    const float *b1, const float *W2, const float *b2, const float *W3,
+                    const float *b3, void *net, void *stream);
+/* out[i] (out_dim columns, row stride out_stride) = MLP(x[i]) (in_dim
+ * columns, row stride x_stride) for n rows (replaces the torch / tcnn
+ * network call of models/network_utils.py:134-140). */
+int angelo_mlp_fused_fwd(int32_t in_dim, int32_t n_hidden, int32_t out_dim, const void *net,
+                         const float *x, int64_t x_stride, int64_t n, float *out,
+                         int64_t out_stride, void *stream);
+/* Backward from dL/dout (g_out, row stride g_stride): writes dL/dx (d_x, row
+ * stride dx_stride; may be NULL) and ACCUMULATES dL/dW into d_net
+ * (angelo_mlp_grad_size floats).  The hidden activations are recomputed
+ * from x. */
+int angelo_mlp_fused_bwd(int32_t in_dim, int32_t n_hidden, int32_t out_dim, const void *net,
+                         const float *x, int64_t x_stride, int64_t n, const float *g_out,
+                         int64_t g_stride, float *d_x, int64_t dx_stride, float *d_net,
+                         void *stream);
+
+/* ------------------------------------------------------------------ serving */
+
+/* The resident field a server renders: device pointers owned by the caller
+ * and left unchanged while the server lives (hash table; SDF MLP prepared by
+ * angelo_sdf_prep; radiance MLP prepared by angelo_radiance_prep; occupancy
+ * bits).  This is the trained NeuSModel the reference's eval path renders
+ * (models/neus.py:285-293). */
+typedef struct {
+    angelo_hashgrid_layout_t lay;
+    int32_t active_levels;
+    const void *table;
+    int32_t table_dtype;
+    angelo_sdf_net_layout sdf_layout;
+    const void *sdf_net;
+    float radius;
+    float eps;                 /* finite-difference step of the normal */
+    int32_t feat_dim;          /* radiance feature width = sdf out_dim + 3 */
+    const void *rad_net;
+    int32_t rad_flags;         /* angelo_radiance_fwd flags (bit 0: dual colour) */
+    const float *variance;     /* device float: inv_s = exp(10 variance) */
+    float cos_anneal_ratio;
+    const float *background;   /* device float[3], blended behind each ray */
+    angelo_grid_t grid;        /* occupancy grid of the march */
+    float render_step;
+    int32_t max_steps;
+    float near_plane;          /* near / far planes; both < 0: the scene box */
+    float far_plane;           /* [-radius, radius]^3 (one < 0: that plane unset) */
+} angelo_serve_field;
+
+/* sizeof(angelo_serve_field), for bindings that mirror the struct. */
+int64_t angelo_serve_field_bytes(void);
+
+typedef struct angelo_server angelo_server;
+
+/* A server of fixed-shape buckets: rays_per_bucket rays with a capacity of
+ * samples_per_ray samples each, points_per_bucket SDF points.  Allocates the
+ * bucket's device buffers, runs one bucket to set the kernels up and, with
+ * use_graph, captures the render bucket as a CUDA graph (thread-local
+ * capture on a stream of its own).  Synchronous. */
+int angelo_serve_create(const angelo_serve_field *field, int64_t rays_per_bucket,
+                        int32_t samples_per_ray, int64_t points_per_bucket, int32_t use_graph,
+                        angelo_server **out);
+/* Render n rays (device, n x 3 origins and directions) in buckets on stream:
+ * rgb (n x 3, background blended), opacity (n), depth (n), as
+ * NeuSModel.forward in eval mode gives comp_rgb_full, opacity and depth.
+ * A bucket whose samples overflow its capacity is rendered again at its
+ * exact size; *overflows (may be NULL) counts them.  Returns after the
+ * outputs are written (one stream synchronisation per call). */
+int angelo_serve_render(angelo_server *srv, const float *rays_o, const float *rays_d, int64_t n,
+                        float *rgb, float *opacity, float *depth, int64_t *overflows, void *stream);
+/* SDF at n device points (VolumeSDF.forward_level, the isosurface lattice of
+ * models/geometry.py:84-92), points_per_bucket at a time; asynchronous. */
+int angelo_serve_sdf(angelo_server *srv, const float *points, int64_t n, float *sdf, void *stream);
+/* Waits for the device and frees the server's buffers and graph. */
+int angelo_serve_destroy(angelo_server *srv);
 
 /* ------------------------------------------------------------ fused compositing */
 

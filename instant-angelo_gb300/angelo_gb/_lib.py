@@ -53,6 +53,15 @@ class SdfNetLayout(ctypes.Structure):
                 ("operand_format", c_i32)]
 
 
+class ServeField(ctypes.Structure):
+    _fields_ = [("lay", HashGridLayout), ("active_levels", c_i32), ("table", c_vp),
+                ("table_dtype", c_i32), ("sdf_layout", SdfNetLayout), ("sdf_net", c_vp),
+                ("radius", c_f32), ("eps", c_f32), ("feat_dim", c_i32), ("rad_net", c_vp),
+                ("rad_flags", c_i32), ("variance", c_vp), ("cos_anneal_ratio", c_f32),
+                ("background", c_vp), ("grid", GridDesc), ("render_step", c_f32),
+                ("max_steps", c_i32), ("near_plane", c_f32), ("far_plane", c_f32)]
+
+
 class AngeloError(RuntimeError):
     def __init__(self, fn, code, msg):
         super().__init__(f"{fn} failed with status {code}: {msg}")
@@ -130,6 +139,17 @@ SIGNATURES = {
                                     c_vp]),
     "angelo_radiance_bwd": (c_i32, [c_i32, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_i64, c_i32, c_vp,
                                     c_vp, c_vp, c_vp, c_vp]),
+    "angelo_mlp_net_bytes": (c_i64, [c_i32, c_i32, c_i32]),
+    "angelo_mlp_grad_size": (c_i64, [c_i32, c_i32, c_i32]),
+    "angelo_mlp_prep": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_mlp_fused_fwd": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_i64, c_i64, c_vp, c_i64, c_vp]),
+    "angelo_mlp_fused_bwd": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_i64, c_i64, c_vp, c_i64, c_vp,
+                                     c_i64, c_vp, c_vp]),
+    "angelo_serve_field_bytes": (c_i64, []),
+    "angelo_serve_create": (c_i32, [c_vp, c_i64, c_i32, c_i64, c_i32, c_vp]),
+    "angelo_serve_render": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_serve_sdf": (c_i32, [c_vp, c_vp, c_i64, c_vp, c_vp]),
+    "angelo_serve_destroy": (c_i32, [c_vp]),
     "angelo_composite_fwd": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_f32,
                                      c_vp, c_f32, c_f32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                      c_vp, c_vp, c_vp]),

@@ -287,6 +287,108 @@ def sdf_query(geom, points):
     return volume_sdf_forward(geom, points, False, False, False)[0]
 
 
+# ------------------------------------------------------------ VanillaMLP (ReLU)
+
+
+class MlpNet:
+    """Prepared tensor-core operands of a ReLU VanillaMLP (one or two hidden
+    layers of 64, no output activation): angelo_mlp_prep's buffer."""
+
+    def __init__(self, in_dim, n_hidden, out_dim, device):
+        self.in_dim, self.n_hidden, self.out_dim = int(in_dim), int(n_hidden), int(out_dim)
+        nbytes = _lib.raw("angelo_mlp_net_bytes")(self.in_dim, self.n_hidden, self.out_dim)
+        if nbytes < 0:
+            raise ValueError(f"MLP {in_dim} -> {n_hidden} x 64 -> {out_dim} not supported by the "
+                             "fused kernel")
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, device=device)
+        self.grad_size = _lib.raw("angelo_mlp_grad_size")(self.in_dim, self.n_hidden, self.out_dim)
+        self.k1cols = 16 * ((self.in_dim + 15) // 16)
+
+    def key(self):
+        return (self.in_dim, self.n_hidden, self.out_dim, self.buf.device)
+
+    def prepare(self, Ws):
+        ts = [t.detach().float().contiguous() for W, b in Ws for t in (W, b)]
+        if self.n_hidden == 1:
+            ts = ts[:2] + [None, None] + ts[2:]
+        call("angelo_mlp_prep", self.in_dim, self.n_hidden, self.out_dim, *[_p(t) for t in ts],
+             _p(self.buf), _s(self.buf.device))
+
+    def unpack_grads(self, g):
+        k1, o = self.k1cols, 0
+        dW1 = g[o:o + 64 * k1].view(64, k1)[:, :self.in_dim]
+        o += 64 * k1
+        dW2 = None
+        if self.n_hidden == 2:
+            dW2 = g[o:o + 4096].view(64, 64)
+            o += 4096
+        dW3 = g[o:o + 16 * 64].view(16, 64)[:self.out_dim]
+        o += 16 * 64
+        db1 = g[o:o + 64]
+        o += 64
+        db2 = None
+        if self.n_hidden == 2:
+            db2 = g[o:o + 64]
+            o += 64
+        db3 = g[o:o + self.out_dim]
+        out = [(dW1, db1)] + ([(dW2, db2)] if self.n_hidden == 2 else []) + [(dW3, db3)]
+        return out
+
+
+class _FusedMlp(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, net, *weights):
+        Ws = [(weights[2 * i], weights[2 * i + 1]) for i in range(len(weights) // 2)]
+        net.prepare(Ws)
+        x = x.contiguous().float()
+        n = x.shape[0]
+        out = torch.empty(n, net.out_dim, device=x.device)
+        call("angelo_mlp_fused_fwd", net.in_dim, net.n_hidden, net.out_dim, _p(net.buf), _p(x),
+             x.stride(0), n, _p(out), out.stride(0), _s(x.device),
+             units=dict(n=n, in_dim=net.in_dim, n_hidden=net.n_hidden, out_dim=net.out_dim, bwd=False))
+        ctx.save_for_backward(x)
+        ctx.net = net
+        return out
+
+    @staticmethod
+    def backward(ctx, g_out):
+        (x,) = ctx.saved_tensors
+        net = ctx.net
+        n = x.shape[0]
+        g_out = g_out.contiguous().float()
+        d_x = torch.empty_like(x) if ctx.needs_input_grad[0] else None
+        d_net = torch.zeros(net.grad_size, device=x.device)
+        call("angelo_mlp_fused_bwd", net.in_dim, net.n_hidden, net.out_dim, _p(net.buf), _p(x),
+             x.stride(0), n, _p(g_out), g_out.stride(0), _p(d_x),
+             d_x.stride(0) if d_x is not None else 0, _p(d_net), _s(x.device),
+             units=dict(n=n, in_dim=net.in_dim, n_hidden=net.n_hidden, out_dim=net.out_dim, bwd=True))
+        flat = []
+        for dW, db in net.unpack_grads(d_net):
+            flat += [dW, db]
+        return (d_x, None, *flat)
+
+
+def mlp_supported(mlp):
+    """Whether a VanillaMLP has the shape the fused kernel runs: ReLU hidden
+    layers of 64 (no sphere init, no weight norm), one or two of them, no
+    output activation, in <= 64, out <= 16."""
+    return (not mlp.sphere_init and not mlp.weight_norm and mlp.n_neurons == 64
+            and mlp.n_hidden_layers in (1, 2) and mlp.output_activation in (None, "none", "None")
+            and 1 <= mlp.dim_in <= 64 and 1 <= mlp.dim_out <= 16)
+
+
+def mlp_forward(mlp, x):
+    """VanillaMLP.forward on the fused kernel (models/network_utils.py:134-140)."""
+    net = getattr(mlp, "_fused_net", None)
+    if net is None or net.key() != (mlp.dim_in, mlp.n_hidden_layers, mlp.dim_out, x.device):
+        net = MlpNet(mlp.dim_in, mlp.n_hidden_layers, mlp.dim_out, x.device)
+        mlp._fused_net = net
+    weights = []
+    for W, b in mlp.effective_weights():
+        weights += [W, b]
+    return _FusedMlp.apply(x, net, *weights)
+
+
 # ----------------------------------------------------------------- radiance
 
 
@@ -332,7 +434,7 @@ class _FusedRadiance(torch.autograd.Function):
         if fnet is not net and any(ctx.needs_input_grad):
             net.prepare(Ws)
         feature = feature.contiguous()
-        grad = grad.contiguous()
+        grad = grad.contiguous() if grad is not None else None
         S = feature.shape[0]
         rgb = torch.empty(S, 3, device=feature.device)
         flags = int(dual) | (2 if meta.get("one_pass") else 0) | \
@@ -351,7 +453,7 @@ class _FusedRadiance(torch.autograd.Function):
         S = feature.shape[0]
         g_rgb = g_rgb.contiguous().float()
         d_feature = torch.zeros_like(feature)
-        d_grad = torch.empty_like(grad)
+        d_grad = torch.empty_like(grad) if grad is not None else None
         d_net = torch.zeros(net.grad_size, device=feature.device)
         call("angelo_radiance_bwd", net.feat_dim, _p(net.buf), _p(feature), feature.stride(0),
              _p(grad), _p(ray_idx), _p(rays_d), S, int(dual), _p(g_rgb), _p(d_feature),
@@ -364,6 +466,10 @@ class _FusedRadiance(torch.autograd.Function):
 
 
 def radiance_forward(texture, feature, grad, ray_idx, rays_d):
+    """The radiance network on the fused kernel; grad None: a VolumeRadiance
+    without a normal input (the learned background's texture, input
+    [feature, SH4]), whose first layer gets three zero columns where the
+    kernel stages the normal."""
     net = getattr(texture, "_fused_net", None)
     F_ = feature.shape[-1]
     if net is None or net.feat_dim != F_ or net.buf.device != feature.device:
@@ -372,6 +478,10 @@ def radiance_forward(texture, feature, grad, ray_idx, rays_d):
     weights = []
     for W, b in texture.network.effective_weights():
         weights += [W, b]
+    if grad is None:
+        if weights[0].shape[1] != F_ + 16:
+            raise ValueError("a radiance network without a normal input takes [feature, SH4]")
+        weights[0] = torch.nn.functional.pad(weights[0], (0, 3))
     prec = _precision(texture)
     meta = dict(net=net, dual=bool(getattr(texture, "dual", False)), one_pass=prec in ("bf16", "fp16"))
     if prec == "fp16":

@@ -103,6 +103,9 @@ class VolumeDensity(nn.Module):
         self.n_output_dims = config.feature_dim
         encoding = get_encoding(self.n_input_dims, config.xyz_encoding_config)
         network = get_mlp(encoding.n_output_dims, self.n_output_dims, config.mlp_network_config)
+        # fused form: the MLP on the fused tensor-core kernel (the hash grid
+        # runs on this library's encode kernels in both forms)
+        network.fused = bool(config.get("fused", False))
         self.encoding_with_network = EncodingWithNetwork(encoding, network)
         self.contraction_type = "unbounded_sphere"
 

@@ -182,8 +182,15 @@ class VanillaMLP(nn.Module):
         self.layers = nn.Sequential(*layers)
         self.output_activation = config.get("output_activation", "none")
         self.dim_in, self.dim_out = dim_in, dim_out
+        # set by the fused forms: run on the fused tensor-core MLP kernel
+        # (ReLU MLPs of the shapes angelo_gb.fused.mlp_supported accepts)
+        self.fused = False
 
     def forward(self, x):
+        if self.fused:
+            from . import fused
+            if fused.mlp_supported(self):
+                return fused.mlp_forward(self, x.reshape(-1, self.dim_in)).view(*x.shape[:-1], self.dim_out)
         x = self.layers(x.float())
         return output_activation(self.output_activation)(x)
 

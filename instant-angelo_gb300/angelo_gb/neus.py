@@ -160,6 +160,23 @@ def chunk_batch(func, chunk_size, move_to_cpu, *args, **kwargs):
     return out
 
 
+def fused_radiance_bg(texture):
+    """Whether the learned background's texture runs on the fused radiance
+    kernel: a VolumeRadiance (models/texture.py:10-30) on [feature,
+    SH4((d+1)/2)] with a sigmoid colour and a ReLU VanillaMLP of two hidden
+    layers of 64, whose input width the kernel is instantiated for."""
+    net = getattr(texture, "network", None)
+    cfg = texture.config
+    if type(texture).__name__ != "VolumeRadiance" or net is None:
+        return False
+    feat = int(cfg.input_feature_dim)
+    return (not net.sphere_init and not net.weight_norm and net.n_neurons == 64
+            and net.n_hidden_layers == 2 and net.output_activation in (None, "none", "None")
+            and str(cfg.get("color_activation", "")).lower() == "sigmoid"
+            and texture.n_dir_dims == 3 and texture.encoding.n_output_dims == 16
+            and net.dim_in == feat + 16 and (feat + 19 + 15) // 16 in (2, 3, 6))
+
+
 @models.register("neus")
 class NeuSModel(nn.Module):
     def __init__(self, config):
@@ -183,6 +200,7 @@ class NeuSModel(nn.Module):
         if self.learned_background:
             # models/neus.py:51-56: density field and radiance outside the box,
             # marched from the box exit (or 0.1) to 1e3 with exponential steps
+            config.geometry_bg["fused"] = fused
             self.geometry_bg = models.make(config.geometry_bg.name, config.geometry_bg)
             self.texture_bg = models.make(config.texture_bg.name, config.texture_bg)
             self.geometry_bg.contraction_type = "unbounded_sphere"
@@ -389,7 +407,14 @@ class NeuSModel(nn.Module):
         positions = rays_o[ray_indices] + t_dirs * midpoints
         intervals = (t1 - t0)[:, None]
         density, feature = self.geometry_bg(positions)
-        rgb = self.texture_bg(feature, t_dirs)
+        if self.fused and fused_radiance_bg(self.texture_bg):
+            # the radiance kernel takes the direction by ray index, as the
+            # foreground's does
+            from . import fused
+            rgb = fused.radiance_forward(self.texture_bg, feature.contiguous(), None, ri,
+                                         rays_d.contiguous())
+        else:
+            rgb = self.texture_bg(feature, t_dirs)
         weights = ops.render_weight_from_density(t0[:, None], t1[:, None], density[:, None], offsets)
         opacity = ops.accumulate_along_rays(weights, offsets)
         depth = ops.accumulate_along_rays(weights, offsets, midpoints)

@@ -255,6 +255,84 @@ class SdfBucket:
             return self.out[:n].clone()
 
 
+class NativeServer:
+    """The library's own server (angelo_serve_*: C ABI, buckets replayed as a
+    CUDA graph) over a NeuSModel's resident state: renders and SDF queries
+    with the kernels and order of RenderBucket / SdfBucket.  The weights are
+    prepared once; the model must not change while the server lives."""
+
+    def __init__(self, model, rays_per_bucket=1 << 14, samples_per_ray=128,
+                 points_per_bucket=1 << 20, background=(1.0, 1.0, 1.0), use_graph=True):
+        geom, tex = model.geometry, model.texture
+        dev = model.scene_aabb.device
+        self.model = model
+        self.sdf_net = fused._net_for(geom)
+        self.sdf_net.layout.mma_passes = 3
+        self.sdf_net.prepare(fused.effective_weights(geom.network))
+        od = self.sdf_net.out_dim
+        self.rad_net = fused.RadNet(od + 3, dev)
+        self.rad_net.prepare(tex.network.effective_weights())
+        self.bg = torch.as_tensor(background, dtype=torch.float32, device=dev).contiguous()
+        self.var = model.variance.variance.detach().reshape(1).float().contiguous()
+        table = geom.hashgrid.encoding.params
+        f = _lib.ServeField()
+        f.lay = geom.hashgrid.encoding.spec.layout
+        f.active_levels = int(geom.hashgrid.mask_levels)
+        f.table = table.data_ptr()
+        f.table_dtype = _lib.DTYPE_F32 if table.dtype == torch.float32 else _lib.DTYPE_F16
+        f.sdf_layout = self.sdf_net.layout
+        f.sdf_net = self.sdf_net.buf.data_ptr()
+        f.radius = float(geom.radius)
+        f.eps = float(geom._finite_difference_eps or 1.0)
+        f.feat_dim = od + 3
+        f.rad_net = self.rad_net.buf.data_ptr()
+        f.rad_flags = int(bool(getattr(tex, "dual", False)))
+        f.variance = self.var.data_ptr()
+        f.cos_anneal_ratio = 1.0
+        f.background = self.bg.data_ptr()
+        f.grid = _grid_desc(model)
+        f.render_step = float(model.render_step_size)
+        f.max_steps = int(min(model.max_march_steps, (1 << 31) - 1))
+        f.near_plane = -1.0 if model.near_plane is None else float(model.near_plane)
+        f.far_plane = -1.0 if model.far_plane is None else float(model.far_plane)
+        self.field = f
+        self.handle = ctypes.c_void_p()
+        _lib.call("angelo_serve_create", ctypes.byref(f), int(rays_per_bucket), int(samples_per_ray),
+                  int(points_per_bucket), int(use_graph), ctypes.byref(self.handle))
+
+    @torch.no_grad()
+    def render(self, rays):
+        """rays (n, 6) on the device -> (rgb with background, opacity, depth,
+        number of buckets rendered again at exact size)."""
+        o, d = rays[:, :3].contiguous().float(), rays[:, 3:].contiguous().float()
+        n = o.shape[0]
+        rgb = torch.empty(n, 3, device=o.device)
+        op = torch.empty(n, 1, device=o.device)
+        dep = torch.empty(n, 1, device=o.device)
+        ovf = ctypes.c_int64(0)
+        _lib.call("angelo_serve_render", self.handle, ops._p(o), ops._p(d), n, ops._p(rgb), ops._p(op),
+                  ops._p(dep), ctypes.byref(ovf), ops._s(o.device))
+        return rgb, op, dep, int(ovf.value)
+
+    @torch.no_grad()
+    def sdf(self, points):
+        p = points.reshape(-1, 3).contiguous().float()
+        out = torch.empty(p.shape[0], device=p.device)
+        _lib.call("angelo_serve_sdf", self.handle, ops._p(p), p.shape[0], ops._p(out), ops._s(p.device))
+        return out.view(points.shape[:-1])
+
+    def close(self):
+        if self.handle:
+            _lib.call("angelo_serve_destroy", self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Server:
     """Continuous batching over RenderBucket / SdfBucket replays.
 

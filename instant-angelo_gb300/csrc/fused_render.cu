@@ -131,6 +131,12 @@ __device__ __forceinline__ void rad_sh_normal(const RadParams &P, int64_t s, flo
     const float y = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(d[1], 1.f), 2.f), 2.f), 1.f);
     const float z = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn(d[2], 1.f), 2.f), 2.f), 1.f);
     sh4_eval(x, y, z, sh);
+    if (!P.grad) {
+        // a radiance network without a normal input (VolumeRadiance of the
+        // learned background): the normal columns stay zero
+        nrm[0] = nrm[1] = nrm[2] = 0.f;
+        return;
+    }
     const float *g = P.grad + s * 3;
     const float gn = fmaxf(sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]), 1e-12f);
 #pragma unroll
@@ -298,7 +304,7 @@ __device__ __forceinline__ void rad_dx_out(const RadParams &P, int64_t s, int b,
             has_n = true;
         }
     }
-    if (!has_n) return;
+    if (!has_n || !P.d_grad) return;
     const float *g = P.grad + s * 3;
     const float gn = sqrtf(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
     const float den = fmaxf(gn, 1e-12f);
@@ -862,10 +868,11 @@ template <bool BWD>
 int dispatch_rad(const RadParams &P, cudaStream_t st) {
     const bool f16 = !BWD && P.fp16;
     switch (P.L.k_tiles1) {
+        case 2: return f16 ? launch_rad<2, BWD, true>(P, st) : launch_rad<2, BWD>(P, st);
         case 3: return f16 ? launch_rad<3, BWD, true>(P, st) : launch_rad<3, BWD>(P, st);
         case 6: return f16 ? launch_rad<6, BWD, true>(P, st) : launch_rad<6, BWD>(P, st);
         default:
-            set_error("radiance: input width %d not instantiated (feature width 16 or 68)", P.L.in_dim);
+            set_error("radiance: input width %d not instantiated (feature width 8, 16 or 68)", P.L.in_dim);
             return ANGELO_E_UNSUPPORTED;
     }
 }
@@ -879,7 +886,7 @@ extern "C" int angelo_radiance_fwd(int32_t feat_dim, const void *net, const floa
     ANGELO_REQUIRE(feat_dim >= 1 && feat_dim + 19 <= kXCols, "radiance_fwd: feature width");
     ANGELO_REQUIRE(n >= 0, "radiance_fwd: negative n");
     if (n == 0) return ANGELO_OK;
-    ANGELO_REQUIRE(net && feature && grad && ray_idx && rays_d && rgb && feat_stride >= feat_dim,
+    ANGELO_REQUIRE(net && feature && ray_idx && rays_d && rgb && feat_stride >= feat_dim,
                    "radiance_fwd: bad argument");
     RadParams P{};
     P.L = rad_layout(feat_dim);
@@ -904,8 +911,9 @@ extern "C" int angelo_radiance_bwd(int32_t feat_dim, const void *net, const floa
     ANGELO_REQUIRE(feat_dim >= 1 && feat_dim + 19 <= kXCols, "radiance_bwd: feature width");
     ANGELO_REQUIRE(n >= 0, "radiance_bwd: negative n");
     if (n == 0) return ANGELO_OK;
-    ANGELO_REQUIRE(net && feature && grad && ray_idx && rays_d && g_rgb && d_feature && d_grad &&
-                   d_net && feat_stride >= feat_dim, "radiance_bwd: bad argument");
+    ANGELO_REQUIRE(net && feature && ray_idx && rays_d && g_rgb && d_feature && d_net &&
+                       feat_stride >= feat_dim && (grad != nullptr) == (d_grad != nullptr),
+                   "radiance_bwd: bad argument");
     RadParams P{};
     P.L = rad_layout(feat_dim);
     P.net = reinterpret_cast<const char *>(net);

@@ -1573,6 +1573,7 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
 }
 
 namespace angelo {
+int64_t mlp_tc_timeouts(int reset);        // fused_mlp.cu
 int64_t radiance_tc_timeouts(int reset);   // fused_render.cu
 }
 
@@ -1584,7 +1585,8 @@ extern "C" int64_t angelo_tc_timeouts(int32_t reset) {
         if (cudaMemcpyToSymbol(g_tc_timeouts, &z, sizeof(z)) != cudaSuccess) return -1;
     }
     const int64_t r = angelo::radiance_tc_timeouts(reset);
-    return r < 0 ? -1 : (int64_t)v + r;
+    const int64_t m = angelo::mlp_tc_timeouts(reset);
+    return (r < 0 || m < 0) ? -1 : (int64_t)v + r + m;
 }
 
 extern "C" int64_t angelo_sdf_grad_size(const angelo_sdf_net_layout *nl) {

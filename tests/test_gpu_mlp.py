@@ -1,0 +1,166 @@
+"""The fused ReLU VanillaMLP (angelo_mlp_fused_fwd / _bwd: the learned
+background's density network, models/network_utils.py:96-140) against float64
+autograd of the same weights: outputs, dL/dx and every weight gradient, for
+one and two hidden layers, ragged row counts (empty, one row, partial tiles,
+many tiles per CTA) and strided inputs."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    from angelo_gb import build
+    build.build()
+    return torch.device("cuda:0")
+
+
+def _mlp(in_dim, n_hidden, out_dim, seed):
+    from angelo_gb.network_utils import VanillaMLP
+    torch.manual_seed(seed)
+    m = VanillaMLP(in_dim, out_dim, dict(n_neurons=64, n_hidden_layers=n_hidden, activation="ReLU",
+                                         output_activation="none"))
+    with torch.no_grad():
+        for lin in m.linears():
+            lin.bias.uniform_(-0.2, 0.2)
+    return m
+
+
+# bf16x3 operands: every product carries ~2^-16 of its operands' magnitude
+FWD_TOL = 2e-5
+BWD_TOL = 5e-5
+# rows whose float64 pre-activations come within this of zero are left out of
+# the exact comparison: ReLU's derivative jumps at 0, and a pre-activation
+# that close may fall on the other side in any arithmetic that is not float64
+# (bf16x3 is ~3e-5 off on pre-activations of order 1)
+MASK_MARGIN = 2e-3
+
+
+def _pre_acts(m, x64):
+    h, pre = x64, []
+    lins = m.linears()
+    for i, lin in enumerate(lins[:-1]):
+        z = h @ lin.weight.detach().double().t() + lin.bias.detach().double()
+        pre.append(z)
+        h = torch.relu(z)
+    return pre
+
+
+def _clear_rows(m, n, in_dim, g, dev):
+    """n rows uniform in [-1, 1]^in_dim whose pre-activations all stay
+    MASK_MARGIN away from zero."""
+    rows = []
+    have = 0
+    while have < n:
+        x = torch.rand(max(2 * (n - have), 64), in_dim, generator=g) * 2 - 1
+        ok = torch.ones(x.shape[0], dtype=torch.bool)
+        for z in _pre_acts(m.cpu(), x.double()):
+            ok &= (z.abs() > MASK_MARGIN).all(dim=1)
+        rows.append(x[ok])
+        have += int(ok.sum())
+    m.to(dev)
+    return torch.cat(rows)[:n]
+
+
+def _fp64(m, x, gout):
+    x64 = x.detach().double().requires_grad_(True)
+    ws = [(lin.weight.detach().double().requires_grad_(True), lin.bias.detach().double().requires_grad_(True))
+          for lin in m.linears()]
+    h = x64
+    for i, (W, b) in enumerate(ws):
+        h = h @ W.t() + b
+        if i + 1 < len(ws):
+            h = torch.relu(h)
+    (h * gout.double()).sum().backward()
+    return h.detach(), x64.grad, ws
+
+
+@pytest.mark.parametrize("shape", [(35, 1, 8), (19, 1, 8), (24, 2, 3), (64, 2, 16), (5, 1, 1)])
+@pytest.mark.parametrize("n", [0, 1, 127, 129, 70001])
+def test_fused_mlp_matches_fp64(dev, shape, n):
+    from angelo_gb import fused
+    in_dim, nh, od = shape
+    m = _mlp(in_dim, nh, od, seed=in_dim * 7 + nh)
+    m.fused = True
+    assert fused.mlp_supported(m)
+    g = torch.Generator(device="cpu").manual_seed(n + in_dim)
+    xs = _clear_rows(m, n, in_dim, g, dev) if n else torch.zeros(0, in_dim)
+    m.to(dev)
+    # strided input: rows of a wider buffer (the encodings' layout)
+    buf = torch.zeros(n, in_dim + 5)
+    buf[:, 2:2 + in_dim] = xs
+    x = buf.to(dev)[:, 2:2 + in_dim].requires_grad_(True)
+    out = m(x)
+    assert out.shape == (n, od)
+    gout = torch.randn(n, od, generator=g).to(dev)
+    (out * gout).sum().backward()
+    h, gx, ws = _fp64(m, x, gout)
+    if n == 0:
+        return
+    scale = float(h.abs().max()) + 1e-12
+    assert float((out.detach().double() - h).abs().max()) <= FWD_TOL * scale
+    gs = float(gx.abs().max()) + 1e-12
+    assert float((x.grad.double() - gx).abs().max()) <= BWD_TOL * gs
+    for lin, (W, b) in zip(m.linears(), ws):
+        for a, r in ((lin.weight.grad, W.grad), (lin.bias.grad, b.grad)):
+            sc = float(r.abs().max()) + 1e-12
+            assert float((a.double() - r).abs().max()) <= BWD_TOL * sc
+
+
+def test_fused_mlp_mask_flips_stay_local(dev):
+    """Unfiltered rows: the few units that sit within the products' rounding
+    of zero may flip their ReLU mask against float64, which moves single
+    gradient rows; the outputs and the 2-norm of every gradient still agree."""
+    m = _mlp(35, 1, 8, seed=11)
+    m.fused = True
+    m.to(dev)
+    g = torch.Generator(device="cpu").manual_seed(12)
+    x = (torch.rand(100000, 35, generator=g) * 2 - 1).to(dev).requires_grad_(True)
+    gout = torch.randn(100000, 8, generator=g).to(dev)
+    out = m(x)
+    (out * gout).sum().backward()
+    h, gx, ws = _fp64(m, x, gout)
+    assert float((out.detach().double() - h).abs().max()) <= FWD_TOL * float(h.abs().max())
+    # a flip moves its whole dL/dx row: few rows move, the rest agree tightly
+    row_err = (x.grad.double() - gx).norm(dim=1) / (gx.norm(dim=1) + 1e-30)
+    assert float((row_err > 1e-3).double().mean()) < 5e-3
+    assert float(row_err.median()) < 1e-4
+    rel2 = lambda a, r: float((a.double() - r).norm() / (r.norm() + 1e-30))  # noqa: E731
+    for lin, (W, b) in zip(m.linears(), ws):
+        assert rel2(lin.weight.grad, W.grad) < 1e-3
+        assert rel2(lin.bias.grad, b.grad) < 1e-3
+
+
+def test_fused_mlp_no_input_gradient(dev):
+    """dL/dx is not written when x needs no gradient (d_x = NULL); the weight
+    gradients are the same as with it."""
+    m = _mlp(35, 1, 8, seed=3).to(dev)
+    m.fused = True
+    x = torch.rand(3000, 35, device=dev) * 2 - 1
+    gout = torch.randn(3000, 8, device=dev)
+    (m(x) * gout).sum().backward()
+    g1 = [p.grad.clone() for p in m.parameters()]
+    m.zero_grad()
+    xr = x.clone().requires_grad_(True)
+    (m(xr) * gout).sum().backward()
+    # the CTAs add their weight gradients with atomics in any order: equal up
+    # to the rounding of that order, relative to the tensor's largest entry
+    for a, b in zip(g1, [p.grad for p in m.parameters()]):
+        assert float((a - b).abs().max()) <= 1e-5 * float(b.abs().max())
+
+
+def test_fused_mlp_deterministic_rows(dev):
+    """A row's output does not depend on the batch it is in (the background
+    reuses the visibility pass's outputs on the kept samples)."""
+    m = _mlp(35, 1, 8, seed=5).to(dev)
+    m.fused = True
+    x = torch.rand(5000, 35, device=dev)
+    with torch.no_grad():
+        a = m(x)
+        idx = torch.randperm(5000, device=dev)[:1234]
+        b = m(x[idx])
+    assert torch.equal(a[idx], b)

@@ -167,3 +167,34 @@ def test_backward_refuses_fp16_prepared_weights(lib):
     rc = lib.angelo_sdf_stencil_fwd(ctypes.byref(lay), 8, p, 0, ctypes.byref(L), p, p, None, 1, 1.0,
                                     1e-2, 0, 0, 0, p, None, None, 0, None, p, None)
     assert rc == _lib.ANGELO_E_INVALID
+
+
+def test_mlp_shape_queries(lib):
+    """The fused VanillaMLP's size queries (host-only): supported shapes give
+    the documented gradient layout, unsupported ones -1, and the fused forms
+    route only MLPs of a supported shape to it."""
+    from angelo_gb import fused
+    from angelo_gb.network_utils import VanillaMLP
+    for in_dim, nh, od in ((35, 1, 8), (19, 1, 8), (24, 2, 3), (64, 2, 16)):
+        k1 = 16 * ((in_dim + 15) // 16)
+        want = 64 * k1 + (64 * 64 + 64 if nh == 2 else 0) + 16 * 64 + 64 + 16
+        assert lib.angelo_mlp_grad_size(in_dim, nh, od) == want
+        assert lib.angelo_mlp_net_bytes(in_dim, nh, od) > 0
+    for bad in ((0, 1, 8), (65, 1, 8), (35, 3, 8), (35, 0, 8), (35, 1, 17), (35, 1, 0)):
+        assert lib.angelo_mlp_net_bytes(*bad) == -1
+        assert lib.angelo_mlp_grad_size(*bad) == -1
+    relu = dict(n_neurons=64, n_hidden_layers=1, activation="ReLU", output_activation="none")
+    assert fused.mlp_supported(VanillaMLP(35, 8, relu))
+    assert not fused.mlp_supported(VanillaMLP(35, 8, {**relu, "n_hidden_layers": 3}))
+    assert not fused.mlp_supported(VanillaMLP(35, 8, {**relu, "output_activation": "sigmoid"}))
+    assert not fused.mlp_supported(VanillaMLP(35, 8, {**relu, "n_neurons": 32}))
+    assert not fused.mlp_supported(VanillaMLP(35, 13, {**relu, "sphere_init": True}))
+    assert not fused.mlp_supported(VanillaMLP(80, 8, relu))
+
+
+def test_serve_field_struct_matches_the_library(lib):
+    """The ctypes mirror of angelo_serve_field has the C struct's size (a
+    mismatch would hand the server shifted pointers)."""
+    import ctypes as ct
+    from angelo_gb import _lib
+    assert ct.sizeof(_lib.ServeField) == lib.angelo_serve_field_bytes()
