@@ -483,6 +483,28 @@ int angelo_mlp_fused_bwd(int32_t in_dim, int32_t n_hidden, int32_t out_dim, cons
                          int64_t g_stride, float *d_x, int64_t dx_stride, float *d_net,
                          void *stream);
 
+/* ------------------------------------------- fused background compositing */
+
+/* The learned background's compositing in one warp per ray
+ * (models/neus.py:171-177: nerfacc 0.3.3 render_weight_from_density, then
+ * accumulate_along_rays of 1, the interval midpoints and the colours, and
+ * the background colour blended behind): w_j = (1 - e^-tau_j)
+ * e^-(tau_0 + .. + tau_{j-1}), tau_j = sigma_j (t_end - t_start);
+ * opacity (n_rays), depth (n_rays), comp_rgb (n_rays x 3) = sum w rgb +
+ * bg (1 - opacity).  weights and trans (per sample) are kept for the
+ * backward. */
+int angelo_density_composite_fwd(const int64_t *offsets, int64_t n_rays, const float *sigmas,
+                                 const float *t_starts, const float *t_ends, const float *rgb,
+                                 const float *bg, float *opacity, float *depth, float *comp_rgb,
+                                 float *weights, float *trans, void *stream);
+/* Backward from dL/dopacity, dL/ddepth, dL/dcomp_rgb (each may be NULL =
+ * zero): writes dL/dsigma (per sample) and dL/drgb (per sample x 3). */
+int angelo_density_composite_bwd(const int64_t *offsets, int64_t n_rays, const float *sigmas,
+                                 const float *t_starts, const float *t_ends, const float *rgb,
+                                 const float *bg, const float *weights, const float *trans,
+                                 const float *g_opacity, const float *g_depth, const float *g_rgb,
+                                 float *d_sigmas, float *d_rgb, void *stream);
+
 /* ------------------------------------------------------------------ serving */
 
 /* The resident field a server renders: device pointers owned by the caller

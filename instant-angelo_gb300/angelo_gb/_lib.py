@@ -145,6 +145,10 @@ SIGNATURES = {
     "angelo_mlp_fused_fwd": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_i64, c_i64, c_vp, c_i64, c_vp]),
     "angelo_mlp_fused_bwd": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_i64, c_i64, c_vp, c_i64, c_vp,
                                      c_i64, c_vp, c_vp]),
+    "angelo_density_composite_fwd": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                             c_vp, c_vp, c_vp, c_vp]),
+    "angelo_density_composite_bwd": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
+                                             c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "angelo_serve_field_bytes": (c_i64, []),
     "angelo_serve_create": (c_i32, [c_vp, c_i64, c_i32, c_i64, c_i32, c_vp]),
     "angelo_serve_render": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),

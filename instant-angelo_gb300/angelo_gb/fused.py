@@ -389,6 +389,108 @@ def mlp_forward(mlp, x):
     return _FusedMlp.apply(x, net, *weights)
 
 
+class _ReusedDensityField(torch.autograd.Function):
+    """The density field's MLP output on samples whose encodings X and
+    outputs a no-grad pass already computed (the learned background's
+    visibility test evaluates every marched sample; the kept ones are
+    evaluated again by the reference, with bit-identical results here).  The
+    forward hands the kept outputs on; the backward runs the MLP backward
+    from the kept encodings and scatters dL/dX into the hash table."""
+
+    @staticmethod
+    def forward(ctx, pts, X, out, table, meta, *weights):
+        ctx.save_for_backward(pts, X, table)
+        ctx.meta = meta
+        return out.clone()
+
+    @staticmethod
+    def backward(ctx, g_out):
+        pts, X, table = ctx.saved_tensors
+        net, spec, active, xyz = ctx.meta["net"], ctx.meta["spec"], ctx.meta["active"], ctx.meta["xyz"]
+        n = X.shape[0]
+        g = g_out.contiguous().float()
+        dX = torch.empty_like(X)
+        d_net = torch.zeros(net.grad_size, device=X.device)
+        call("angelo_mlp_fused_bwd", net.in_dim, net.n_hidden, net.out_dim, _p(net.buf), _p(X),
+             X.stride(0), n, _p(g), g.stride(0), _p(dX), dX.stride(0), _p(d_net), _s(X.device),
+             units=dict(n=n, in_dim=net.in_dim, n_hidden=net.n_hidden, out_dim=net.out_dim, bwd=True))
+        dtable = None
+        if ctx.needs_input_grad[3] and active > 0:
+            dtable = torch.zeros(spec.n_params, device=X.device, dtype=torch.float32)
+            call("angelo_hashgrid_bwd", ctypes.byref(spec.layout), int(active), _p(pts), n, _p(table),
+                 _table_dtype(table), int(xyz), _p(dX), dX.stride(0), 0, _p(dtable), None, _s(X.device),
+                 units=dict(n=n, active=int(active), L=spec.n_levels, tbytes=table.element_size(),
+                            dtable=True, dx=False))
+        elif ctx.needs_input_grad[3]:
+            dtable = torch.zeros(spec.n_params, device=X.device, dtype=torch.float32)
+        flat = []
+        for dW, db in net.unpack_grads(d_net):
+            flat += [dW, db]
+        return (None, None, None, dtable, None, *flat)
+
+
+def density_field_reused(geom, pts, X, out):
+    """VolumeDensity's (density, feature) on kept samples from the visibility
+    pass's contracted points, encodings and MLP outputs (see
+    _ReusedDensityField); differentiable w.r.t. the hash table and the MLP."""
+    enc, mlp = geom.encoding_with_network.encoding, geom.encoding_with_network.network
+    grid = enc.encoding
+    net = mlp._fused_net
+    weights = []
+    for W, b in mlp.effective_weights():
+        weights += [W, b]
+    meta = dict(net=net, spec=grid.encoding.spec, active=int(grid.mask_levels), xyz=bool(enc.include_xyz))
+    o = _ReusedDensityField.apply(pts.contiguous(), X.contiguous(), out.contiguous(), grid.encoding.params,
+                                  meta, *weights)
+    return geom.outputs(o)
+
+
+class _DensityComposite(torch.autograd.Function):
+    """The learned background's weights from density, accumulation and
+    background blend in one kernel each way (angelo_density_composite_*)."""
+
+    @staticmethod
+    def forward(ctx, sigma, rgb, t0, t1, offsets, bg):
+        n_rays = offsets.numel() - 1
+        S = sigma.numel()
+        dev = sigma.device
+        sigma, rgb = sigma.contiguous().float(), rgb.contiguous().float()
+        t0, t1, bg = t0.contiguous(), t1.contiguous(), bg.contiguous().float()
+        opacity = torch.empty(n_rays, 1, device=dev)
+        depth = torch.empty(n_rays, 1, device=dev)
+        comp = torch.empty(n_rays, 3, device=dev)
+        weights = torch.empty(S, device=dev)
+        trans = torch.empty(S, device=dev)
+        call("angelo_density_composite_fwd", _p(offsets), n_rays, _p(sigma), _p(t0), _p(t1), _p(rgb),
+             _p(bg), _p(opacity), _p(depth), _p(comp), _p(weights), _p(trans), _s(dev),
+             units=dict(n=S, rays=n_rays, bwd=False))
+        ctx.save_for_backward(sigma, rgb, t0, t1, offsets, bg, weights, trans)
+        ctx.mark_non_differentiable(weights)
+        ctx.set_materialize_grads(False)
+        return comp, opacity, depth, weights
+
+    @staticmethod
+    def backward(ctx, g_comp, g_op, g_depth, g_w):
+        sigma, rgb, t0, t1, offsets, bg, weights, trans = ctx.saved_tensors
+        n_rays = offsets.numel() - 1
+        dev = sigma.device
+
+        def c(t):
+            return t.contiguous().float() if t is not None else None
+        d_sigma = torch.empty_like(sigma)
+        d_rgb = torch.empty_like(rgb)
+        call("angelo_density_composite_bwd", _p(offsets), n_rays, _p(sigma), _p(t0), _p(t1), _p(rgb),
+             _p(bg), _p(weights), _p(trans), _p(c(g_op)), _p(c(g_depth)), _p(c(g_comp)), _p(d_sigma),
+             _p(d_rgb), _s(dev), units=dict(n=sigma.numel(), rays=n_rays, bwd=True))
+        return d_sigma, d_rgb, None, None, None, None
+
+
+def density_composite(sigma, rgb, t0, t1, offsets, bg):
+    """(comp_rgb with bg blended, opacity, depth, weights) of the learned
+    background (models/neus.py:171-177)."""
+    return _DensityComposite.apply(sigma.reshape(-1), rgb, t0.reshape(-1), t1.reshape(-1), offsets, bg)
+
+
 # ----------------------------------------------------------------- radiance
 
 

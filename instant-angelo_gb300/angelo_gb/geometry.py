@@ -125,6 +125,35 @@ class VolumeDensity(nn.Module):
             feature = get_activation(self.config.feature_activation)(feature)
         return self._density(out), feature
 
+    def fused_reuse_ok(self):
+        """Whether the fused form can hand the visibility pass's encodings and
+        outputs to the training pass (angelo_gb.fused.density_field_reused):
+        the MLP on the fused kernel and the encoding the hash grid's own
+        [x*2-1, grid] kernel."""
+        from . import fused
+        from .network_utils import CompositeEncoding, ProgressiveBandHashGrid
+        enc, net = self.encoding_with_network.encoding, self.encoding_with_network.network
+        return (getattr(net, "fused", False) and fused.mlp_supported(net)
+                and isinstance(enc, CompositeEncoding)
+                and isinstance(enc.encoding, ProgressiveBandHashGrid)
+                and enc.xyz_scale == 2.0 and enc.xyz_offset == -1.0)
+
+    def encode_and_evaluate(self, points):
+        """(contracted points, encodings X, MLP output) of world points, the
+        pieces forward() composes (no autograd graph is kept when called
+        under no_grad)."""
+        pts = contract_unbounded_sphere(points, self.radius).view(-1, self.n_input_dims)
+        X = self.encoding_with_network.encoding(pts)
+        out = self.encoding_with_network.network(X).float()
+        return pts, X, out
+
+    def outputs(self, out):
+        """(density, feature) from the MLP output, as forward() forms them."""
+        feature = out
+        if "feature_activation" in self.config:
+            feature = get_activation(self.config.feature_activation)(feature)
+        return self._density(out), feature
+
     def forward_level(self, points):
         pts = contract_unbounded_sphere(points, self.radius)
         out = self.encoding_with_network(pts.reshape(-1, self.n_input_dims)).reshape(

@@ -394,19 +394,37 @@ class NeuSModel(nn.Module):
                                                max_samples_per_ray=self._bg_samples_bound(), **grid)
             rl = ri.long()
             pos = rays_o[rl] + rays_d[rl] * ((t0 + t1) * 0.5)[:, None]
-            sigma, _ = self.geometry_bg(pos)
+            reuse = self.fused and self.geometry_bg.fused_reuse_ok()
+            if reuse:
+                # the fused form keeps the visibility pass's encodings and
+                # outputs for the kept samples instead of evaluating them again
+                pts_c, X_all, out_all = self.geometry_bg.encode_and_evaluate(pos)
+                sigma, _ = self.geometry_bg.outputs(out_all)
+            else:
+                sigma, _ = self.geometry_bg(pos)
             alpha = 1.0 - torch.exp(-sigma * (t1 - t0))
             keep = ops.transmittance_from_alpha(alpha, offsets) >= 1e-4
             self._last_march_bg_full = (offsets, ri, t0, t1)
-            ri, t0, t1 = ri[keep], t0[keep], t1[keep]
+            # the kept samples' indices once (one device read of their
+            # count), then one gather per tensor
+            kidx = keep.nonzero().squeeze(1)
+            ri, t0, t1 = ri.index_select(0, kidx), t0.index_select(0, kidx), t1.index_select(0, kidx)
+            if reuse:
+                pts_c, X_all, out_all = (pts_c.index_select(0, kidx), X_all.index_select(0, kidx),
+                                         out_all.index_select(0, kidx))
             offsets = ops.offsets_from_ray_indices(ri, n_rays)
             self._last_march_bg = (offsets, ri, t0, t1)
         ray_indices = ri.long()
-        t_dirs = rays_d[ray_indices]
         midpoints = ((t0 + t1) * 0.5)[:, None]
-        positions = rays_o[ray_indices] + t_dirs * midpoints
         intervals = (t1 - t0)[:, None]
-        density, feature = self.geometry_bg(positions)
+        t_dirs = None
+        if reuse:
+            from . import fused
+            density, feature = fused.density_field_reused(self.geometry_bg, pts_c, X_all, out_all)
+        else:
+            t_dirs = rays_d[ray_indices]
+            positions = rays_o[ray_indices] + t_dirs * midpoints
+            density, feature = self.geometry_bg(positions)
         if self.fused and fused_radiance_bg(self.texture_bg):
             # the radiance kernel takes the direction by ray index, as the
             # foreground's does
@@ -414,12 +432,20 @@ class NeuSModel(nn.Module):
             rgb = fused.radiance_forward(self.texture_bg, feature.contiguous(), None, ri,
                                          rays_d.contiguous())
         else:
+            if t_dirs is None:
+                t_dirs = rays_d[ray_indices]
             rgb = self.texture_bg(feature, t_dirs)
-        weights = ops.render_weight_from_density(t0[:, None], t1[:, None], density[:, None], offsets)
-        opacity = ops.accumulate_along_rays(weights, offsets)
-        depth = ops.accumulate_along_rays(weights, offsets, midpoints)
-        comp_rgb = ops.accumulate_along_rays(weights, offsets, rgb)
-        comp_rgb = comp_rgb + self.background_color * (1.0 - opacity)
+        if self.fused:
+            from . import fused
+            comp_rgb, opacity, depth, weights = fused.density_composite(
+                density, rgb, t0, t1, offsets, self.background_color)
+            weights = weights[:, None]
+        else:
+            weights = ops.render_weight_from_density(t0[:, None], t1[:, None], density[:, None], offsets)
+            opacity = ops.accumulate_along_rays(weights, offsets)
+            depth = ops.accumulate_along_rays(weights, offsets, midpoints)
+            comp_rgb = ops.accumulate_along_rays(weights, offsets, rgb)
+            comp_rgb = comp_rgb + self.background_color * (1.0 - opacity)
         out = {"comp_rgb": comp_rgb, "opacity": opacity, "depth": depth, "rays_valid": opacity > 0,
                "num_samples": torch.full((1,), len(t0), dtype=torch.int32, device=rays_o.device)}
         if self.training:

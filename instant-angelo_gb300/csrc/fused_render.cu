@@ -800,9 +800,172 @@ __global__ void __launch_bounds__(256) comp_bwd_kernel(const __grid_constant__ C
     }
 }
 
+// ------------------------------------------- density compositing (background)
+// The learned background's compositing (models/neus.py:171-177 with nerfacc
+// 0.3.3 render_weight_from_density and accumulate_along_rays), one warp per
+// ray over chunks of 32 samples: tau_j = sigma_j (t1_j - t0_j), T_j =
+// exp(-(tau_0 + .. + tau_{j-1})) from a warp prefix sum carried across the
+// chunks, w_j = (1 - exp(-tau_j)) T_j; per ray opacity = sum w, depth =
+// sum w (t0 + t1) / 2, rgb = sum w rgb + bg (1 - opacity).  The backward
+// walks the chunks back to front with a warp suffix sum:
+// dL/dsigma_j = dt_j (g_j T_j exp(-tau_j) - sum_{k>j} g_k w_k),
+// g_j = dL/dw_j, dL/drgb_j = w_j dL/drgb.
+
+struct DCompParams {
+    const int64_t *off;
+    int64_t n_rays;
+    const float *sigma, *t0, *t1, *rgb, *bg;
+    float *opacity, *depth, *comp_rgb, *weights, *trans;
+    const float *g_opacity, *g_depth, *g_rgb;
+    float *d_sigma, *d_rgb;
+};
+
+__global__ void __launch_bounds__(256) dcomp_fwd_kernel(const __grid_constant__ DCompParams P) {
+    const int lane = threadIdx.x & 31;
+    const int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (ray >= P.n_rays) return;
+    const int64_t b = P.off[ray], e = P.off[ray + 1];
+    float carry = 0.f;   // optical depth before the chunk
+    float acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int64_t c0 = b; c0 < e; c0 += 32) {
+        const int64_t j = c0 + lane;
+        const bool v = j < e;
+        float tau = 0.f, tm = 0.f;
+        if (v) {
+            const float t0 = P.t0[j], t1 = P.t1[j];
+            tau = __fmul_rn(P.sigma[j], __fsub_rn(t1, t0));
+            tm = (t0 + t1) * 0.5f;
+        }
+        float incl = tau;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        float excl = __shfl_up_sync(0xffffffffu, incl, 1);
+        if (lane == 0) excl = 0.f;
+        const float T = expf(-(carry + excl));
+        if (v) {
+            const float w = (1.0f - expf(-tau)) * T;
+            P.weights[j] = w;
+            P.trans[j] = T;
+            const float *c = P.rgb + j * 3;
+            acc[0] += w;
+            acc[1] += w * tm;
+            acc[2] += w * c[0];
+            acc[3] += w * c[1];
+            acc[4] += w * c[2];
+        }
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) acc[k] = warp_sum(acc[k]);
+    if (lane == 0) {
+        P.opacity[ray] = acc[0];
+        P.depth[ray] = acc[1];
+        for (int k = 0; k < 3; ++k) P.comp_rgb[ray * 3 + k] = acc[2 + k] + P.bg[k] * (1.0f - acc[0]);
+    }
+}
+
+__global__ void __launch_bounds__(256) dcomp_bwd_kernel(const __grid_constant__ DCompParams P) {
+    const int lane = threadIdx.x & 31;
+    const int64_t ray = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (ray >= P.n_rays) return;
+    const int64_t b = P.off[ray], e = P.off[ray + 1];
+    float g_c[3], g_op = P.g_opacity ? P.g_opacity[ray] : 0.f;
+    const float g_dep = P.g_depth ? P.g_depth[ray] : 0.f;
+    for (int k = 0; k < 3; ++k) {
+        g_c[k] = P.g_rgb ? P.g_rgb[ray * 3 + k] : 0.f;
+        g_op -= g_c[k] * P.bg[k];   // rgb = .. + bg (1 - opacity)
+    }
+    float R = 0.f;   // sum of g_k w_k over the samples after the chunk
+    const int64_t n = e - b;
+    for (int64_t c0 = b + ((n - 1) / 32) * 32; n > 0 && c0 >= b; c0 -= 32) {
+        const int64_t j = c0 + lane;
+        const bool v = j < e;
+        float gw = 0.f, w = 0.f, tau = 0.f, T = 0.f, dt = 0.f;
+        if (v) {
+            const float t0 = P.t0[j], t1 = P.t1[j];
+            dt = __fsub_rn(t1, t0);
+            tau = __fmul_rn(P.sigma[j], dt);
+            const float tm = (t0 + t1) * 0.5f;
+            const float *c = P.rgb + j * 3;
+            w = P.weights[j];
+            T = P.trans[j];
+            gw = g_op + g_dep * tm + g_c[0] * c[0] + g_c[1] * c[1] + g_c[2] * c[2];
+            for (int k = 0; k < 3; ++k) P.d_rgb[j * 3 + k] = w * g_c[k];
+        }
+        // inclusive suffix sum of g w within the chunk, then exclusive
+        float suf = gw * w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const float y = __shfl_down_sync(0xffffffffu, suf, o);
+            if (lane + o < 32) suf += y;
+        }
+        float after = __shfl_down_sync(0xffffffffu, suf, 1);
+        if (lane == 31) after = 0.f;
+        if (v) P.d_sigma[j] = dt * (gw * T * expf(-tau) - (after + R));
+        R += __shfl_sync(0xffffffffu, suf, 0);
+    }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ host API
+
+extern "C" int angelo_density_composite_fwd(const int64_t *offsets, int64_t n_rays, const float *sigmas,
+                                            const float *t_starts, const float *t_ends, const float *rgb,
+                                            const float *bg, float *opacity, float *depth, float *comp_rgb,
+                                            float *weights, float *trans, void *stream) {
+    ANGELO_REQUIRE(n_rays >= 0, "density_composite_fwd: negative n_rays");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(offsets && sigmas && t_starts && t_ends && rgb && bg && opacity && depth && comp_rgb &&
+                       weights && trans,
+                   "density_composite_fwd: null pointer");
+    DCompParams P{};
+    P.off = offsets;
+    P.n_rays = n_rays;
+    P.sigma = sigmas;
+    P.t0 = t_starts;
+    P.t1 = t_ends;
+    P.rgb = rgb;
+    P.bg = bg;
+    P.opacity = opacity;
+    P.depth = depth;
+    P.comp_rgb = comp_rgb;
+    P.weights = weights;
+    P.trans = trans;
+    dcomp_fwd_kernel<<<blocks_for(n_rays * 32, 256), 256, 0, as_stream(stream)>>>(P);
+    return check_launch("density_composite_fwd");
+}
+
+extern "C" int angelo_density_composite_bwd(const int64_t *offsets, int64_t n_rays, const float *sigmas,
+                                            const float *t_starts, const float *t_ends, const float *rgb,
+                                            const float *bg, const float *weights, const float *trans,
+                                            const float *g_opacity, const float *g_depth, const float *g_rgb,
+                                            float *d_sigmas, float *d_rgb, void *stream) {
+    ANGELO_REQUIRE(n_rays >= 0, "density_composite_bwd: negative n_rays");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(offsets && sigmas && t_starts && t_ends && rgb && bg && weights && trans && d_sigmas && d_rgb,
+                   "density_composite_bwd: null pointer");
+    DCompParams P{};
+    P.off = offsets;
+    P.n_rays = n_rays;
+    P.sigma = sigmas;
+    P.t0 = t_starts;
+    P.t1 = t_ends;
+    P.rgb = rgb;
+    P.bg = bg;
+    P.weights = const_cast<float *>(weights);   // read only in the backward
+    P.trans = const_cast<float *>(trans);
+    P.g_opacity = g_opacity;
+    P.g_depth = g_depth;
+    P.g_rgb = g_rgb;
+    P.d_sigma = d_sigmas;
+    P.d_rgb = d_rgb;
+    dcomp_bwd_kernel<<<blocks_for(n_rays * 32, 256), 256, 0, as_stream(stream)>>>(P);
+    return check_launch("density_composite_bwd");
+}
 
 namespace angelo {
 // CTAs of the radiance kernels that stopped waiting for the tensor cores

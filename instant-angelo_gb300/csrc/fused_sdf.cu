@@ -383,6 +383,10 @@ __global__ void __launch_bounds__(kEncThreads, ANGELO_ENCODE_MIN_BLOCKS)
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
             const int d = k >> 1;
+            // a curvature tap whose pair clamps to one point: neither its
+            // encoding nor its Jacobian is read (the MLP kernels stage a zero
+            // row for it, the scatter skips it)
+            if (GROUP == kCurv && coincident_taps(base[d], r, eps)) continue;
             float xc[3];
             int m, delta;
             tap_point(r, eps, base, e0 + k, xc, &m);
@@ -531,11 +535,19 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
         const int ek = e0 + (int)(k % ne);
         const bool vk = sk < P.S;
         if (slice < KH) {
+            // a dead curvature tap's row is zero: the encode wrote nothing
+            // for it, and both taps of the pair get the same output
+            bool xk = vk;
+            if (GROUP == kCurv && vk) {
+                float b[3];
+                item_base(sk, b);
+                xk = !coincident_taps(b[(ek - 7) >> 1], r_, eps);
+            }
             float x[16];
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int l = 8 * slice + j;
-                const float2 f = (vk && l < P.active) ? __ldg(P.X + xidx(P, ek, l, sk)) : make_float2(0.f, 0.f);
+                const float2 f = (xk && l < P.active) ? __ldg(P.X + xidx(P, ek, l, sk)) : make_float2(0.f, 0.f);
                 x[2 * j] = f.x;
                 x[2 * j + 1] = f.y;
             }
@@ -921,10 +933,13 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
 #pragma unroll
         for (int j = 0; j < 16; ++j) xv[j] = 0.f;
         if (slice < KH) {
+            // a dead curvature tap's row is zero (its encoding is not written)
+            bool xk = v;
+            if (GROUP == kCurv && v) xk = !coincident_taps(P.state[s * kState + 13 + ((e - 7) >> 1)], r_, eps);
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int l = 8 * slice + j;
-                const float2 f = (v && l < P.active) ? __ldg(P.X + xidx(P, e, l, s)) : make_float2(0.f, 0.f);
+                const float2 f = (xk && l < P.active) ? __ldg(P.X + xidx(P, e, l, s)) : make_float2(0.f, 0.f);
                 xv[2 * j] = f.x;
                 xv[2 * j + 1] = f.y;
             }
@@ -1148,7 +1163,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
 #pragma unroll
                 for (int j = 0; j < CPS / 2; ++j) {
                     const int l = (CPS / 2) * slice + j;
-                    if (!v || l >= P.active) continue;
+                    // a dead tap has no Jacobian (and dL/dX = 0)
+                    if (dead || l >= P.active) continue;
                     const float sc = P.lay.scales[l] * inv2r;
 #pragma unroll
                     for (int dd = 0; dd < 3; ++dd) {

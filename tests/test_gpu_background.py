@@ -97,6 +97,51 @@ def test_density_weights_match_fp64(dev):
     np.testing.assert_allclose(s.grad.cpu().numpy(), s64.grad.numpy(), rtol=1e-4, atol=1e-5)
 
 
+def test_fused_density_composite_matches_fp64(dev):
+    """The fused background compositing (weights from density, opacity,
+    depth, colour and the background blend in one kernel each way) against
+    float64 autograd of the same formulas, with empty and long rays."""
+    from angelo_gb import fused
+    from oracle import neus_fp64 as O
+    g = np.random.default_rng(43)
+    counts = g.integers(0, 300, 200)
+    counts[:4] = 0
+    counts[4] = 1
+    off = np.zeros(201, np.int64)
+    np.cumsum(counts, out=off[1:])
+    n = int(off[-1])
+    dt = g.uniform(0.001, 0.2, n).astype(np.float32)
+    t0 = np.zeros(n, np.float32)
+    for r in range(200):
+        seg = slice(off[r], off[r + 1])
+        t0[seg] = np.cumsum(np.concatenate([[0.5], dt[seg][:-1]])).astype(np.float32)
+    t1 = (t0 + dt).astype(np.float32)
+    sigma = np.exp(g.normal(size=n) - 0.5).astype(np.float32)
+    rgb = g.uniform(0, 1, (n, 3)).astype(np.float32)
+    bg = np.array([0.2, 0.5, 0.8], np.float32)
+    gc, go, gd = g.normal(size=(200, 3)), g.normal(size=(200, 1)), g.normal(size=(200, 1))
+    tt = lambda a: torch.from_numpy(a).to(dev)  # noqa: E731
+    s_, c_ = tt(sigma).requires_grad_(True), tt(rgb).requires_grad_(True)
+    comp, op, dep, w = fused.density_composite(s_, c_, tt(t0), tt(t1), tt(off), tt(bg))
+    ((comp * tt(gc.astype(np.float32))).sum() + (op * tt(go.astype(np.float32))).sum()
+     + (dep * tt(gd.astype(np.float32))).sum()).backward()
+    s64 = torch.from_numpy(sigma.astype(np.float64)).requires_grad_(True)
+    c64 = torch.from_numpy(rgb.astype(np.float64)).requires_grad_(True)
+    w64 = O.density_weights(torch.from_numpy(t0).double(), torch.from_numpy(t1).double(), s64, list(off))
+    mid = (torch.from_numpy(t0).double() + torch.from_numpy(t1).double()) * 0.5
+    ridx = torch.repeat_interleave(torch.arange(200), torch.from_numpy(counts))
+    op64 = torch.zeros(200, 1, dtype=torch.float64).index_add(0, ridx, w64[:, None])
+    dep64 = torch.zeros(200, 1, dtype=torch.float64).index_add(0, ridx, (w64 * mid)[:, None])
+    comp64 = torch.zeros(200, 3, dtype=torch.float64).index_add(0, ridx, w64[:, None] * c64)
+    comp64 = comp64 + torch.from_numpy(bg).double() * (1.0 - op64)
+    ((comp64 * torch.from_numpy(gc)).sum() + (op64 * torch.from_numpy(go)).sum()
+     + (dep64 * torch.from_numpy(gd)).sum()).backward()
+    for a, b in ((w, w64), (op, op64), (dep, dep64), (comp, comp64)):
+        np.testing.assert_allclose(a.detach().cpu().numpy(), b.detach().numpy(), rtol=2e-5, atol=2e-6)
+    np.testing.assert_allclose(s_.grad.cpu().numpy(), s64.grad.numpy(), rtol=2e-4, atol=2e-5)
+    np.testing.assert_allclose(c_.grad.cpu().numpy(), c64.grad.numpy(), rtol=2e-5, atol=2e-6)
+
+
 def _model(dev, fused):
     from angelo_gb import models, workloads
     cfg = workloads.model_config("small", fused=fused, **workloads.background(
