@@ -477,9 +477,12 @@ int angelo_mlp_fused_fwd(int32_t in_dim, int32_t n_hidden, int32_t out_dim, cons
 /* Backward from dL/dout (g_out, row stride g_stride): writes dL/dx (d_x, row
  * stride dx_stride; may be NULL) and ACCUMULATES dL/dW into d_net
  * (angelo_mlp_grad_size floats).  The hidden activations are recomputed
- * from x. */
+ * from x; with x_rows (may be NULL), row i of the call reads x row
+ * x_rows[i] (the inputs of a subset of an earlier forward's rows, without
+ * copying them out). */
 int angelo_mlp_fused_bwd(int32_t in_dim, int32_t n_hidden, int32_t out_dim, const void *net,
-                         const float *x, int64_t x_stride, int64_t n, const float *g_out,
+                         const float *x, int64_t x_stride, const int32_t *x_rows, int64_t n,
+                         const float *g_out,
                          int64_t g_stride, float *d_x, int64_t dx_stride, float *d_net,
                          void *stream);
 

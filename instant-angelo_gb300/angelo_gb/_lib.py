@@ -143,8 +143,8 @@ SIGNATURES = {
     "angelo_mlp_grad_size": (c_i64, [c_i32, c_i32, c_i32]),
     "angelo_mlp_prep": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "angelo_mlp_fused_fwd": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_i64, c_i64, c_vp, c_i64, c_vp]),
-    "angelo_mlp_fused_bwd": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_i64, c_i64, c_vp, c_i64, c_vp,
-                                     c_i64, c_vp, c_vp]),
+    "angelo_mlp_fused_bwd": (c_i32, [c_i32, c_i32, c_i32, c_vp, c_vp, c_i64, c_vp, c_i64, c_vp, c_i64,
+                                     c_vp, c_i64, c_vp, c_vp]),
     "angelo_density_composite_fwd": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                              c_vp, c_vp, c_vp, c_vp]),
     "angelo_density_composite_bwd": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,

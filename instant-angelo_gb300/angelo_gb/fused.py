@@ -359,7 +359,7 @@ class _FusedMlp(torch.autograd.Function):
         d_x = torch.empty_like(x) if ctx.needs_input_grad[0] else None
         d_net = torch.zeros(net.grad_size, device=x.device)
         call("angelo_mlp_fused_bwd", net.in_dim, net.n_hidden, net.out_dim, _p(net.buf), _p(x),
-             x.stride(0), n, _p(g_out), g_out.stride(0), _p(d_x),
+             x.stride(0), None, n, _p(g_out), g_out.stride(0), _p(d_x),
              d_x.stride(0) if d_x is not None else 0, _p(d_net), _s(x.device),
              units=dict(n=n, in_dim=net.in_dim, n_hidden=net.n_hidden, out_dim=net.out_dim, bwd=True))
         flat = []
@@ -398,40 +398,44 @@ class _ReusedDensityField(torch.autograd.Function):
     from the kept encodings and scatters dL/dX into the hash table."""
 
     @staticmethod
-    def forward(ctx, pts, X, out, table, meta, *weights):
-        ctx.save_for_backward(pts, X, table)
+    def forward(ctx, pts, X, rows, out, table, meta, *weights):
+        ctx.save_for_backward(pts, X, rows, table)
         ctx.meta = meta
         return out.clone()
 
     @staticmethod
     def backward(ctx, g_out):
-        pts, X, table = ctx.saved_tensors
+        pts, X, rows, table = ctx.saved_tensors
         net, spec, active, xyz = ctx.meta["net"], ctx.meta["spec"], ctx.meta["active"], ctx.meta["xyz"]
-        n = X.shape[0]
+        n = rows.shape[0]
         g = g_out.contiguous().float()
-        dX = torch.empty_like(X)
+        dX = torch.empty(n, X.shape[1], device=X.device)
         d_net = torch.zeros(net.grad_size, device=X.device)
+        # the kept rows' encodings are read in place from the visibility
+        # pass's X through their row indices
         call("angelo_mlp_fused_bwd", net.in_dim, net.n_hidden, net.out_dim, _p(net.buf), _p(X),
-             X.stride(0), n, _p(g), g.stride(0), _p(dX), dX.stride(0), _p(d_net), _s(X.device),
+             X.stride(0), _p(rows), n, _p(g), g.stride(0), _p(dX), dX.stride(0), _p(d_net), _s(X.device),
              units=dict(n=n, in_dim=net.in_dim, n_hidden=net.n_hidden, out_dim=net.out_dim, bwd=True))
         dtable = None
-        if ctx.needs_input_grad[3] and active > 0:
+        need_table = ctx.needs_input_grad[4]
+        if need_table and active > 0:
             dtable = torch.zeros(spec.n_params, device=X.device, dtype=torch.float32)
             call("angelo_hashgrid_bwd", ctypes.byref(spec.layout), int(active), _p(pts), n, _p(table),
                  _table_dtype(table), int(xyz), _p(dX), dX.stride(0), 0, _p(dtable), None, _s(X.device),
                  units=dict(n=n, active=int(active), L=spec.n_levels, tbytes=table.element_size(),
                             dtable=True, dx=False))
-        elif ctx.needs_input_grad[3]:
+        elif need_table:
             dtable = torch.zeros(spec.n_params, device=X.device, dtype=torch.float32)
         flat = []
         for dW, db in net.unpack_grads(d_net):
             flat += [dW, db]
-        return (None, None, None, dtable, None, *flat)
+        return (None, None, None, None, dtable, None, *flat)
 
 
-def density_field_reused(geom, pts, X, out):
+def density_field_reused(geom, pts, X, rows, out):
     """VolumeDensity's (density, feature) on kept samples from the visibility
-    pass's contracted points, encodings and MLP outputs (see
+    pass: their contracted points and MLP outputs, and the visibility pass's
+    encodings X of every sample with the kept rows' indices (see
     _ReusedDensityField); differentiable w.r.t. the hash table and the MLP."""
     enc, mlp = geom.encoding_with_network.encoding, geom.encoding_with_network.network
     grid = enc.encoding
@@ -440,8 +444,8 @@ def density_field_reused(geom, pts, X, out):
     for W, b in mlp.effective_weights():
         weights += [W, b]
     meta = dict(net=net, spec=grid.encoding.spec, active=int(grid.mask_levels), xyz=bool(enc.include_xyz))
-    o = _ReusedDensityField.apply(pts.contiguous(), X.contiguous(), out.contiguous(), grid.encoding.params,
-                                  meta, *weights)
+    o = _ReusedDensityField.apply(pts.contiguous(), X.contiguous(), rows.to(torch.int32).contiguous(),
+                                  out.contiguous(), grid.encoding.params, meta, *weights)
     return geom.outputs(o)
 
 

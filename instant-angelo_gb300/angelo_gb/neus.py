@@ -410,8 +410,9 @@ class NeuSModel(nn.Module):
             kidx = keep.nonzero().squeeze(1)
             ri, t0, t1 = ri.index_select(0, kidx), t0.index_select(0, kidx), t1.index_select(0, kidx)
             if reuse:
-                pts_c, X_all, out_all = (pts_c.index_select(0, kidx), X_all.index_select(0, kidx),
-                                         out_all.index_select(0, kidx))
+                # the encodings stay where they are: the backward reads the
+                # kept rows through kidx
+                pts_c, out_all = pts_c.index_select(0, kidx), out_all.index_select(0, kidx)
             offsets = ops.offsets_from_ray_indices(ri, n_rays)
             self._last_march_bg = (offsets, ri, t0, t1)
         ray_indices = ri.long()
@@ -420,7 +421,7 @@ class NeuSModel(nn.Module):
         t_dirs = None
         if reuse:
             from . import fused
-            density, feature = fused.density_field_reused(self.geometry_bg, pts_c, X_all, out_all)
+            density, feature = fused.density_field_reused(self.geometry_bg, pts_c, X_all, kidx, out_all)
         else:
             t_dirs = rays_d[ray_indices]
             positions = rays_o[ray_indices] + t_dirs * midpoints

@@ -109,6 +109,7 @@ struct MlpParams {
     const char *net;
     const float *x;
     int64_t x_stride;
+    const int32_t *x_rows;   // row r reads x row x_rows[r] (NULL: row r)
     int64_t S;
     float *out;
     int64_t out_stride;
@@ -159,7 +160,7 @@ __device__ __forceinline__ void mlp_stage_x(const MlpParams &P, int64_t s, bool 
 #pragma unroll
         for (int j = 0; j < 16; ++j) x[j] = 0.f;
         if (v) {
-            const float *src = P.x + s * P.x_stride;
+            const float *src = P.x + (P.x_rows ? (int64_t)P.x_rows[s] : s) * P.x_stride;
 #pragma unroll
             for (int j = 0; j < 16; ++j)
                 if (c0 + j < P.L.in_dim) x[j] = __ldg(src + c0 + j);
@@ -579,7 +580,8 @@ extern "C" int angelo_mlp_fused_fwd(int32_t in_dim, int32_t n_hidden, int32_t ou
 }
 
 extern "C" int angelo_mlp_fused_bwd(int32_t in_dim, int32_t n_hidden, int32_t out_dim, const void *net,
-                                    const float *x, int64_t x_stride, int64_t n, const float *g_out,
+                                    const float *x, int64_t x_stride, const int32_t *x_rows, int64_t n,
+                                    const float *g_out,
                                     int64_t g_stride, float *d_x, int64_t dx_stride, float *d_net,
                                     void *stream) {
     MlpLayout L;
@@ -594,6 +596,7 @@ extern "C" int angelo_mlp_fused_bwd(int32_t in_dim, int32_t n_hidden, int32_t ou
     P.net = reinterpret_cast<const char *>(net);
     P.x = x;
     P.x_stride = x_stride;
+    P.x_rows = x_rows;
     P.S = n;
     P.g_out = g_out;
     P.g_stride = g_stride;

@@ -1125,15 +1125,15 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
         pending1 = true;
         if (!(alive = tc_wait_all(&bar[0], ph0))) break;
         ph0 ^= 1;
+        constexpr int CPS = 4 * KH;   // dL/dX columns of a slice
+        float dxs[CPS];
         {
             // dL/dX of hash levels (CPS / 2) slice .. : all four slices
-            constexpr int CPS = 4 * KH;
-            float dx[CPS];
-            tc::ldn(tmem + lane_off + Sh::tB + CPS * slice, dx);
+            tc::ldn(tmem + lane_off + Sh::tB + CPS * slice, dxs);
 #pragma unroll
             for (int j = 0; j < CPS / 2; ++j) {
                 const int l = (CPS / 2) * slice + j;
-                if (v && l < P.active) P.dX[xidx(P, e, l, s)] = make_float2(dx[2 * j], dx[2 * j + 1]);
+                if (v && l < P.active) P.dX[xidx(P, e, l, s)] = make_float2(dxs[2 * j], dxs[2 * j + 1]);
             }
         }
         if (GROUP == kCurv) {
@@ -1149,11 +1149,9 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
                     if ((m >> d) & 1) dsh[d] += 2.f * dx[d] * inv2r;
             }
             {
-                // tcgen05.ld is warp-collective: every lane loads, only the
-                // rows of valid samples use the values
-                constexpr int CPS = 4 * KH;
-                float dx[CPS];
-                tc::ldn(tmem + lane_off + Sh::tB + CPS * slice, dx);
+                // this slice's dL/dX (dxs, loaded by every lane above: the
+                // load is warp-collective); only live rows use it
+                const float *dx = dxs;
                 const int k6 = e - 7;
 #pragma unroll
                 for (int j = 0; j < CPS / 2; ++j) {

@@ -178,3 +178,28 @@ def test_fused_mlp_deterministic_rows(dev):
         idx = torch.randperm(5000, device=dev)[:1234]
         b = m(x[idx])
     assert torch.equal(a[idx], b)
+
+
+def test_fused_mlp_backward_reads_rows_by_index(dev):
+    """angelo_mlp_fused_bwd with x_rows (the background's kept samples read
+    in place from the visibility pass's encodings) equals the backward on the
+    gathered rows: dL/dx bit for bit, dL/dW up to the CTAs' atomic order."""
+    from angelo_gb import _lib, fused
+    from angelo_gb.ops import _p, _s
+    m = _mlp(35, 1, 8, seed=21).to(dev)
+    g = torch.Generator(device="cpu").manual_seed(22)
+    X = (torch.rand(20000, 35, generator=g) * 2 - 1).to(dev)
+    rows = torch.randperm(20000, generator=g)[:7777].sort().values.to(dev)
+    gout = torch.randn(7777, 8, generator=g).to(dev)
+    net = fused.MlpNet(35, 1, 8, dev)
+    net.prepare(m.effective_weights())
+    outs = []
+    for x, r in ((X.index_select(0, rows).contiguous(), None), (X, rows.to(torch.int32))):
+        dx = torch.empty(7777, 35, device=dev)
+        dn = torch.zeros(net.grad_size, device=dev)
+        _lib.call("angelo_mlp_fused_bwd", 35, 1, 8, _p(net.buf), _p(x), x.stride(0), _p(r), 7777,
+                  _p(gout), gout.stride(0), _p(dx), dx.stride(0), _p(dn), _s(dev))
+        outs.append((dx, dn))
+    torch.cuda.synchronize()
+    assert torch.equal(outs[0][0], outs[1][0])
+    assert float((outs[0][1] - outs[1][1]).abs().max()) <= 1e-5 * float(outs[0][1].abs().max())
