@@ -112,6 +112,7 @@ struct RadParams {
     int dual;
     int passes;   // forward tensor-core products per layer: 3 (hi/lo x3) or 1 (hi parts alone)
     int fp16;     // forward operands fp16 (the buffer prepared in fp16) instead of bf16
+    int vec4;     // feature / d_feature rows start 16-byte aligned: 4-float accesses
     float *rgb;
     const float *g_rgb;
     float *d_feature;
@@ -152,8 +153,21 @@ __device__ __forceinline__ void rad_stage_x(const RadParams &P, int64_t s, bool 
     for (int b = slice; b < KT1; b += 4) {
         const int c0 = 16 * b;
         float x[16];
+        const float *frow = P.feature + (v ? s : 0) * P.feat_stride;
 #pragma unroll
-        for (int j = 0; j < 16; ++j) x[j] = (v && c0 + j < F) ? P.feature[s * P.feat_stride + c0 + j] : 0.f;
+        for (int q = 0; q < 4; ++q) {
+            const int c = c0 + 4 * q;
+            if (v && P.vec4 && c + 3 < F) {
+                const float4 f = __ldg(reinterpret_cast<const float4 *>(frow + c));
+                x[4 * q] = f.x;
+                x[4 * q + 1] = f.y;
+                x[4 * q + 2] = f.z;
+                x[4 * q + 3] = f.w;
+            } else {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) x[4 * q + t] = (v && c + t < F) ? frow[c + t] : 0.f;
+            }
+        }
         if (v && c0 + 16 > F && c0 < F + 19) {
             float sh[16], nrm[3];
             rad_sh_normal(P, s, sh, nrm);
@@ -292,16 +306,27 @@ __device__ __forceinline__ void rad_dx_out(const RadParams &P, int64_t s, int b,
     const int F = P.L.feat_dim;
     float dn[3] = {0.f, 0.f, 0.f};
     bool has_n = false;
+    float o[16];
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
         const int c = 16 * b + j;
-        if (c < F) {
-            float o = dx[j];
-            if (P.dual && c >= 1 && c <= 3) o += dual_g[c - 1];
-            P.d_feature[s * P.feat_stride + c] = o;
-        } else if (c >= F + 16 && c < F + 19) {
+        o[j] = dx[j];
+        if (P.dual && c >= 1 && c <= 3) o[j] += dual_g[c - 1];
+        if (c >= F + 16 && c < F + 19) {
             dn[c - F - 16] = dx[j];
             has_n = true;
+        }
+    }
+    float *drow = P.d_feature + s * P.feat_stride;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int c = 16 * b + 4 * q;
+        if (P.vec4 && c + 3 < F) {
+            *reinterpret_cast<float4 *>(drow + c) = make_float4(o[4 * q], o[4 * q + 1], o[4 * q + 2], o[4 * q + 3]);
+        } else {
+#pragma unroll
+            for (int t = 0; t < 4; ++t)
+                if (c + t < F) drow[c + t] = o[4 * q + t];
         }
     }
     if (!has_n || !P.d_grad) return;
@@ -1063,6 +1088,7 @@ extern "C" int angelo_radiance_fwd(int32_t feat_dim, const void *net, const floa
     P.dual = flags & 1;
     P.passes = (flags & 2) ? 1 : 3;
     P.fp16 = (flags & 4) != 0;
+    P.vec4 = (feat_stride % 4 == 0) && (reinterpret_cast<uintptr_t>(feature) % 16 == 0);
     P.rgb = rgb;
     return dispatch_rad<false>(P, as_stream(stream));
 }
@@ -1091,6 +1117,8 @@ extern "C" int angelo_radiance_bwd(int32_t feat_dim, const void *net, const floa
     P.d_feature = d_feature;
     P.d_grad = d_grad;
     P.d_net = d_net;
+    P.vec4 = (feat_stride % 4 == 0) && (reinterpret_cast<uintptr_t>(feature) % 16 == 0) &&
+             (reinterpret_cast<uintptr_t>(d_feature) % 16 == 0);
     return dispatch_rad<true>(P, as_stream(stream));
 }
 

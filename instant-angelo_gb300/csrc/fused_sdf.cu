@@ -162,6 +162,7 @@ struct SdfParams {
     // outputs
     float *sdf, *grad, *feature, *laplace;
     int64_t feat_stride;
+    int feat_vec4, gfeat_vec4;   // feature / dL/dfeature rows 16-byte aligned: 4-float accesses
     // forward workspace
     float2 *X;        // encodings, X[(e * n_levels + l) * S + s]
     float2 *J;        // curvature taps: d(encoding)/d(cell fraction),
@@ -621,10 +622,23 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
                     tc::ld16(tmem + lane_off + 128 + 16 * q, y);
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
-                        const int col = 16 * q + j;
-                        const float val = y[j] + bias[128 + col];
-                        if (col == 0) s13[row] = val;
-                        if (v && col < od) P.feature[s * P.feat_stride + col] = val;
+                        y[j] += bias[128 + 16 * q + j];
+                        if (16 * q + j == 0) s13[row] = y[j];
+                    }
+                    if (v) {
+                        float *frow = P.feature + s * P.feat_stride;
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            const int c = 16 * q + 4 * t;
+                            if (P.feat_vec4 && c + 3 < od) {
+                                *reinterpret_cast<float4 *>(frow + c) =
+                                    make_float4(y[4 * t], y[4 * t + 1], y[4 * t + 2], y[4 * t + 3]);
+                            } else {
+#pragma unroll
+                                for (int u = 0; u < 4; ++u)
+                                    if (c + u < od) frow[c + u] = y[4 * t + u];
+                            }
+                        }
                     }
                 }
                 if (v && slice == 0) {
@@ -1010,12 +1024,26 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
             for (int q = slice; q < N3 / 16; q += 4) {
                 float yv[16];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const int col = 16 * q + j;
-                    float g = (v && col < od && P.g_feature) ? P.g_feature[s * P.gfeat_stride + col] : 0.f;
-                    if (col == 0) g += d0;
-                    yv[j] = g;
+                for (int j = 0; j < 16; ++j) yv[j] = 0.f;
+                if (v && P.g_feature) {
+                    const float *grow = P.g_feature + s * P.gfeat_stride;
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) {
+                        const int c = 16 * q + 4 * t;
+                        if (P.gfeat_vec4 && c + 3 < od) {
+                            const float4 g4 = __ldg(reinterpret_cast<const float4 *>(grow + c));
+                            yv[4 * t] = g4.x;
+                            yv[4 * t + 1] = g4.y;
+                            yv[4 * t + 2] = g4.z;
+                            yv[4 * t + 3] = g4.w;
+                        } else {
+#pragma unroll
+                            for (int u = 0; u < 4; ++u)
+                                if (c + u < od) yv[4 * t + u] = grow[c + u];
+                        }
+                    }
                 }
+                if (q == 0) yv[0] += d0;
                 stage16_2(ys, row, 16 * q, N3, Sh::CY, yv);
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
@@ -1569,6 +1597,7 @@ extern "C" int angelo_sdf_stencil_fwd(const angelo_hashgrid_layout_t *lay, int32
     P.grad = grad;
     P.feature = feature;
     P.feat_stride = feat_stride;
+    P.feat_vec4 = (feat_stride % 4 == 0) && (reinterpret_cast<uintptr_t>(feature) % 16 == 0);
     P.laplace = laplace;
     P.X = reinterpret_cast<float2 *>(workspace);
     P.state = workspace + 2 * n_evals(with_grad, with_laplace) * lay->n_levels * n;
@@ -1653,6 +1682,7 @@ extern "C" int angelo_sdf_stencil_bwd(const angelo_hashgrid_layout_t *lay, int32
     P.g_grad = g_grad;
     P.g_feature = g_feature;
     P.gfeat_stride = gfeat_stride;
+    P.gfeat_vec4 = (gfeat_stride % 4 == 0) && (reinterpret_cast<uintptr_t>(g_feature) % 16 == 0);
     P.g_laplace = g_laplace;
     P.d_table = d_table;
     P.d_net = d_net;
