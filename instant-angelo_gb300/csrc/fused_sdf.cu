@@ -350,8 +350,12 @@ template <int GROUP>
 __global__ void __launch_bounds__(kEncThreads, ANGELO_ENCODE_MIN_BLOCKS)
     stencil_encode_kernel(const __grid_constant__ SdfParams P) {
     const int l = blockIdx.y;
-    const int64_t s = (int64_t)blockIdx.x * kEncThreads + threadIdx.x;
-    if (s >= P.S) return;
+    // position p of the pass; the curvature pass visits its samples in the
+    // dead-tap order and keeps X and J by position, so that the MLP kernels'
+    // rows (consecutive positions) read them coalesced
+    const int64_t pidx = (int64_t)blockIdx.x * kEncThreads + threadIdx.x;
+    if (pidx >= P.S) return;
+    const int64_t s = (GROUP == kCurv && P.perm) ? (int64_t)P.perm[pidx] : pidx;
     const float r = P.radius, eps = P.eps;
     const float *src = GROUP == kCurv ? P.state + s * kState + 13 : P.pos + s * 3;
     const float base[3] = {src[0], src[1], src[2]};
@@ -418,10 +422,10 @@ __global__ void __launch_bounds__(kEncThreads, ANGELO_ENCODE_MIN_BLOCKS)
                     }
                 }
             }
-            P.X[xidx(P, e0 + k, l, s)] = f;
+            P.X[xidx(P, e0 + k, l, pidx)] = f;
             if (GROUP == kCurv) {
 #pragma unroll
-                for (int dd = 0; dd < 3; ++dd) P.J[((int64_t)(k * P.lay.n_levels + l) * 3 + dd) * P.S + s] = jac[dd];
+                for (int dd = 0; dd < 3; ++dd) P.J[((int64_t)(k * P.lay.n_levels + l) * 3 + dd) * P.S + pidx] = jac[dd];
             }
         }
     }
@@ -541,7 +545,8 @@ __global__ void __launch_bounds__(kTcThreads, 2) sdf_mlp_fwd_kernel(const __grid
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int l = 8 * slice + j;
-                const float2 f = (vk && l < P.active) ? __ldg(P.X + xidx(P, ek, l, sk)) : make_float2(0.f, 0.f);
+                const float2 f = (vk && l < P.active) ? __ldg(P.X + xidx(P, ek, l, GROUP == kCurv ? item_pos(k) : sk))
+                                                      : make_float2(0.f, 0.f);
                 x[2 * j] = f.x;
                 x[2 * j + 1] = f.y;
             }
@@ -929,10 +934,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
     // layer-1 operand of item k (slice q < KH: hash levels 8q .. 8q + 7; slice
     // KH: xyz) into registers; issued two rounds before it is staged
     // position k of the pass -> sample (the curvature pass in P.perm's order)
+    auto item_pos = [&](int64_t k) { return (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row; };
     auto item_sample = [&](int64_t k) {
-        const int64_t pk = (blockIdx.x + (k / ne) * (int64_t)gridDim.x) * 128 + row;
+        const int64_t pk = item_pos(k);
         return (GROUP == kCurv && P.perm && pk < P.S) ? (int64_t)P.perm[pk] : pk;
     };
+    // the row of X, J and dX: the position (the curvature pass keeps them by
+    // position in its sample order), else the sample
+    auto item_row = [&](int64_t k, int64_t sk) { return GROUP == kCurv ? item_pos(k) : sk; };
     auto load_x = [&](int64_t k, float (&xv)[16]) {
         const int64_t s = item_sample(k);
         const bool v = s < P.S;
@@ -943,7 +952,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 const int l = 8 * slice + j;
-                const float2 f = (v && l < P.active) ? __ldg(P.X + xidx(P, e, l, s)) : make_float2(0.f, 0.f);
+                const float2 f = (v && l < P.active) ? __ldg(P.X + xidx(P, e, l, item_row(k, s))) : make_float2(0.f, 0.f);
                 xv[2 * j] = f.x;
                 xv[2 * j + 1] = f.y;
             }
@@ -1155,13 +1164,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
         ph0 ^= 1;
         constexpr int CPS = 4 * KH;   // dL/dX columns of a slice
         float dxs[CPS];
+        const int64_t xr = item_row(k, s);   // this item's row of dX and J
         {
             // dL/dX of hash levels (CPS / 2) slice .. : all four slices
             tc::ldn(tmem + lane_off + Sh::tB + CPS * slice, dxs);
 #pragma unroll
             for (int j = 0; j < CPS / 2; ++j) {
                 const int l = (CPS / 2) * slice + j;
-                if (v && l < P.active) P.dX[xidx(P, e, l, s)] = make_float2(dxs[2 * j], dxs[2 * j + 1]);
+                if (v && l < P.active) P.dX[xidx(P, e, l, xr)] = make_float2(dxs[2 * j], dxs[2 * j + 1]);
             }
         }
         if (GROUP == kCurv) {
@@ -1190,7 +1200,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) sdf_mlp_bwd_tc_kernel(const __g
 #pragma unroll
                     for (int dd = 0; dd < 3; ++dd) {
                         if (!((m >> dd) & 1)) continue;
-                        const float2 jv = __ldg(P.J + ((int64_t)(k6 * P.lay.n_levels + l) * 3 + dd) * P.S + s);
+                        const float2 jv = __ldg(P.J + ((int64_t)(k6 * P.lay.n_levels + l) * 3 + dd) * P.S + xr);
                         dsh[dd] += sc * (dx[2 * j] * jv.x + dx[2 * j + 1] * jv.y);
                     }
                 }
@@ -1255,9 +1265,12 @@ __device__ __forceinline__ void centre_add(float2 (&acc)[8], int delta, int cc, 
 template <int GROUP>
 __device__ __forceinline__ void scatter_body(const SdfParams &P) {
     const int l = blockIdx.y;
+    // position s of the pass (the curvature pass: its dead-tap order, in which
+    // dL/dX is kept; the sample is perm[s])
     const int64_t s = (int64_t)blockIdx.x * kEncThreads + threadIdx.x;
     const bool valid = s < P.S;
-    const int64_t sv = valid ? s : P.S - 1;   // lanes past the end stay for the warp-collective adds
+    const int64_t pv = valid ? s : P.S - 1;   // lanes past the end stay for the warp-collective adds
+    const int64_t sv = (GROUP == kCurv && P.perm) ? (int64_t)P.perm[pv] : pv;
     const float r = P.radius, eps = P.eps;
     const float *src = GROUP == kCurv ? P.state + sv * kState + 13 : P.pos + sv * 3;
     const float base[3] = {src[0], src[1], src[2]};
@@ -1496,8 +1509,8 @@ int run_fwd(const SdfParams &P, cudaStream_t s) {
         if ((rc = launch_mlp_fwd<KH, NH, NT3, kPoint>(P, s)) != ANGELO_OK) return rc;
     }
     if (P.with_laplace) {
-        if ((rc = launch_encode<kCurv>(P, s)) != ANGELO_OK) return rc;
         if ((rc = launch_perm(P, s)) != ANGELO_OK) return rc;
+        if ((rc = launch_encode<kCurv>(P, s)) != ANGELO_OK) return rc;
         if ((rc = launch_mlp_fwd<KH, NH, NT3, kCurv>(P, s)) != ANGELO_OK) return rc;
     }
     return ANGELO_OK;

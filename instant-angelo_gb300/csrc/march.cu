@@ -16,6 +16,21 @@ using namespace angelo;
 
 namespace {
 
+// lanes per ray of the AABB grid's march (1: the sequential march itself)
+#ifndef ANGELO_MARCH_AABB_LANES
+#define ANGELO_MARCH_AABB_LANES 1
+#endif
+constexpr int kAabbLanes = ANGELO_MARCH_AABB_LANES;
+
+// The march kernels map a group of G lanes to a ray (G = 32: a warp) or one
+// thread to a ray (G = 1).
+// The launch picks the warp for the unbounded-sphere grid (the learned
+// background: no empty-space skipping, so every round of the warp's
+// lookahead is a full run of 32 steps) and one thread per ray for the AABB
+// grid, whose steps alternate between short runs of occupied steps and DDA
+// skips (measured: the warp form took the foreground's march from 0.25 to
+// 0.38 ms per step, the background's from ~0.19 to ~0.06).
+
 struct Grid {
     float lo[3], hi[3];
     int res[3];
@@ -142,6 +157,121 @@ __device__ __forceinline__ int64_t march_ray(const Grid &g, const float o[3], co
     return j;
 }
 
+// The same march with one warp per ray.  The recurrence stays sequential in
+// its arithmetic, but the occupancy lookups need not wait for each other:
+// each round, lane k takes the march state k steps ahead of the warp's state,
+// assuming the next k steps are all of the current kind (advance within
+// occupied cells, or DDA skips over empty ones), by applying the sequential
+// update k times with the same rounding; all 32 lanes then look their cell up
+// at once.  The first lane whose step is of the other kind (or past the far
+// plane or the step limit) ends the round: the steps before it are the
+// sequential march's steps, its state is where the next round starts.
+// Samples come out in the sequential order with the same values.
+struct MarchState {
+    float t0, t1, tm;
+};
+
+__device__ __forceinline__ MarchState march_advance(const MarchState &s, float cone, float step) {
+    MarchState r;
+    r.t0 = s.t1;
+    r.t1 = __fadd_rn(r.t0, calc_dt(r.t0, cone, step));
+    r.tm = __fmul_rn(__fadd_rn(r.t0, r.t1), 0.5f);
+    return r;
+}
+
+__device__ __forceinline__ MarchState march_skip(const Grid &g, const MarchState &s, const float o[3],
+                                                 const float d[3], const float inv[3], float cone, float step,
+                                                 int64_t max_steps) {
+    float xyz[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) xyz[k] = __fmaf_rn(s.tm, d[k], o[k]);
+    const float tgt = __fadd_rn(s.tm, dist_next_voxel(g, xyz, d, inv));
+    float tt = s.tm;
+    int64_t guard = 0;
+    do {
+        tt = __fadd_rn(tt, step);
+    } while (tt < tgt && ++guard < max_steps);
+    MarchState r;
+    r.tm = tt;
+    const float dt = calc_dt(tt, cone, step);
+    r.t0 = __fsub_rn(tt, __fmul_rn(dt, 0.5f));
+    r.t1 = __fadd_rn(tt, __fmul_rn(dt, 0.5f));
+    return r;
+}
+
+// Every lane of a group of G lanes (G a power of two up to 32, groups
+// aligned in the warp) calls this for the same ray; emit(j, t0, t1) is called
+// by the lane that owns sample j.  Returns the sample count (the same in
+// every lane of the group).
+template <int G, typename Emit>
+__device__ __forceinline__ int64_t march_ray_group(const Grid &g, const float o[3], const float d[3], float near,
+                                                   float far, float step, float cone, int64_t max_steps,
+                                                   int32_t *status, Emit emit) {
+    const int lane = threadIdx.x & (G - 1);
+    const int gbase = (threadIdx.x & 31) & ~(G - 1);   // the group's first lane in the warp
+    const uint32_t gmask = G == 32 ? 0xffffffffu : (((1u << G) - 1u) << gbase);
+    const uint32_t all = G == 32 ? 0xffffffffu : ((1u << G) - 1u);
+    const bool aabb = g.contraction == ANGELO_CONTRACT_AABB;
+    float inv[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) inv[k] = __fdiv_rn(1.0f, d[k]);
+    MarchState S;
+    S.t0 = near;
+    S.t1 = __fadd_rn(S.t0, calc_dt(S.t0, cone, step));
+    S.tm = __fmul_rn(__fadd_rn(S.t0, S.t1), 0.5f);
+    bool skipping = false;   // the kind of step the round assumes
+    int64_t j = 0, it = 0;
+    while (true) {
+        // this lane's state: `lane` steps of the assumed kind after S
+        MarchState st = S;
+        for (int k = 0; k < lane; ++k)
+            st = skipping ? march_skip(g, st, o, d, inv, cone, step, max_steps) : march_advance(st, cone, step);
+        const bool in_range = st.tm < far;
+        const bool in_steps = it + lane + 1 <= max_steps;
+        bool occ = false;
+        if (in_range && in_steps) {
+            float xyz[3];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) xyz[k] = __fmaf_rn(st.tm, d[k], o[k]);
+            occ = occupied(g, xyz);
+        }
+        // the step's kind: contracted grids always advance (no skipping)
+        const bool skip_here = aabb && !occ;
+        const bool same = in_range && in_steps && skip_here == skipping;
+        const uint32_t ok = (__ballot_sync(gmask, same) >> gbase) & all;
+        const int first = ok == all ? G : __ffs(~ok) - 1;   // the first step that ends the run
+        // the run's samples: lanes before `first` whose cell is occupied
+        const uint32_t emits = (__ballot_sync(gmask, lane < first && occ) >> gbase) & all;
+        if (lane < first && occ) emit(j + __popc(emits & ((1u << lane) - 1u)), st.t0, st.t1);
+        j += __popc(emits);
+        it += first;
+        if (first == G) {
+            // the whole run held: the next round starts one step after the
+            // group's last lane
+            MarchState nx = skipping ? march_skip(g, st, o, d, inv, cone, step, max_steps)
+                                     : march_advance(st, cone, step);
+            S.t0 = __shfl_sync(gmask, nx.t0, gbase + G - 1);
+            S.t1 = __shfl_sync(gmask, nx.t1, gbase + G - 1);
+            S.tm = __shfl_sync(gmask, nx.tm, gbase + G - 1);
+            continue;
+        }
+        // the run ends at lane `first`: past the far plane, out of steps, or
+        // a step of the other kind, which the next round starts with
+        const bool f_range = __shfl_sync(gmask, in_range, gbase + first);
+        const bool f_steps = __shfl_sync(gmask, in_steps, gbase + first);
+        if (!f_range) break;
+        if (!f_steps) {
+            if (status && lane == 0) atomicOr(status, 1);
+            break;
+        }
+        S.t0 = __shfl_sync(gmask, st.t0, gbase + first);
+        S.t1 = __shfl_sync(gmask, st.t1, gbase + first);
+        S.tm = __shfl_sync(gmask, st.tm, gbase + first);
+        skipping = !skipping;
+    }
+    return j;
+}
+
 __global__ void ray_aabb_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
                                 int64_t n, const float *__restrict__ aabb, float *__restrict__ tmin_out,
                                 float *__restrict__ tmax_out) {
@@ -172,61 +302,68 @@ __global__ void ray_aabb_kernel(const float *__restrict__ ro, const float *__res
     tmax_out[i] = fr;
 }
 
+template <int G>
 __global__ void march_count_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
                                    const float *__restrict__ tmin, const float *__restrict__ tmax,
                                    int64_t n, Grid g, float step, float cone, int64_t max_steps,
                                    int32_t *__restrict__ counts, int32_t *status) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
     if (i >= n) return;
     const float o[3] = {ro[i * 3], ro[i * 3 + 1], ro[i * 3 + 2]};
     const float d[3] = {rd[i * 3], rd[i * 3 + 1], rd[i * 3 + 2]};
-    const int64_t c = march_ray(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status,
-                                [](int64_t, float, float) {});
-    counts[i] = (int32_t)(c > 0x7fffffff ? 0x7fffffff : c);
+    auto none = [](int64_t, float, float) {};
+    const int64_t c = G > 1 ? march_ray_group<G>(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status, none)
+                            : march_ray(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status, none);
+    if ((threadIdx.x & (G - 1)) == 0) counts[i] = (int32_t)(c > 0x7fffffff ? 0x7fffffff : c);
 }
 
+template <int G>
 __global__ void march_fill_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
                                   const float *__restrict__ tmin, const float *__restrict__ tmax,
                                   int64_t n, Grid g, float step, float cone, int64_t max_steps,
                                   const int64_t *__restrict__ offsets, int64_t capacity,
                                   int32_t *__restrict__ ray_idx, float *__restrict__ ts,
                                   float *__restrict__ te, int32_t *status) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
     if (i >= n) return;
     const float o[3] = {ro[i * 3], ro[i * 3 + 1], ro[i * 3 + 2]};
     const float d[3] = {rd[i * 3], rd[i * 3 + 1], rd[i * 3 + 2]};
     const int64_t base = offsets[i];
     const int64_t limit = offsets[i + 1];
     bool dropped = false;
-    march_ray(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status,
-              [&](int64_t j, float t0, float t1) {
-                  const int64_t p = base + j;
-                  if (p < capacity && p < limit) {
-                      ray_idx[p] = (int32_t)i;
-                      ts[p] = t0;
-                      te[p] = t1;
-                  } else {
-                      dropped = true;
-                  }
-              });
+    auto emit = [&](int64_t j, float t0, float t1) {
+        const int64_t p = base + j;
+        if (p < capacity && p < limit) {
+            ray_idx[p] = (int32_t)i;
+            ts[p] = t0;
+            te[p] = t1;
+        } else {
+            dropped = true;
+        }
+    };
+    if (G > 1) march_ray_group<G>(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status, emit);
+    else march_ray(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status, emit);
     if (dropped && status) atomicOr(status, 2);
 }
 
 // One march per ray: the count and the first per_ray samples into scratch.
+template <int G>
 __global__ void march_record_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
                                     const float *__restrict__ tmin, const float *__restrict__ tmax,
                                     int64_t n, Grid g, float step, float cone, int64_t max_steps,
                                     int32_t per_ray, float2 *__restrict__ scratch,
                                     int32_t *__restrict__ counts, int32_t *status) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t i = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;
     if (i >= n) return;
     const float o[3] = {ro[i * 3], ro[i * 3 + 1], ro[i * 3 + 2]};
     const float d[3] = {rd[i * 3], rd[i * 3 + 1], rd[i * 3 + 2]};
     float2 *dst = scratch + i * per_ray;
-    const int64_t c = march_ray(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status,
-                                [&](int64_t j, float t0, float t1) {
-                                    if (j < per_ray) dst[j] = make_float2(t0, t1);
-                                });
+    auto emit = [&](int64_t j, float t0, float t1) {
+        if (j < per_ray) dst[j] = make_float2(t0, t1);
+    };
+    const int64_t c = G > 1 ? march_ray_group<G>(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status, emit)
+                            : march_ray(g, o, d, tmin[i], tmax[i], step, cone, max_steps, status, emit);
+    if ((threadIdx.x & (G - 1)) != 0) return;
     if (c > per_ray) atomicOr(status, 4);
     counts[i] = (int32_t)(c > 0x7fffffff ? 0x7fffffff : c);
 }
@@ -390,7 +527,12 @@ extern "C" int angelo_march_count(const float *rays_o, const float *rays_d, cons
     ANGELO_REQUIRE(n_rays >= 0 && step > 0.f && max_steps > 0, "march_count: bad arguments");
     if (n_rays == 0) return ANGELO_OK;
     ANGELO_REQUIRE(rays_o && rays_d && t_min && t_max && counts, "march_count: null pointer");
-    march_count_kernel<<<blocks_for(n_rays, 128), 128, 0, as_stream(stream)>>>(
+    const bool warp = g.contraction != ANGELO_CONTRACT_AABB;
+    if (warp)
+        march_count_kernel<32><<<blocks_for(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(
+        rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, counts, status);
+    else
+        march_count_kernel<kAabbLanes><<<blocks_for(n_rays * kAabbLanes, 128), 128, 0, as_stream(stream)>>>(
         rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, counts, status);
     return check_launch("march_count");
 }
@@ -430,7 +572,13 @@ extern "C" int angelo_march_fill(const float *rays_o, const float *rays_d, const
     if (n_rays == 0) return ANGELO_OK;
     ANGELO_REQUIRE(rays_o && rays_d && t_min && t_max && offsets, "march_fill: null pointer");
     ANGELO_REQUIRE(capacity == 0 || (ray_indices && t_starts && t_ends), "march_fill: null output");
-    march_fill_kernel<<<blocks_for(n_rays, 128), 128, 0, as_stream(stream)>>>(
+    const bool warp = g.contraction != ANGELO_CONTRACT_AABB;
+    if (warp)
+        march_fill_kernel<32><<<blocks_for(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(
+        rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, offsets, capacity,
+        ray_indices, t_starts, t_ends, status);
+    else
+        march_fill_kernel<kAabbLanes><<<blocks_for(n_rays * kAabbLanes, 128), 128, 0, as_stream(stream)>>>(
         rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, offsets, capacity,
         ray_indices, t_starts, t_ends, status);
     return check_launch("march_fill");
@@ -447,7 +595,13 @@ extern "C" int angelo_march_record(const float *rays_o, const float *rays_d, con
     ANGELO_REQUIRE(rays_o && rays_d && t_min && t_max && counts && scratch && status,
                    "march_record: null pointer");
     ANGELO_REQUIRE((reinterpret_cast<uintptr_t>(scratch) & 7) == 0, "march_record: scratch alignment");
-    march_record_kernel<<<blocks_for(n_rays, 128), 128, 0, as_stream(stream)>>>(
+    const bool warp = g.contraction != ANGELO_CONTRACT_AABB;
+    if (warp)
+        march_record_kernel<32><<<blocks_for(n_rays * 32, 128), 128, 0, as_stream(stream)>>>(
+        rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, per_ray,
+        reinterpret_cast<float2 *>(scratch), counts, status);
+    else
+        march_record_kernel<kAabbLanes><<<blocks_for(n_rays * kAabbLanes, 128), 128, 0, as_stream(stream)>>>(
         rays_o, rays_d, t_min, t_max, n_rays, g, step, cone_angle, max_steps, per_ray,
         reinterpret_cast<float2 *>(scratch), counts, status);
     return check_launch("march_record");
