@@ -353,9 +353,9 @@ def algorithmic_bytes(name, u):
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per processed
 # sample of a call, from one ncu capture of its kernels on a step of this
-# workload (the four kernels of one angelo_sdf_stencil_bwd call: 2.479 GB
-# for 284,088 samples); `traffic` scales it to the launch's samples.
-TRAFFIC_BYTES_PER_SAMPLE = {"angelo_sdf_stencil_bwd": 2.479e9 / 284088}
+# workload (the three kernels of one angelo_sdf_stencil_bwd call: 2.293 GB
+# for 283,862 samples); `traffic` scales it to the launch's samples.
+TRAFFIC_BYTES_PER_SAMPLE = {"angelo_sdf_stencil_bwd": 2.2934e9 / 283862}
 
 
 def mlp_flops(name, u):

@@ -18,18 +18,18 @@ namespace {
 
 // lanes per ray of the AABB grid's march (1: the sequential march itself)
 #ifndef ANGELO_MARCH_AABB_LANES
-#define ANGELO_MARCH_AABB_LANES 1
+#define ANGELO_MARCH_AABB_LANES 8
 #endif
 constexpr int kAabbLanes = ANGELO_MARCH_AABB_LANES;
 
 // The march kernels map a group of G lanes to a ray (G = 32: a warp) or one
-// thread to a ray (G = 1).
-// The launch picks the warp for the unbounded-sphere grid (the learned
-// background: no empty-space skipping, so every round of the warp's
-// lookahead is a full run of 32 steps) and one thread per ray for the AABB
-// grid, whose steps alternate between short runs of occupied steps and DDA
-// skips (measured: the warp form took the foreground's march from 0.25 to
-// 0.38 ms per step, the background's from ~0.19 to ~0.06).
+// thread to a ray (G = 1).  The launch picks the warp for the
+// unbounded-sphere grid (the learned background: no empty-space skipping, so
+// every round of the lookahead is a full run of 32 steps) and groups of 8 for
+// the AABB grid, whose steps alternate between short runs of occupied steps
+// and DDA skips: measured on the training step, the foreground's march took
+// 0.25 ms per step one thread per ray, 0.23 with 4 lanes, 0.21 with 8 and
+// 0.38 with 32; the background's went from ~0.19 to ~0.06 with 32.
 
 struct Grid {
     float lo[3], hi[3];
