@@ -35,3 +35,22 @@ def test_trainer_refuses_wmask_config():
     model = torch.nn.Module()
     with pytest.raises(NotImplementedError, match="lambda_mask"):
         system.NeuSTrainer(model, {"loss": WMASK_LOSS})
+
+
+def test_background_fused_routing():
+    """Which background modules run on the fused kernels (host logic, CPU):
+    the sparse configs' VolumeRadiance texture and ReLU density MLP do; a
+    texture with another input, activation or depth does not."""
+    from angelo_gb import models, neus, workloads
+    cfg = workloads.background(n_levels=8, log2_hashmap_size=12, base_resolution=16,
+                               per_level_scale=1.5, start_level=8, radius=1.0)
+    tex = models.make(cfg["texture_bg"]["name"], cfg["texture_bg"])
+    assert neus.fused_radiance_bg(tex)
+    for change in ({"color_activation": "none"},
+                   {"mlp_network_config": {**cfg["texture_bg"]["mlp_network_config"], "n_hidden_layers": 1}},
+                   {"input_feature_dim": 40}):
+        assert not neus.fused_radiance_bg(models.make("volume-radiance", {**cfg["texture_bg"], **change}))
+    geo_cfg = dict(cfg["geometry_bg"])
+    assert not models.make(geo_cfg["name"], geo_cfg).fused_reuse_ok()
+    geo = models.make(geo_cfg["name"], {**geo_cfg, "fused": True})
+    assert geo.encoding_with_network.network.fused and geo.fused_reuse_ok()
