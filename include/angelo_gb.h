@@ -555,7 +555,9 @@ int angelo_serve_create(const angelo_serve_field *field, int64_t rays_per_bucket
  * NeuSModel.forward in eval mode gives comp_rgb_full, opacity and depth.
  * A bucket whose samples overflow its capacity is rendered again at its
  * exact size; *overflows (may be NULL) counts them.  Returns after the
- * outputs are written (one stream synchronisation per call). */
+ * outputs are written (one stream synchronisation per call).  A server's
+ * bucket buffers serve one call at a time: calls on one server from several
+ * threads or streams race (create one server per stream). */
 int angelo_serve_render(angelo_server *srv, const float *rays_o, const float *rays_d, int64_t n,
                         float *rgb, float *opacity, float *depth, int64_t *overflows, void *stream);
 /* SDF at n device points (VolumeSDF.forward_level, the isosurface lattice of
