@@ -97,7 +97,8 @@ class _FusedSdf(torch.autograd.Function):
         # the forward's operands (fp16 in the fp16 precision form); the
         # backward always reads the bf16 buffer
         fnet = meta.get("net_fwd", net)
-        fnet.prepare(Ws)
+        if not meta.get("prepared"):
+            fnet.prepare(Ws)
         if training and fnet is not net:
             net.prepare(Ws)
         spec = geom.hashgrid.encoding.spec
@@ -242,6 +243,34 @@ def _net_for(geom, operand_format=_lib.OPERAND_BF16):
     return net
 
 
+def prepare_ahead(model):
+    """The training step's weight preparation, enqueued before the march
+    reads its sample count on the host: the geometry MLP's effective weights
+    (the native weight norm) and both networks' tensor-core operands.  The
+    next fused VolumeSDF and radiance calls take them as they are, so the
+    host has less to enqueue between that read and the forward's kernels.
+    Only the default form (fp32 table, bf16x3 operands) is prepared ahead."""
+    geom, tex = model.geometry, model.texture
+    if (_precision(geom) != "fp32" or getattr(geom, "fused_table_dtype", "fp32") != "fp32"
+            or geom.hashgrid.encoding.params.dtype != torch.float32):
+        return
+    net = _net_for(geom)
+    net.layout.mma_passes = 3
+    Ws = effective_weights(geom.network)
+    net.prepare(Ws)
+    geom._ahead = (Ws, net)
+    if (type(tex).__name__ in ("VolumeRadiance", "VolumeDualColor") and _precision(tex) == "fp32"
+            and tex.config.get("color_activation") == "sigmoid"):
+        rnet = getattr(tex, "_fused_net", None)
+        F_ = geom.n_output_dims + 3
+        if rnet is None or rnet.feat_dim != F_ or rnet.buf.device != geom.hashgrid.encoding.params.device:
+            rnet = RadNet(F_, geom.hashgrid.encoding.params.device)
+            tex._fused_net = rnet
+        RW = tex.network.effective_weights()
+        rnet.prepare(RW)
+        tex._ahead = (RW, rnet)
+
+
 def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
     """VolumeSDF.forward in one fused kernel (see the module docstring)."""
     if with_laplace and not with_grad:
@@ -252,8 +281,10 @@ def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
     if with_laplace:
         pts_c = (pos - (-geom.radius)) / (geom.radius - (-geom.radius))
         rd = geom.curvature_dirs_fn(pts_c).float().contiguous()
+    ahead = getattr(geom, "_ahead", None)
+    geom._ahead = None
     weights = []
-    for W, b in effective_weights(geom.network):
+    for W, b in (ahead[0] if ahead is not None and ahead[1] is net else effective_weights(geom.network)):
         weights += [W, b]
     table = geom.hashgrid.encoding.params
     prec = _precision(geom)
@@ -262,7 +293,8 @@ def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
         table_fwd = table.detach().half()
     net.layout.mma_passes = 1 if prec == "bf16" else 3
     meta = dict(geom=geom, net=net, flags=(bool(with_grad), bool(with_laplace),
-                                           bool(with_feature)))
+                                           bool(with_feature)),
+                prepared=ahead is not None and ahead[1] is net and prec == "fp32")
     if prec == "fp16":
         fnet = _net_for(geom, _lib.OPERAND_FP16)
         fnet.layout.mma_passes = 1
@@ -536,7 +568,8 @@ class _FusedRadiance(torch.autograd.Function):
         net, dual = meta["net"], meta["dual"]
         Ws = [(weights[2 * i], weights[2 * i + 1]) for i in range(3)]
         fnet = meta.get("net_fwd", net)
-        fnet.prepare(Ws)
+        if not meta.get("prepared"):
+            fnet.prepare(Ws)
         if fnet is not net and any(ctx.needs_input_grad):
             net.prepare(Ws)
         feature = feature.contiguous()
@@ -581,15 +614,19 @@ def radiance_forward(texture, feature, grad, ray_idx, rays_d):
     if net is None or net.feat_dim != F_ or net.buf.device != feature.device:
         net = RadNet(F_, feature.device)
         texture._fused_net = net
+    ahead = getattr(texture, "_ahead", None)
+    texture._ahead = None
+    use_ahead = ahead is not None and ahead[1] is net and grad is not None
     weights = []
-    for W, b in texture.network.effective_weights():
+    for W, b in (ahead[0] if use_ahead else texture.network.effective_weights()):
         weights += [W, b]
     if grad is None:
         if weights[0].shape[1] != F_ + 16:
             raise ValueError("a radiance network without a normal input takes [feature, SH4]")
         weights[0] = torch.nn.functional.pad(weights[0], (0, 3))
     prec = _precision(texture)
-    meta = dict(net=net, dual=bool(getattr(texture, "dual", False)), one_pass=prec in ("bf16", "fp16"))
+    meta = dict(net=net, dual=bool(getattr(texture, "dual", False)), one_pass=prec in ("bf16", "fp16"),
+                prepared=use_ahead and prec == "fp32")
     if prec == "fp16":
         fnet = getattr(texture, "_fused_net_fp16", None)
         if fnet is None or fnet.feat_dim != F_ or fnet.buf.device != feature.device:

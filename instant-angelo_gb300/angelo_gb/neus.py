@@ -319,6 +319,10 @@ class NeuSModel(nn.Module):
     def forward_(self, rays):
         n_rays = rays.shape[0]
         rays_o, rays_d = rays[:, 0:3].contiguous(), rays[:, 3:6].contiguous()
+        if self.fused and self.training:
+            # weight preparation ahead of the march's host read of its count
+            from . import fused
+            fused.prepare_ahead(self)
         ri, t0, t1, offsets = self.march_rays(rays_o, rays_d)
         if self.fused:
             from . import fused
