@@ -508,6 +508,28 @@ int angelo_density_composite_bwd(const int64_t *offsets, int64_t n_rays, const f
                                  const float *g_opacity, const float *g_depth, const float *g_rgb,
                                  float *d_sigmas, float *d_rgb, void *stream);
 
+/* The learned background's sample points and visibility test
+ * (models/neus.py:141-170), one launch each.  bg_points: the world point
+ * o + d (t_start + t_end)/2 of every sample, contracted to [0,1]^3 by the
+ * unbounded-sphere contraction of radius (models/geometry.py:22-28).
+ * bg_visibility: per ray the number of leading samples whose transmittance
+ * (sequential float32 product of 1 - alpha, alpha = 1 - exp(-exp(out0 +
+ * density_bias) dt), out0 = out[j * out_stride]) is at least early_stop_eps:
+ * nerfacc's visibility test keeps that prefix of each ray.  bg_compact:
+ * those samples (their ray index, t, point, out_dim outputs and their row in
+ * the inputs) at kept_offsets, the exclusive scan of kept. */
+int angelo_bg_points(const float *rays_o, const float *rays_d, const int32_t *ray_indices,
+                     const float *t_starts, const float *t_ends, int64_t n, float radius,
+                     float *points, void *stream);
+int angelo_bg_visibility(const float *out, int64_t out_stride, float density_bias,
+                         const float *t_starts, const float *t_ends, const int64_t *offsets,
+                         int64_t n_rays, float early_stop_eps, int32_t *kept, void *stream);
+int angelo_bg_compact(const int64_t *offsets, const int32_t *kept, const int64_t *kept_offsets,
+                      int64_t n_rays, const int32_t *ray_indices, const float *t_starts,
+                      const float *t_ends, const float *points, const float *out, int32_t out_dim,
+                      int32_t *ray_indices_k, float *t_starts_k, float *t_ends_k, float *points_k,
+                      float *out_k, int32_t *rows_k, void *stream);
+
 /* ------------------------------------------------------------------ serving */
 
 /* The resident field a server renders: device pointers owned by the caller

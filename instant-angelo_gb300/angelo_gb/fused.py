@@ -527,6 +527,42 @@ def density_composite(sigma, rgb, t0, t1, offsets, bg):
     return _DensityComposite.apply(sigma.reshape(-1), rgb, t0.reshape(-1), t1.reshape(-1), offsets, bg)
 
 
+def bg_points(rays_o, rays_d, ri, t0, t1, radius):
+    """The learned background's samples as contracted points (angelo_bg_points)."""
+    n = t0.numel()
+    pts = torch.empty(n, 3, device=t0.device)
+    call("angelo_bg_points", _p(rays_o), _p(rays_d), _p(ri), _p(t0), _p(t1), n, float(radius), _p(pts),
+         _s(t0.device), units=dict(n=n))
+    return pts
+
+
+def bg_visible(out, density_bias, ri, t0, t1, offsets, pts, eps=1e-4):
+    """nerfacc's visibility test on the background's samples from the density
+    MLP's output (density exp(out0 + bias)): the kept prefix of every ray,
+    compacted.  Returns (ray indices, t0, t1, points, outputs, their rows in
+    the inputs, offsets); one device read (the kept count)."""
+    n_rays = offsets.numel() - 1
+    dev = t0.device
+    kept = torch.empty(n_rays, dtype=torch.int32, device=dev)
+    call("angelo_bg_visibility", _p(out), out.stride(0), float(density_bias), _p(t0), _p(t1), _p(offsets),
+         n_rays, float(eps), _p(kept), _s(dev), units=dict(rays=n_rays))
+    koff = torch.empty(n_rays + 1, dtype=torch.int64, device=dev)
+    ws = torch.empty(_lib.raw("angelo_scan_workspace_size")(n_rays), dtype=torch.uint8, device=dev)
+    call("angelo_scan", _p(kept), n_rays, _p(koff), _p(ws), _s(dev))
+    total = int(koff[n_rays].item())
+    od = out.shape[1]
+    ri_k = torch.empty(total, dtype=torch.int32, device=dev)
+    t0_k = torch.empty(total, device=dev)
+    t1_k = torch.empty(total, device=dev)
+    pts_k = torch.empty(total, 3, device=dev)
+    out_k = torch.empty(total, od, device=dev)
+    rows = torch.empty(total, dtype=torch.int32, device=dev)
+    call("angelo_bg_compact", _p(offsets), _p(kept), _p(koff), n_rays, _p(ri), _p(t0), _p(t1), _p(pts),
+         _p(out.contiguous()), od, _p(ri_k), _p(t0_k), _p(t1_k), _p(pts_k), _p(out_k), _p(rows), _s(dev),
+         units=dict(rays=n_rays, n=total))
+    return ri_k, t0_k, t1_k, pts_k, out_k, rows, koff
+
+
 # ----------------------------------------------------------------- radiance
 
 

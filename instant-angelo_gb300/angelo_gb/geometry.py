@@ -147,6 +147,17 @@ class VolumeDensity(nn.Module):
         out = self.encoding_with_network.network(X).float()
         return pts, X, out
 
+    def native_visibility_ok(self):
+        """Whether the fused form's native visibility test applies: the reuse
+        of fused_reuse_ok and the trunc_exp density the kernel computes."""
+        return (self.fused_reuse_ok()
+                and str(self.config.get("density_activation", "")).lower() == "trunc_exp")
+
+    def evaluate_contracted(self, pts):
+        """(encodings X, MLP output) of contracted points."""
+        X = self.encoding_with_network.encoding(pts)
+        return X, self.encoding_with_network.network(X).float()
+
     def outputs(self, out):
         """(density, feature) from the MLP output, as forward() forms them."""
         feature = out

@@ -396,29 +396,43 @@ class NeuSModel(nn.Module):
                                                cone_angle=self.cone_angle_bg,
                                                max_steps=self.max_march_steps,
                                                max_samples_per_ray=self._bg_samples_bound(), **grid)
-            rl = ri.long()
-            pos = rays_o[rl] + rays_d[rl] * ((t0 + t1) * 0.5)[:, None]
             reuse = self.fused and self.geometry_bg.fused_reuse_ok()
-            if reuse:
-                # the fused form keeps the visibility pass's encodings and
-                # outputs for the kept samples instead of evaluating them again
-                pts_c, X_all, out_all = self.geometry_bg.encode_and_evaluate(pos)
-                sigma, _ = self.geometry_bg.outputs(out_all)
-            else:
-                sigma, _ = self.geometry_bg(pos)
-            alpha = 1.0 - torch.exp(-sigma * (t1 - t0))
-            keep = ops.transmittance_from_alpha(alpha, offsets) >= 1e-4
-            self._last_march_bg_full = (offsets, ri, t0, t1)
-            # the kept samples' indices once (one device read of their
-            # count), then one gather per tensor
-            kidx = keep.nonzero().squeeze(1)
-            ri, t0, t1 = ri.index_select(0, kidx), t0.index_select(0, kidx), t1.index_select(0, kidx)
-            if reuse:
-                # the encodings stay where they are: the backward reads the
-                # kept rows through kidx
-                pts_c, out_all = pts_c.index_select(0, kidx), out_all.index_select(0, kidx)
-            offsets = ops.offsets_from_ray_indices(ri, n_rays)
-            self._last_march_bg = (offsets, ri, t0, t1)
+            native = reuse and self.geometry_bg.native_visibility_ok()
+        if native:
+            # the fused form: points, visibility test and compaction in native
+            # launches (one device read, the kept count)
+            from . import fused
+            with torch.no_grad():
+                pts_c = fused.bg_points(rays_o, rays_d, ri, t0, t1, self.geometry_bg.radius)
+                X_all, out_all = self.geometry_bg.evaluate_contracted(pts_c)
+                self._last_march_bg_full = (offsets, ri, t0, t1)
+                ri, t0, t1, pts_c, out_all, kidx, offsets = fused.bg_visible(
+                    out_all, float(self.geometry_bg.config.density_bias), ri, t0, t1, offsets, pts_c)
+                self._last_march_bg = (offsets, ri, t0, t1)
+        else:
+            with torch.no_grad():
+                rl = ri.long()
+                pos = rays_o[rl] + rays_d[rl] * ((t0 + t1) * 0.5)[:, None]
+                if reuse:
+                    # the fused form keeps the visibility pass's encodings and
+                    # outputs for the kept samples instead of evaluating them again
+                    pts_c, X_all, out_all = self.geometry_bg.encode_and_evaluate(pos)
+                    sigma, _ = self.geometry_bg.outputs(out_all)
+                else:
+                    sigma, _ = self.geometry_bg(pos)
+                alpha = 1.0 - torch.exp(-sigma * (t1 - t0))
+                keep = ops.transmittance_from_alpha(alpha, offsets) >= 1e-4
+                self._last_march_bg_full = (offsets, ri, t0, t1)
+                # the kept samples' indices once (one device read of their
+                # count), then one gather per tensor
+                kidx = keep.nonzero().squeeze(1)
+                ri, t0, t1 = ri.index_select(0, kidx), t0.index_select(0, kidx), t1.index_select(0, kidx)
+                if reuse:
+                    # the encodings stay where they are: the backward reads the
+                    # kept rows through kidx
+                    pts_c, out_all = pts_c.index_select(0, kidx), out_all.index_select(0, kidx)
+                offsets = ops.offsets_from_ray_indices(ri, n_rays)
+                self._last_march_bg = (offsets, ri, t0, t1)
         ray_indices = ri.long()
         midpoints = ((t0 + t1) * 0.5)[:, None]
         intervals = (t1 - t0)[:, None]

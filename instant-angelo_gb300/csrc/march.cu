@@ -637,3 +637,130 @@ extern "C" int angelo_offsets_clamp(int64_t *offsets, int64_t n_rays, int64_t ca
     offsets_clamp_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(offsets, n, capacity);
     return check_launch("offsets_clamp");
 }
+
+// ------------------------------------------------ learned background samples
+// The background's sample points and its visibility test (models/neus.py:
+// 141-170 with nerfacc's sigma_fn), each one launch instead of a chain of
+// elementwise ops: the points in the order of the reference's torch ops, the
+// visibility with the sequential float32 transmittance of the foreground's
+// weights kernel, and the kept samples (a prefix of each ray) compacted by
+// their scanned counts.
+
+namespace {
+
+// world point o + d (t0 + t1) / 2 of sample j and its contraction to the
+// radius-2 ball in [0, 1]^3 (UN_BOUNDED_SPHERE, models/geometry.py:22-28):
+// [-r, r]^3 -> [-1, 1]^3, |x| > 1 -> (2 - 1/|x|) x/|x|, then x / 4 + 1/2
+__global__ void bg_points_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
+                                 const int32_t *__restrict__ ri, const float *__restrict__ t0,
+                                 const float *__restrict__ t1, int64_t n, float radius,
+                                 float *__restrict__ pts) {
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int64_t r = ri[j];
+    const float mid = __fmul_rn(__fadd_rn(t0[j], t1[j]), 0.5f);
+    const float two_r = __fsub_rn(radius, -radius);
+    float x[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float p = __fadd_rn(ro[r * 3 + k], __fmul_rn(rd[r * 3 + k], mid));
+        x[k] = __fsub_rn(__fmul_rn(__fdiv_rn(__fsub_rn(p, -radius), two_r), 2.0f), 1.0f);
+    }
+    const float mag = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x[0], x[0]), __fmul_rn(x[1], x[1])),
+                                           __fmul_rn(x[2], x[2])));
+    if (mag > 1.0f) {
+        const float sc = __fsub_rn(2.0f, __fdiv_rn(1.0f, mag));
+#pragma unroll
+        for (int k = 0; k < 3; ++k) x[k] = __fmul_rn(sc, __fdiv_rn(x[k], mag));
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) pts[j * 3 + k] = __fadd_rn(__fdiv_rn(x[k], 4.0f), 0.5f);
+}
+
+// per ray: density exp(out0 + bias) (trunc_exp), alpha = 1 - exp(-density dt),
+// transmittance T by the sequential product (held once below eps); the count
+// of samples with T >= eps (a prefix of the ray)
+__global__ void bg_visibility_kernel(const float *__restrict__ out, int64_t out_stride, float bias,
+                                     const float *__restrict__ t0, const float *__restrict__ t1,
+                                     const int64_t *__restrict__ off, int64_t n_rays, float eps,
+                                     int32_t *__restrict__ kept) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rays) return;
+    float T = 1.0f;
+    int32_t k = 0;
+    for (int64_t j = off[r]; j < off[r + 1]; ++j) {
+        if (T < eps) break;
+        ++k;
+        const float sigma = expf(__fadd_rn(out[j * out_stride], bias));
+        const float a = __fsub_rn(1.0f, expf(-__fmul_rn(sigma, __fsub_rn(t1[j], t0[j]))));
+        T = __fmul_rn(T, __fsub_rn(1.0f, a));
+    }
+    kept[r] = k;
+}
+
+// the kept samples (the first kept[r] of ray r) at their scanned offsets:
+// ray index, t0, t1, contracted point, the MLP output row and the row index
+// into the visibility pass's arrays
+__global__ void bg_compact_kernel(const int64_t *__restrict__ off, const int32_t *__restrict__ kept,
+                                  const int64_t *__restrict__ koff, int64_t n_rays,
+                                  const int32_t *__restrict__ ri, const float *__restrict__ t0,
+                                  const float *__restrict__ t1, const float *__restrict__ pts,
+                                  const float *__restrict__ out, int32_t out_dim,
+                                  int32_t *__restrict__ ri_k, float *__restrict__ t0_k,
+                                  float *__restrict__ t1_k, float *__restrict__ pts_k,
+                                  float *__restrict__ out_k, int32_t *__restrict__ rows_k) {
+    const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (r >= n_rays) return;
+    const int64_t src = off[r], dst = koff[r];
+    for (int i = lane; i < kept[r]; i += 32) {
+        const int64_t a = src + i, b = dst + i;
+        ri_k[b] = ri[a];
+        t0_k[b] = t0[a];
+        t1_k[b] = t1[a];
+        rows_k[b] = (int32_t)a;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) pts_k[b * 3 + k] = pts[a * 3 + k];
+        for (int c = 0; c < out_dim; ++c) out_k[b * out_dim + c] = out[a * out_dim + c];
+    }
+}
+
+}  // namespace
+
+extern "C" int angelo_bg_points(const float *rays_o, const float *rays_d, const int32_t *ray_indices,
+                                const float *t_starts, const float *t_ends, int64_t n, float radius,
+                                float *points, void *stream) {
+    ANGELO_REQUIRE(n >= 0 && radius > 0.f, "bg_points: bad arguments");
+    if (n == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(rays_o && rays_d && ray_indices && t_starts && t_ends && points, "bg_points: null pointer");
+    bg_points_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(rays_o, rays_d, ray_indices, t_starts,
+                                                                         t_ends, n, radius, points);
+    return check_launch("bg_points");
+}
+
+extern "C" int angelo_bg_visibility(const float *out, int64_t out_stride, float density_bias,
+                                    const float *t_starts, const float *t_ends, const int64_t *offsets,
+                                    int64_t n_rays, float early_stop_eps, int32_t *kept, void *stream) {
+    ANGELO_REQUIRE(n_rays >= 0 && out_stride >= 1, "bg_visibility: bad arguments");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(out && t_starts && t_ends && offsets && kept, "bg_visibility: null pointer");
+    bg_visibility_kernel<<<blocks_for(n_rays, 128), 128, 0, as_stream(stream)>>>(
+        out, out_stride, density_bias, t_starts, t_ends, offsets, n_rays, early_stop_eps, kept);
+    return check_launch("bg_visibility");
+}
+
+extern "C" int angelo_bg_compact(const int64_t *offsets, const int32_t *kept, const int64_t *kept_offsets,
+                                 int64_t n_rays, const int32_t *ray_indices, const float *t_starts,
+                                 const float *t_ends, const float *points, const float *out, int32_t out_dim,
+                                 int32_t *ray_indices_k, float *t_starts_k, float *t_ends_k, float *points_k,
+                                 float *out_k, int32_t *rows_k, void *stream) {
+    ANGELO_REQUIRE(n_rays >= 0 && out_dim >= 1, "bg_compact: bad arguments");
+    if (n_rays == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(offsets && kept && kept_offsets && ray_indices && t_starts && t_ends && points && out,
+                   "bg_compact: null input");
+    ANGELO_REQUIRE(n_rays < (1ll << 26), "bg_compact: too many rays");
+    bg_compact_kernel<<<blocks_for(n_rays * 32, 256), 256, 0, as_stream(stream)>>>(
+        offsets, kept, kept_offsets, n_rays, ray_indices, t_starts, t_ends, points, out, out_dim, ray_indices_k,
+        t_starts_k, t_ends_k, points_k, out_k, rows_k);
+    return check_launch("bg_compact");
+}

@@ -97,6 +97,62 @@ def test_density_weights_match_fp64(dev):
     np.testing.assert_allclose(s.grad.cpu().numpy(), s64.grad.numpy(), rtol=1e-4, atol=1e-5)
 
 
+def test_native_visibility_matches_reference_ops(dev):
+    """The fused form's native background sampling (angelo_bg_points,
+    angelo_bg_visibility, angelo_bg_compact) against the reference's chain of
+    ops on the same samples: midpoints contracted by UN_BOUNDED_SPHERE, the
+    trunc_exp density's alpha, nerfacc's visibility test (T >= 1e-4) and the
+    kept samples gathered in order."""
+    from angelo_gb import fused, ops
+    from angelo_gb.geometry import contract_unbounded_sphere
+    g = np.random.default_rng(43)
+    n_rays, radius, bias = 500, 0.5, -1.0
+    counts = g.integers(0, 90, n_rays)
+    counts[:7] = 0
+    off = np.zeros(n_rays + 1, np.int64)
+    np.cumsum(counts, out=off[1:])
+    n = int(off[-1])
+    dt = g.uniform(0.001, 0.4, n).astype(np.float32)
+    t0 = np.zeros(n, np.float32)
+    for r in range(n_rays):
+        seg = slice(off[r], off[r + 1])
+        t0[seg] = np.cumsum(np.concatenate([[0.6], dt[seg][:-1]])).astype(np.float32)
+    t1 = (t0 + dt).astype(np.float32)
+    ri = np.repeat(np.arange(n_rays, dtype=np.int32), counts)
+    o, d = _rays(n_rays, 44, radius)
+    out = g.normal(0.5, 1.5, (n, 8)).astype(np.float32)
+    tt = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    o_t, d_t, ri_t, t0_t, t1_t, off_t, out_t = map(tt, (o, d, ri, t0, t1, off, out))
+
+    pts = fused.bg_points(o_t, d_t, ri_t, t0_t, t1_t, radius)
+    rl = ri_t.long()
+    pos = o_t[rl] + d_t[rl] * ((t0_t + t1_t) * 0.5)[:, None]
+    ref_pts = contract_unbounded_sphere(pos, radius)
+    # the kernel's norm is the plain sum of squares; torch's reduction may
+    # round it differently by an ulp or two
+    torch.testing.assert_close(pts, ref_pts, rtol=0, atol=1e-6)
+
+    ri_k, t0_k, t1_k, pts_k, out_k, rows, koff = fused.bg_visible(out_t, bias, ri_t, t0_t, t1_t, off_t, pts)
+    sigma = torch.exp(out_t[:, 0] + bias)
+    alpha = 1.0 - torch.exp(-sigma * (t1_t - t0_t))
+    keep = ops.transmittance_from_alpha(alpha, off_t) >= 1e-4
+    kidx = keep.nonzero().squeeze(1)
+    assert torch.equal(rows.long(), kidx)
+    assert torch.equal(koff, ops.offsets_from_ray_indices(ri_t[kidx], n_rays))
+    assert torch.equal(ri_k, ri_t[kidx]) and torch.equal(t0_k, t0_t[kidx]) and torch.equal(t1_k, t1_t[kidx])
+    assert torch.equal(pts_k, pts[kidx]) and torch.equal(out_k, out_t[kidx])
+    # every ray keeps a prefix; a good share of the samples is dropped
+    assert 0.2 * n < kidx.numel() < 0.9 * n
+    # the float64 transmittance agrees except within rounding of the threshold
+    a64 = 1.0 - np.exp(-np.exp(out[:, 0].astype(np.float64) + bias) * (t1 - t0).astype(np.float64))
+    T64 = np.ones(n)
+    for r in range(n_rays):
+        seg = slice(off[r], off[r + 1])
+        T64[seg] = np.concatenate([[1.0], np.cumprod(1.0 - a64[seg])[:-1]])
+    differ = (T64 >= 1e-4) != keep.cpu().numpy()
+    assert np.all(np.abs(T64[differ] / 1e-4 - 1.0) < 1e-4)
+
+
 def test_fused_density_composite_matches_fp64(dev):
     """The fused background compositing (weights from density, opacity,
     depth, colour and the background blend in one kernel each way) against
