@@ -48,37 +48,58 @@ extern "C" int angelo_hashgrid_layout(const angelo_hashgrid_desc *desc,
 
 namespace {
 
-__global__ void __launch_bounds__(256) hashgrid_fwd_kernel(
+// One thread per point over every level: the point's output row (x*2-1, then
+// two features per level) is assembled in shared memory and written out a row
+// per warp instruction, so that every sector of the output is written whole
+// once.  (A launch dimension per level wrote 8 bytes into every row per level;
+// with outputs larger than L2 those sectors were evicted partly written and
+// read back from HBM once per level.)
+constexpr int kFwdRows = 128;
+
+__global__ void __launch_bounds__(kFwdRows) hashgrid_fwd_kernel(
     const __grid_constant__ angelo_hashgrid_layout_t lay, int active, const float *__restrict__ x,
     int64_t n, const void *__restrict__ table, int dtype, int include_xyz, float *__restrict__ out,
     int64_t out_stride, int64_t out_col) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const int l = blockIdx.y;
-    if (i >= n) return;
-    const float x0 = x[i * 3 + 0], x1 = x[i * 3 + 1], x2 = x[i * 3 + 2];
-    float *o = out + i * out_stride + out_col;
-    if (include_xyz) {
-        if (l == 0) {
-            o[0] = __fsub_rn(__fmul_rn(x0, 2.0f), 1.0f);
-            o[1] = __fsub_rn(__fmul_rn(x1, 2.0f), 1.0f);
-            o[2] = __fsub_rn(__fmul_rn(x2, 2.0f), 1.0f);
+    extern __shared__ float rows[];
+    const int width = (include_xyz ? 3 : 0) + 2 * lay.n_levels;
+    const int pitch = width | 1;   // odd: one row per thread without bank conflicts
+    const int64_t i0 = (int64_t)blockIdx.x * kFwdRows;
+    const int t = threadIdx.x;
+    const int64_t i = i0 + t;
+    if (i < n) {
+        const float x0 = x[i * 3 + 0], x1 = x[i * 3 + 1], x2 = x[i * 3 + 2];
+        float *r = rows + t * pitch;
+        if (include_xyz) {
+            r[0] = __fsub_rn(__fmul_rn(x0, 2.0f), 1.0f);
+            r[1] = __fsub_rn(__fmul_rn(x1, 2.0f), 1.0f);
+            r[2] = __fsub_rn(__fmul_rn(x2, 2.0f), 1.0f);
+            r += 3;
         }
-        o += 3;
-    }
-    float r0 = 0.0f, r1 = 0.0f;
-    if (l < active) {
-        const LevelPos p = level_pos(x0, x1, x2, lay.scales[l]);
-        const uint64_t base = lay.offsets[l];
+        for (int l = 0; l < lay.n_levels; ++l) {
+            float r0 = 0.0f, r1 = 0.0f;
+            if (l < active) {
+                const LevelPos p = level_pos(x0, x1, x2, lay.scales[l]);
+                const uint64_t base = lay.offsets[l];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-            const float w = corner_weight(p, c);
-            const float2 v = load_entry(table, dtype, base + corner_index(lay, l, p, c));
-            r0 = __fmaf_rn(w, v.x, r0);
-            r1 = __fmaf_rn(w, v.y, r1);
+                for (int c = 0; c < 8; ++c) {
+                    const float w = corner_weight(p, c);
+                    const float2 v = load_entry(table, dtype, base + corner_index(lay, l, p, c));
+                    r0 = __fmaf_rn(w, v.x, r0);
+                    r1 = __fmaf_rn(w, v.y, r1);
+                }
+            }
+            r[2 * l] = r0;
+            r[2 * l + 1] = r1;
         }
     }
-    o[l * 2 + 0] = r0;
-    o[l * 2 + 1] = r1;
+    __syncthreads();
+    const int warp = t >> 5, lane = t & 31;
+    const int64_t nr = n - i0 < kFwdRows ? n - i0 : kFwdRows;
+    for (int64_t q = warp; q < nr; q += kFwdRows / 32) {
+        float *o = out + (i0 + q) * out_stride + out_col;
+        const float *r = rows + q * pitch;
+        for (int c = lane; c < width; c += 32) o[c] = r[c];
+    }
 }
 
 __global__ void __launch_bounds__(256) hashgrid_bwd_table_kernel(
@@ -203,10 +224,10 @@ extern "C" int angelo_hashgrid_fwd(const angelo_hashgrid_layout_t *lay, int32_t 
                    "hashgrid_fwd: bad table dtype");
     ANGELO_REQUIRE(out_stride >= out_col + lay->n_levels * 2 + (include_xyz ? 3 : 0),
                    "hashgrid_fwd: out_stride too small");
-    dim3 grid(blocks_for(n, 256), lay->n_levels);
-    hashgrid_fwd_kernel<<<grid, 256, 0, as_stream(stream)>>>(*lay, active_levels, x, n, table,
-                                                             table_dtype, include_xyz, out,
-                                                             out_stride, out_col);
+    const int width = (include_xyz ? 3 : 0) + 2 * lay->n_levels;
+    const size_t smem = (size_t)kFwdRows * (width | 1) * sizeof(float);
+    hashgrid_fwd_kernel<<<blocks_for(n, kFwdRows), kFwdRows, smem, as_stream(stream)>>>(
+        *lay, active_levels, x, n, table, table_dtype, include_xyz, out, out_stride, out_col);
     return check_launch("hashgrid_fwd");
 }
 
