@@ -508,6 +508,14 @@ int angelo_density_composite_bwd(const int64_t *offsets, int64_t n_rays, const f
                                  const float *g_opacity, const float *g_depth, const float *g_rgb,
                                  float *d_sigmas, float *d_rgb, void *stream);
 
+/* The samples' world points (models/neus.py:222-226): midpoint
+ * m = (t_start + t_end) * 0.5 and point o + d * m of ray ray_indices[j], in
+ * that order of float32 operations (bit-identical to the reference's torch
+ * expression); midpoints (n floats) is optional. */
+int angelo_sample_points(const float *rays_o, const float *rays_d, const int32_t *ray_indices,
+                         const float *t_starts, const float *t_ends, int64_t n, float *points,
+                         float *midpoints, void *stream);
+
 /* The learned background's sample points and visibility test
  * (models/neus.py:141-170), one launch each.  bg_points: the world point
  * o + d (t_start + t_end)/2 of every sample, contracted to [0,1]^3 by the

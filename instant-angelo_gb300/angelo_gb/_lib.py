@@ -149,6 +149,7 @@ SIGNATURES = {
                                              c_vp, c_vp, c_vp, c_vp]),
     "angelo_density_composite_bwd": (c_i32, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp,
                                              c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "angelo_sample_points": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "angelo_bg_points": (c_i32, [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_f32, c_vp, c_vp]),
     "angelo_bg_visibility": (c_i32, [c_vp, c_i64, c_f32, c_vp, c_vp, c_vp, c_i64, c_f32, c_vp, c_vp]),
     "angelo_bg_compact": (c_i32, [c_vp, c_vp, c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_i32, c_vp, c_vp,

@@ -279,8 +279,13 @@ def volume_sdf_forward(geom, points, with_grad, with_feature, with_laplace):
     pos = points.reshape(-1, 3).float().contiguous()
     rd = None
     if with_laplace:
-        pts_c = (pos - (-geom.radius)) / (geom.radius - (-geom.radius))
-        rd = geom.curvature_dirs_fn(pts_c).float().contiguous()
+        if geom.curvature_dirs_fn is torch.randn_like:
+            # the same draws as randn_like of the contracted points (shape,
+            # dtype and device are all it reads)
+            rd = torch.randn_like(pos)
+        else:
+            pts_c = (pos - (-geom.radius)) / (geom.radius - (-geom.radius))
+            rd = geom.curvature_dirs_fn(pts_c).float().contiguous()
     ahead = getattr(geom, "_ahead", None)
     geom._ahead = None
     weights = []
@@ -527,6 +532,18 @@ def density_composite(sigma, rgb, t0, t1, offsets, bg):
     return _DensityComposite.apply(sigma.reshape(-1), rgb, t0.reshape(-1), t1.reshape(-1), offsets, bg)
 
 
+def sample_points(rays_o, rays_d, ri, t0, t1):
+    """(world points (S, 3), midpoints (S,)) of the marched samples in one
+    launch (angelo_sample_points), bit-identical to
+    rays_o[ri] + rays_d[ri] * ((t0 + t1) * 0.5)[:, None]."""
+    n = t0.numel()
+    pts = torch.empty(n, 3, device=t0.device)
+    mid = torch.empty(n, device=t0.device)
+    call("angelo_sample_points", _p(rays_o), _p(rays_d), _p(ri), _p(t0), _p(t1), n, _p(pts), _p(mid),
+         _s(t0.device), units=dict(n=n))
+    return pts, mid
+
+
 def bg_points(rays_o, rays_d, ri, t0, t1, radius):
     """The learned background's samples as contracted points (angelo_bg_points)."""
     n = t0.numel()
@@ -737,11 +754,10 @@ def neus_forward(model, rays_o, rays_d, ri, t0, t1, offsets, n_rays):
     """NeuSModel.forward_ (models/neus.py:205-283) on the fused kernels:
     fused VolumeSDF -> fused radiance (VolumeRadiance / VolumeDualColor) ->
     fused compositing; VolumeDualColorV3 runs its own module between them."""
-    ray_indices = ri.long()
-    mid = (t0 + t1) * 0.5
-    positions = rays_o[ray_indices] + rays_d[ray_indices] * mid[:, None]
+    positions, mid = sample_points(rays_o, rays_d, ri, t0, t1)
     sdf, sdf_grad, feature, sdf_laplace = model.geometry(positions, with_grad=True,
                                                          with_feature=True, with_laplace=True)
+    ray_indices = ri.long()
     tex = model.texture
     if not FUSED_RENDER:
         return _plain_render(model, rays_o, rays_d, ray_indices, t0, t1, offsets, sdf, sdf_grad,

@@ -243,8 +243,8 @@ def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), 
     call("angelo_scan", _p(counts), n, _p(offsets), _p(ws), s, launches=3 if n else 0)
     if single:
         # the total and the record-overflow bit in one device read
-        head = torch.cat([offsets[n:], status.to(torch.int64)]).cpu()
-        total, overflow = int(head[0]), bool(int(head[1]) & 4)
+        total, flags = torch.cat([offsets[n:], status.to(torch.int64)]).tolist()
+        overflow = bool(flags & 4)
     else:
         total, overflow = int(offsets[n].item()), False
     ri = torch.empty(total, device=dev, dtype=torch.int32)

@@ -648,33 +648,40 @@ extern "C" int angelo_offsets_clamp(int64_t *offsets, int64_t n_rays, int64_t ca
 
 namespace {
 
-// world point o + d (t0 + t1) / 2 of sample j and its contraction to the
+// world point o + d (t0 + t1) / 2 of sample j (the reference's
+// positions = t_origins + t_dirs * midpoints, models/neus.py:222-226, in its
+// order of float32 operations); with a radius, its contraction to the
 // radius-2 ball in [0, 1]^3 (UN_BOUNDED_SPHERE, models/geometry.py:22-28):
-// [-r, r]^3 -> [-1, 1]^3, |x| > 1 -> (2 - 1/|x|) x/|x|, then x / 4 + 1/2
-__global__ void bg_points_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
-                                 const int32_t *__restrict__ ri, const float *__restrict__ t0,
-                                 const float *__restrict__ t1, int64_t n, float radius,
-                                 float *__restrict__ pts) {
+// [-r, r]^3 -> [-1, 1]^3, |x| > 1 -> (2 - 1/|x|) x/|x|, then x / 4 + 1/2;
+// the midpoint too where mids is given
+__global__ void sample_points_kernel(const float *__restrict__ ro, const float *__restrict__ rd,
+                                     const int32_t *__restrict__ ri, const float *__restrict__ t0,
+                                     const float *__restrict__ t1, int64_t n, float radius,
+                                     float *__restrict__ pts, float *__restrict__ mids) {
     const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const int64_t r = ri[j];
     const float mid = __fmul_rn(__fadd_rn(t0[j], t1[j]), 0.5f);
-    const float two_r = __fsub_rn(radius, -radius);
+    if (mids) mids[j] = mid;
     float x[3];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const float p = __fadd_rn(ro[r * 3 + k], __fmul_rn(rd[r * 3 + k], mid));
-        x[k] = __fsub_rn(__fmul_rn(__fdiv_rn(__fsub_rn(p, -radius), two_r), 2.0f), 1.0f);
-    }
-    const float mag = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x[0], x[0]), __fmul_rn(x[1], x[1])),
-                                           __fmul_rn(x[2], x[2])));
-    if (mag > 1.0f) {
-        const float sc = __fsub_rn(2.0f, __fdiv_rn(1.0f, mag));
+    for (int k = 0; k < 3; ++k) x[k] = __fadd_rn(ro[r * 3 + k], __fmul_rn(rd[r * 3 + k], mid));
+    if (radius > 0.f) {
+        const float two_r = __fsub_rn(radius, -radius);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) x[k] = __fmul_rn(sc, __fdiv_rn(x[k], mag));
+        for (int k = 0; k < 3; ++k) x[k] = __fsub_rn(__fmul_rn(__fdiv_rn(__fsub_rn(x[k], -radius), two_r), 2.0f), 1.0f);
+        const float mag = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x[0], x[0]), __fmul_rn(x[1], x[1])),
+                                               __fmul_rn(x[2], x[2])));
+        if (mag > 1.0f) {
+            const float sc = __fsub_rn(2.0f, __fdiv_rn(1.0f, mag));
+#pragma unroll
+            for (int k = 0; k < 3; ++k) x[k] = __fmul_rn(sc, __fdiv_rn(x[k], mag));
+        }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) x[k] = __fadd_rn(__fdiv_rn(x[k], 4.0f), 0.5f);
     }
 #pragma unroll
-    for (int k = 0; k < 3; ++k) pts[j * 3 + k] = __fadd_rn(__fdiv_rn(x[k], 4.0f), 0.5f);
+    for (int k = 0; k < 3; ++k) pts[j * 3 + k] = x[k];
 }
 
 // per ray: density exp(out0 + bias) (trunc_exp), alpha = 1 - exp(-density dt),
@@ -733,9 +740,20 @@ extern "C" int angelo_bg_points(const float *rays_o, const float *rays_d, const 
     ANGELO_REQUIRE(n >= 0 && radius > 0.f, "bg_points: bad arguments");
     if (n == 0) return ANGELO_OK;
     ANGELO_REQUIRE(rays_o && rays_d && ray_indices && t_starts && t_ends && points, "bg_points: null pointer");
-    bg_points_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(rays_o, rays_d, ray_indices, t_starts,
-                                                                         t_ends, n, radius, points);
+    sample_points_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(
+        rays_o, rays_d, ray_indices, t_starts, t_ends, n, radius, points, nullptr);
     return check_launch("bg_points");
+}
+
+extern "C" int angelo_sample_points(const float *rays_o, const float *rays_d, const int32_t *ray_indices,
+                                    const float *t_starts, const float *t_ends, int64_t n, float *points,
+                                    float *midpoints, void *stream) {
+    ANGELO_REQUIRE(n >= 0, "sample_points: bad arguments");
+    if (n == 0) return ANGELO_OK;
+    ANGELO_REQUIRE(rays_o && rays_d && ray_indices && t_starts && t_ends && points, "sample_points: null pointer");
+    sample_points_kernel<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(
+        rays_o, rays_d, ray_indices, t_starts, t_ends, n, 0.f, points, midpoints);
+    return check_launch("sample_points");
 }
 
 extern "C" int angelo_bg_visibility(const float *out, int64_t out_stride, float density_bias,

@@ -97,12 +97,12 @@ def test_density_weights_match_fp64(dev):
     np.testing.assert_allclose(s.grad.cpu().numpy(), s64.grad.numpy(), rtol=1e-4, atol=1e-5)
 
 
-def test_native_visibility_matches_reference_ops(dev):
-    """The fused form's native background sampling (angelo_bg_points,
+def test_native_sampling_matches_reference_ops(dev):
+    """The fused form's native sampling (angelo_sample_points, angelo_bg_points,
     angelo_bg_visibility, angelo_bg_compact) against the reference's chain of
-    ops on the same samples: midpoints contracted by UN_BOUNDED_SPHERE, the
-    trunc_exp density's alpha, nerfacc's visibility test (T >= 1e-4) and the
-    kept samples gathered in order."""
+    ops on the same samples: world points and midpoints, the points contracted
+    by UN_BOUNDED_SPHERE, the trunc_exp density's alpha, nerfacc's visibility
+    test (T >= 1e-4) and the kept samples gathered in order."""
     from angelo_gb import fused, ops
     from angelo_gb.geometry import contract_unbounded_sphere
     g = np.random.default_rng(43)
@@ -131,6 +131,11 @@ def test_native_visibility_matches_reference_ops(dev):
     # the kernel's norm is the plain sum of squares; torch's reduction may
     # round it differently by an ulp or two
     torch.testing.assert_close(pts, ref_pts, rtol=0, atol=1e-6)
+
+    # the foreground's world points and midpoints (angelo_sample_points): the
+    # reference's expression bit for bit
+    wpts, mid = fused.sample_points(o_t, d_t, ri_t, t0_t, t1_t)
+    assert torch.equal(mid, (t0_t + t1_t) * 0.5) and torch.equal(wpts, pos)
 
     ri_k, t0_k, t1_k, pts_k, out_k, rows, koff = fused.bg_visible(out_t, bias, ri_t, t0_t, t1_t, off_t, pts)
     sigma = torch.exp(out_t[:, 0] + bias)
