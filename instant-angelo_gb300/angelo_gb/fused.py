@@ -644,7 +644,8 @@ class _FusedRadiance(torch.autograd.Function):
         net, dual = ctx.meta["net"], ctx.meta["dual"]
         S = feature.shape[0]
         g_rgb = g_rgb.contiguous().float()
-        d_feature = torch.zeros_like(feature)
+        # the kernel writes every column of every row
+        d_feature = torch.empty_like(feature)
         d_grad = torch.empty_like(grad) if grad is not None else None
         d_net = torch.zeros(net.grad_size, device=feature.device)
         call("angelo_radiance_bwd", net.feat_dim, _p(net.buf), _p(feature), feature.stride(0),
