@@ -176,6 +176,8 @@ def load(path: str = None):
     library next to this package, or the file $ANGELO_GB_LIB names (a build
     of the same sources with other compile-time settings)."""
     global _lib
+    if _lib is not None and path is None:
+        return _lib
     path = path or os.environ.get("ANGELO_GB_LIB") or LIB_PATH
     with _lock:
         if _lib is None:

@@ -751,7 +751,7 @@ class _FusedComposite(torch.autograd.Function):
                 None)
 
 
-def neus_forward(model, rays_o, rays_d, ri, t0, t1, offsets, n_rays):
+def neus_forward(model, rays_o, rays_d, ri, t0, t1, offsets, n_rays, bg_samples=None):
     """NeuSModel.forward_ (models/neus.py:205-283) on the fused kernels:
     fused VolumeSDF -> fused radiance (VolumeRadiance / VolumeDualColor) ->
     fused compositing; VolumeDualColorV3 runs its own module between them."""
@@ -762,7 +762,7 @@ def neus_forward(model, rays_o, rays_d, ri, t0, t1, offsets, n_rays):
     tex = model.texture
     if not FUSED_RENDER:
         return _plain_render(model, rays_o, rays_d, ray_indices, t0, t1, offsets, sdf, sdf_grad,
-                             feature, sdf_laplace)
+                             feature, sdf_laplace, bg_samples)
     if type(tex).__name__ in ("VolumeRadiance", "VolumeDualColor") and \
             tex.config.get("color_activation") == "sigmoid":
         rgb = radiance_forward(tex, feature, sdf_grad, ri, rays_d)
@@ -785,7 +785,7 @@ def neus_forward(model, rays_o, rays_d, ri, t0, t1, offsets, n_rays):
         out.update({"sdf_samples": sdf, "sdf_grad_samples": sdf_grad, "weights": weights,
                     "points": mid, "intervals": t1 - t0, "ray_indices": ray_indices,
                     "sdf_laplace_samples": sdf_laplace})
-    out_bg = model.background(out, comp_rgb, rays_o, rays_d)
+    out_bg = model.background(out, comp_rgb, rays_o, rays_d, bg_samples)
     if model.learned_background:
         comp_full = comp_rgb + out_bg["comp_rgb"] * (1.0 - opacity)
     out_full = {"comp_rgb": comp_full,
@@ -796,7 +796,7 @@ def neus_forward(model, rays_o, rays_d, ri, t0, t1, offsets, n_rays):
 
 
 def _plain_render(model, rays_o, rays_d, ray_indices, t0, t1, offsets, sdf, sdf_grad, feature,
-                  sdf_laplace):
+                  sdf_laplace, bg_samples=None):
     """The reference's texture / alpha / compositing steps on the library's
     plain kernels, after the fused geometry."""
     from . import ops
@@ -822,4 +822,4 @@ def _plain_render(model, rays_o, rays_d, ray_indices, t0, t1, offsets, sdf, sdf_
                     "weights": weights.view(-1), "points": mid.view(-1),
                     "intervals": dists.view(-1), "ray_indices": ray_indices.view(-1),
                     "sdf_laplace_samples": sdf_laplace})
-    return model._with_background(out, comp_rgb, rays_o, rays_d)
+    return model._with_background(out, comp_rgb, rays_o, rays_d, bg_samples)

@@ -292,6 +292,7 @@ class NeuSModel(nn.Module):
 
     def march_rays(self, rays_o, rays_d):
         """nerfacc.ray_marching as called at models/neus.py:210-220."""
+        prev_grad = torch.is_grad_enabled()
         with torch.no_grad():
             if self.near_plane is None and self.far_plane is None:
                 t_min, t_max = ops.ray_aabb_intersect(rays_o, rays_d, self.scene_aabb)
@@ -309,24 +310,50 @@ class NeuSModel(nn.Module):
                 grid = dict(roi=g.roi, res=(g.res,) * 3, bits=g.bits)
             else:
                 grid = dict(roi=ops.UNBOUNDED_ROI, res=(1, 1, 1), bits=None)
+            before_read = None
+            if self.fused and self.training:
+                # the training step's weight preparation is enqueued while
+                # the march's sample count travels to the host, so the GPU
+                # runs it while the host sizes the outputs
+                grad_mode = prev_grad
+
+                def before_read():
+                    from . import fused
+                    with torch.set_grad_enabled(grad_mode):
+                        fused.prepare_ahead(self)
             ri, t0, t1, offsets, _ = ops.march(rays_o, rays_d, t_min, t_max, self.render_step_size,
                                                cone_angle=0.0, max_steps=self.max_march_steps,
-                                               max_samples_per_ray=self._samples_bound(), **grid)
+                                               max_samples_per_ray=self._samples_bound(),
+                                               before_read=before_read, **grid)
         self._last_march = (t_min, t_max)
-        self.last_num_samples = int(t0.shape[0])   # host-side, no device read
+        self._n_fg = int(t0.shape[0])   # host-side, no device read
         return ri, t0, t1, offsets
+
+    @property
+    def last_num_samples(self):
+        """Samples of the last forward as the reference counts them for its
+        dynamic ray count (num_samples_full, models/neus.py:275): the
+        foreground's plus the learned background's kept samples, known on
+        the host (None before the first forward)."""
+        n = self.__dict__.get("_n_fg")
+        return None if n is None else n + self.__dict__.get("_n_bg", 0)
 
     def forward_(self, rays):
         n_rays = rays.shape[0]
         rays_o, rays_d = rays[:, 0:3].contiguous(), rays[:, 3:6].contiguous()
-        if self.fused and self.training:
-            # weight preparation ahead of the march's host read of its count
-            from . import fused
-            fused.prepare_ahead(self)
+        bg_samples = None
+        self._n_bg = 0
+        if self.fused and self.learned_background:
+            # the background's kept samples first: its two host reads (its
+            # march's count, the kept count) then come before the foreground's
+            # march, and the GPU runs the foreground's VolumeSDF forward while
+            # the host enqueues the background's render and the loss
+            bg_samples = self._bg_samples(rays_o, rays_d)
         ri, t0, t1, offsets = self.march_rays(rays_o, rays_d)
         if self.fused:
             from . import fused
-            return fused.neus_forward(self, rays_o, rays_d, ri, t0, t1, offsets, n_rays)
+            return fused.neus_forward(self, rays_o, rays_d, ri, t0, t1, offsets, n_rays,
+                                      bg_samples=bg_samples)
         ray_indices = ri.long()
         t_origins = rays_o[ray_indices]
         t_dirs = rays_d[ray_indices]
@@ -373,12 +400,15 @@ class NeuSModel(nn.Module):
         self._bg_bound = (key, n + 4)
         return n + 4
 
-    def forward_bg_(self, rays_o, rays_d):
-        """The learned background (models/neus.py:141-203): marched from the
-        box exit (0.1 when the ray misses the box) to 1e3 through the
-        unbounded-sphere grid, samples of transmittance < 1e-4 dropped
-        (nerfacc's sigma_fn visibility test), weights from density."""
+    def _bg_samples(self, rays_o, rays_d):
+        """The learned background's kept samples (no autograd graph): marched
+        from the box exit (0.1 when the ray misses the box) to 1e3 through
+        the unbounded-sphere grid, samples of transmittance < 1e-4 dropped
+        (nerfacc's sigma_fn visibility test).  Returns (ray indices, t0, t1,
+        offsets, reuse, and for the fused form's reuse the contracted points,
+        the visibility pass's encodings and outputs and the kept rows)."""
         n_rays = rays_o.shape[0]
+        pts_c = X_all = out_all = kidx = None
         with torch.no_grad():
             _, t_exit = ops.ray_aabb_intersect(rays_o, rays_d, self.scene_aabb)
             near = torch.where(t_exit > 1e9, torch.full_like(t_exit, self.near_plane_bg), t_exit)
@@ -433,6 +463,17 @@ class NeuSModel(nn.Module):
                     pts_c, out_all = pts_c.index_select(0, kidx), out_all.index_select(0, kidx)
                 offsets = ops.offsets_from_ray_indices(ri, n_rays)
                 self._last_march_bg = (offsets, ri, t0, t1)
+        self._n_bg = int(t0.shape[0])
+        return ri, t0, t1, offsets, reuse, pts_c, X_all, out_all, kidx
+
+    def forward_bg_(self, rays_o, rays_d, samples=None):
+        """The learned background (models/neus.py:141-203): its kept samples
+        (``_bg_samples``, or the ones given), then density, colour and weights
+        from density."""
+        n_rays = rays_o.shape[0]
+        if samples is None:
+            samples = self._bg_samples(rays_o, rays_d)
+        ri, t0, t1, offsets, reuse, pts_c, X_all, out_all, kidx = samples
         ray_indices = ri.long()
         midpoints = ((t0 + t1) * 0.5)[:, None]
         intervals = (t1 - t0)[:, None]
@@ -472,22 +513,22 @@ class NeuSModel(nn.Module):
                         "intervals": intervals.view(-1), "ray_indices": ray_indices.view(-1)})
         return out
 
-    def background(self, out, comp_rgb, rays_o, rays_d):
-        """The background outputs: the learned background, or the constant
-        colour (models/neus.py:265-272)."""
+    def background(self, out, comp_rgb, rays_o, rays_d, samples=None):
+        """The background outputs: the learned background (on its kept
+        samples when given), or the constant colour (models/neus.py:265-272)."""
         if self.learned_background:
-            return self.forward_bg_(rays_o, rays_d)
+            return self.forward_bg_(rays_o, rays_d, samples)
         bg = self.background_color
         return {"comp_rgb": bg[None, :].expand(*comp_rgb.shape),
                 "num_samples": torch.zeros_like(out["num_samples"]),
                 "rays_valid": torch.zeros_like(out["rays_valid"])}
 
-    def _with_background(self, out, comp_rgb, rays_o=None, rays_d=None):
+    def _with_background(self, out, comp_rgb, rays_o=None, rays_d=None, bg_samples=None):
         bg = self.background_color
         if bg is None:
             raise RuntimeError("set model.background_color before rendering "
                                "(the reference's system sets it per batch)")
-        out_bg = self.background(out, comp_rgb, rays_o, rays_d)
+        out_bg = self.background(out, comp_rgb, rays_o, rays_d, bg_samples)
         out_full = {"comp_rgb": out["comp_rgb"] + out_bg["comp_rgb"] * (1.0 - out["opacity"]),
                     "num_samples": out["num_samples"] + out_bg["num_samples"],
                     "rays_valid": out["rays_valid"] | out_bg["rays_valid"]}

@@ -20,7 +20,16 @@ def _p(t):
     return _vp(t.data_ptr()) if t is not None else _vp(0)
 
 
+# the current stream's handle without constructing a torch Stream object (the
+# launches of a step follow one another from the host: a few microseconds
+# each that the GPU may wait for)
+_raw_stream = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+
+
 def _s(device=None):
+    if _raw_stream is not None and isinstance(device, torch.device) and device.type == "cuda" \
+            and device.index is not None:
+        return _vp(_raw_stream(device.index))
     return _vp(torch.cuda.current_stream(device).cuda_stream)
 
 
@@ -204,7 +213,7 @@ MARCH_SCRATCH_BYTES = 1 << 28   # single-march path while its scratch stays belo
 
 def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), bits=None,
           cone_angle=0.0, max_steps=1 << 20, max_samples_per_ray=None,
-          contraction=_lib.CONTRACT_AABB):
+          contraction=_lib.CONTRACT_AABB, before_read=None):
     """Occupancy-grid ray marching.  Returns (ray_indices int32 (S,),
     t_starts (S,), t_ends (S,), offsets int64 (R+1,), status): the sample
     count is read back to the host to size the outputs, as the reference
@@ -214,7 +223,12 @@ def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), 
     With max_samples_per_ray (a bound on every ray's sample count, e.g.
     ceil(ray length / step) + 2) each ray is marched once: its samples are
     recorded in a scratch buffer while counting and compacted after the scan;
-    a ray over the bound falls back to the second march (same samples)."""
+    a ray over the bound falls back to the second march (same samples).
+
+    before_read: a callable run after the count's copy to the host is
+    enqueued and before the host waits for it: work it enqueues (that does
+    not depend on the samples) runs on the GPU while the host sizes the
+    outputs."""
     rays_o = _cuda(rays_o, "rays_o", dims=2)
     rays_d = _cuda(rays_d, "rays_d", dims=2)
     t_min = _cuda(t_min, "t_min").reshape(-1)
@@ -241,12 +255,20 @@ def march(rays_o, rays_d, t_min, t_max, step, roi=UNBOUNDED_ROI, res=(1, 1, 1), 
              ctypes.byref(g), float(step), float(cone_angle), int(max_steps), _p(counts),
              _p(status), s)
     call("angelo_scan", _p(counts), n, _p(offsets), _p(ws), s, launches=3 if n else 0)
-    if single:
-        # the total and the record-overflow bit in one device read
-        total, flags = torch.cat([offsets[n:], status.to(torch.int64)]).tolist()
-        overflow = bool(flags & 4)
+    # the total (and, single-march, the record-overflow bit) in one device read
+    head = torch.cat([offsets[n:], status.to(torch.int64)]) if single else offsets[n:]
+    if before_read is None:
+        vals = head.tolist()
     else:
-        total, overflow = int(offsets[n].item()), False
+        host = torch.empty(head.numel(), dtype=torch.int64, pin_memory=True)
+        host.copy_(head, non_blocking=True)
+        copied = torch.cuda.Event()
+        copied.record()
+        before_read()
+        copied.synchronize()
+        vals = host.tolist()
+    total = vals[0]
+    overflow = single and bool(vals[1] & 4)
     ri = torch.empty(total, device=dev, dtype=torch.int32)
     t0 = torch.empty(total, device=dev)
     t1 = torch.empty(total, device=dev)

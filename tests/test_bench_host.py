@@ -58,3 +58,19 @@ def test_roofline_from_call_records():
     assert abs(rl["frac"] - rl["achieved"] / 6000.0) < 1e-4
     assert rl["traffic"] == int(bench.TRAFFIC_BYTES_PER_SAMPLE["angelo_sdf_stencil_bwd"] * 1000)
     assert list(shares) == ["angelo_sdf_stencil_bwd", "angelo_adamw_step"]
+
+
+def test_dynamic_ray_count_targets_and_counts_the_background():
+    """The learned-background form aims its dynamic ray count at the
+    reference's target with the background's samples
+    (train_num_rays * (num_samples_per_ray + num_samples_per_ray_bg),
+    systems/neus.py:28), and the count compared with it is the foreground's
+    plus the kept background samples (num_samples_full)."""
+    import torch
+    _, tr = bench.make_trainer("fused", torch.device("cpu"))
+    assert tr.train_num_samples == 1 << 18
+    m, tr = bench.make_trainer("fused_bg", torch.device("cpu"))
+    assert tr.train_num_samples == (1 << 18) * (512 + 256) // 512
+    assert m.last_num_samples is None
+    m._n_fg, m._n_bg = 1000, 250
+    assert m.last_num_samples == 1250
