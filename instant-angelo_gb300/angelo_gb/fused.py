@@ -560,6 +560,8 @@ def bg_visible(out, density_bias, ri, t0, t1, offsets, pts, eps=1e-4):
     the inputs, offsets); one device read (the kept count)."""
     n_rays = offsets.numel() - 1
     dev = t0.device
+    if t0.numel() >= 1 << 31:
+        raise ValueError("bg_visible: the kept rows are int32 indices (fewer than 2^31 samples)")
     kept = torch.empty(n_rays, dtype=torch.int32, device=dev)
     call("angelo_bg_visibility", _p(out), out.stride(0), float(density_bias), _p(t0), _p(t1), _p(offsets),
          n_rays, float(eps), _p(kept), _s(dev), units=dict(rays=n_rays))
