@@ -209,6 +209,37 @@ def test_march_single_pass_matches_oracle(dev, per_ray):
         assert int(st) & 4   # the bound was exceeded: second march used
 
 
+@pytest.mark.parametrize("per_ray", [None, 1200, 7])
+def test_march_count_read_through_event_matches(dev, per_ray):
+    """The training step's count read (a pinned copy and an event, with the
+    caller's work enqueued between them) gives the same samples, flags and
+    offsets as the plain read, and the caller's work runs before the outputs
+    are sized."""
+    from angelo_gb import ops
+    r = 1.0
+    o, d = _rays(2048, 24, 2.0)
+    aabb = np.array([-r, -r, -r, r, r, r], np.float32)
+    ot, dt = torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev)
+    tmin, tmax = ops.ray_aabb_intersect(ot, dt, torch.from_numpy(aabb).to(dev))
+    binary, words = _random_bits(128, 0.3, 25)
+    grid = dict(roi=aabb, res=(128, 128, 128), bits=torch.from_numpy(words.view(np.int32)).to(dev),
+                max_samples_per_ray=per_ray)
+    step = 1.732 * 2 * r / 1024
+    ref = ops.march(ot, dt, tmin, tmax, step, **grid)
+    side = torch.zeros(1 << 20, device=dev)
+    calls = []
+
+    def before_read():
+        calls.append(1)
+        side.add_(1.0)   # work on the stream between the copy and the wait
+
+    got = ops.march(ot, dt, tmin, tmax, step, before_read=before_read, **grid)
+    assert calls == [1] and float(side[-1]) == 1.0
+    for a, b in zip(ref[:4], got[:4]):
+        assert torch.equal(a, b)
+    assert int(ref[4]) == int(got[4])
+
+
 def test_march_without_grid_between_planes(dev):
     """Config-1 style: no grid, samples between near 0.5 and far 4.5, dt 1/32."""
     from angelo_gb import ops
